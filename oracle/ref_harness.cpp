@@ -1,0 +1,299 @@
+// Test infrastructure, not product code: a driver that links the reference solver's
+// own, unmodified hot-path sources (compiled from the reference tree by
+// oracle/build_ref.sh into oracle/_ref) and runs its fluid Newton loop on a mesh
+// built in code, so that the CPU restatement and the GPU kernels can be checked
+// against the reference itself.
+//
+// The loop follows iterate_solution (Code/Source/solver/main.cpp:292-762) for a single
+// fluid equation:
+//   picp (pic.cpp:591) -> strong Dirichlet values -> Newton loop:
+//     pici (pic.cpp:486) -> ls_alloc (ls.cpp:51) -> global_eq_assem (eq_assem.cpp:377,
+//     construct_fluid fluid.cpp:464) -> outlet Neumann/backflow b_assem_neu_bc
+//     (eq_assem.cpp:58) -> ls_solve (ls.cpp:69 -> fsils_solve solve.cpp:50) -> picc
+//     (pic.cpp:74)
+//   -> Ao = An, Yo = Yn (main.cpp:752-757).
+// Dirichlet values are written directly (the role of set_bc_dir, set_bc.cpp:794): the
+// inlet gets u_z = u_c(t) * profile, walls get zero velocity; acceleration on the
+// inlet is du_c/dt * profile (the Fourier branch of set_bc_dir_l, set_bc.cpp:1033).
+//
+// Input: a case directory written by tests/golden/make_golden.py (raw little-endian
+// arrays + params.txt).  Output: raw arrays for the requested step/iteration.
+#include "Simulation.h"
+#include "ComMod.h"
+#include "eq_assem.h"
+#include "fluid.h"
+#include "fs.h"
+#include "lhsa.h"
+#include "ls.h"
+#include "nn.h"
+#include "pic.h"
+#include "FsilsLinearAlgebra.h"
+#include "fsils_api.hpp"
+#include "commu.h"
+#include "lhs.h"
+
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <chrono>
+
+static std::map<std::string, std::string> read_params(const std::string& dir) {
+  std::map<std::string, std::string> p;
+  std::ifstream f(dir + "/params.txt");
+  std::string line;
+  while (std::getline(f, line)) {
+    auto eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    p[line.substr(0, eq)] = line.substr(eq + 1);
+  }
+  return p;
+}
+
+template <typename T>
+static std::vector<T> read_raw(const std::string& path) {
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  size_t n = f.tellg();
+  f.seekg(0);
+  std::vector<T> v(n / sizeof(T));
+  f.read(reinterpret_cast<char*>(v.data()), n);
+  return v;
+}
+
+template <typename T>
+static void write_raw(const std::string& path, const T* p, size_t n) {
+  std::ofstream f(path, std::ios::binary);
+  f.write(reinterpret_cast<const char*>(p), n * sizeof(T));
+}
+
+static void setup_face(faceType& fa, const std::string& dir, const std::string& name) {
+  auto ien = read_raw<int>(dir + "/" + name + "_ien.bin");
+  auto gE = read_raw<int>(dir + "/" + name + "_gE.bin");
+  auto gN = read_raw<int>(dir + "/" + name + "_gN.bin");
+  fa.name = name;
+  fa.iM = 0;
+  fa.eNoN = 3;
+  fa.nEl = (int)gE.size();
+  fa.gnEl = fa.nEl;
+  fa.nNo = (int)gN.size();
+  fa.IEN.resize(3, fa.nEl);
+  for (int e = 0; e < fa.nEl; e++)
+    for (int a = 0; a < 3; a++) fa.IEN(a, e) = ien[3 * e + a];
+  fa.gE.resize(fa.nEl);
+  for (int e = 0; e < fa.nEl; e++) fa.gE(e) = gE[e];
+  fa.gN.resize(fa.nNo);
+  for (int a = 0; a < fa.nNo; a++) fa.gN(a) = gN[a];
+  fa.eType = consts::ElementType::TRI3;
+  fa.nG = 3;
+  fa.w.resize(fa.nG);
+  fa.xi.resize(2, fa.nG);
+  fa.N.resize(3, fa.nG);
+  fa.Nx.resize(2, 3, fa.nG);
+  nn::get_gip(nullptr, fa);
+  for (int g = 0; g < fa.nG; g++) nn::get_gnn(nullptr, g, fa);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::fprintf(stderr, "usage: %s CASE_DIR OUT_DIR\n", argv[0]);
+    return 2;
+  }
+  std::string dir = argv[1], out = argv[2];
+  auto P = read_params(dir);
+  auto getd = [&](const char* k) { return std::stod(P.at(k)); };
+  auto geti = [&](const char* k) { return std::stoi(P.at(k)); };
+
+  Simulation sim;
+  auto& com = sim.com_mod;
+  auto xs = read_raw<double>(dir + "/x.bin");
+  auto iens = read_raw<int>(dir + "/ien.bin");
+  const int nNo = (int)xs.size() / 3;
+  const int nEl = (int)iens.size() / 4;
+
+  com.nsd = 3;
+  com.nsymd = 6;
+  com.tnNo = nNo;
+  com.gtnNo = nNo;
+  com.nMsh = 1;
+  com.msh.resize(1);
+  com.nEq = 1;
+  com.eq.resize(1);
+  com.dt = getd("dt");
+  com.mvMsh = false;
+  com.dFlag = false;
+  com.sstEq = false;
+  com.pstEq = false;
+
+  auto& msh = com.msh[0];
+  msh.name = "pipe";
+  msh.eNoN = 4;
+  msh.nEl = nEl;
+  msh.gnEl = nEl;
+  msh.nNo = nNo;
+  msh.gnNo = nNo;
+  msh.IEN.resize(4, nEl);
+  for (int e = 0; e < nEl; e++)
+    for (int a = 0; a < 4; a++) msh.IEN(a, e) = iens[4 * e + a];
+  msh.gN.resize(nNo);
+  for (int a = 0; a < nNo; a++) msh.gN(a) = a;
+  nn::select_ele(com, msh);
+  msh.nFs = 1;
+  fs::init_fs_msh(com, msh);
+  msh.fa.resize(3);
+  msh.nFa = 3;
+  setup_face(msh.fa[0], dir, "inlet");
+  setup_face(msh.fa[1], dir, "wall");
+  setup_face(msh.fa[2], dir, "outlet");
+
+  com.x.resize(3, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < 3; i++) com.x(i, a) = xs[3 * a + i];
+  com.Bf.resize(3, nNo);
+
+  // Equation: fluid, dof = nsd + 1 (initialize.cpp:426-465 for the gen-alpha constants)
+  auto& eq = com.eq[0];
+  eq.phys = consts::EquationType::phys_fluid;
+  eq.sym = "NS";
+  eq.dof = 4;
+  eq.roInf = getd("rho_inf");
+  eq.am = 0.5 * (3.0 - eq.roInf) / (1.0 + eq.roInf);
+  eq.af = 1.0 / (1.0 + eq.roInf);
+  eq.beta = 0.25 * std::pow((1.0 + eq.am - eq.af), 2.0);
+  eq.gam = 0.5 + eq.am - eq.af;
+  eq.pNorm = std::numeric_limits<double>::max();
+  eq.s = 0;
+  eq.e = 3;
+  eq.minItr = geti("newton_min");
+  eq.maxItr = geti("newton_max");
+  eq.tol = getd("newton_tol");
+  eq.nDmn = 1;
+  eq.dmn.resize(1);
+  auto& dmn = eq.dmn[0];
+  dmn.Id = -1;
+  dmn.phys = consts::EquationType::phys_fluid;
+  using PP = consts::PhysicalProperyType;
+  dmn.prop[PP::fluid_density] = getd("rho");
+  dmn.prop[PP::f_x] = 0.0;
+  dmn.prop[PP::f_y] = 0.0;
+  dmn.prop[PP::f_z] = 0.0;
+  dmn.prop[PP::backflow_stab] = getd("backflow_beta");
+  dmn.prop[PP::inverse_darcy_permeability] = 0.0;
+  dmn.fluid_visc.viscType = consts::FluidViscosityModelType::viscType_Const;
+  dmn.fluid_visc.mu_i = getd("mu");
+  com.tDof = 4;
+  com.dof = 4;
+
+  com.Ao.resize(4, nNo); com.An.resize(4, nNo);
+  com.Yo.resize(4, nNo); com.Yn.resize(4, nNo);
+  com.Do.resize(4, nNo); com.Dn.resize(4, nNo);
+  Array<double> Ag(4, nNo), Yg(4, nNo), Dg(4, nNo);
+
+  // CSR pattern (lhsa.cpp:153) and FSILS handles (initialize.cpp:571-574, baf_ini.cpp:719-744)
+  int nnz = 0;
+  lhsa_ns::lhsa(&sim, nnz);
+  com.lhs.nnz = nnz;
+  fsi_linear_solver::FSILS_commuType commu;
+  fsi_linear_solver::fsils_commu_create(commu, MPI_COMM_WORLD);
+  Vector<int> gNodes(nNo);
+  for (int a = 0; a < nNo; a++) gNodes(a) = a;
+  const int nFacesLS = 2;
+  fsi_linear_solver::fsils_lhs_create(com.lhs, commu, nNo, nNo, nnz, gNodes, com.rowPtr, com.colPtr, nFacesLS);
+  for (int f = 0; f < 2; f++) {
+    auto& fa = msh.fa[f];
+    Array<double> sVl(3, fa.nNo);  // zero: velocity rows/cols removed (baf_ini.cpp:724-742)
+    Vector<int> gN(fa.nNo);
+    for (int a = 0; a < fa.nNo; a++) gN(a) = fa.gN(a);
+    fsi_linear_solver::fsils_bc_create(com.lhs, f, fa.nNo, 3, fsi_linear_solver::BcType::BC_TYPE_Dir, gN, sVl);
+  }
+  fsi_linear_solver::fsils_ls_create(eq.FSILS, fsi_linear_solver::LinearSolverType::LS_TYPE_GMRES,
+                                     getd("ls_rel_tol"), getd("ls_abs_tol"), geti("ls_max_itr"), geti("ls_krylov_dim"));
+  FsilsLinearAlgebra fsils_la;
+  eq.linear_algebra = &fsils_la;
+  eq.linear_algebra_preconditioner = consts::PreconditionerType::PREC_FSILS;
+
+  auto prof = read_raw<double>(dir + "/inlet_prof.bin");
+  const double u_mean = getd("u_mean"), u_amp = getd("u_amp"), freq = getd("u_freq");
+  const int nSteps = geti("n_steps");
+  const int dump_step = geti("dump_step");
+  const int dump_iter = geti("dump_iter");
+  Vector<int> incL(nFacesLS);
+  Vector<double> res(nFacesLS);
+  Vector<double> hg(nNo);
+
+  std::ofstream log(out + "/log.txt");
+  log.precision(17);
+  double time = 0.0;
+  double t_asm = 0.0, t_solve = 0.0;
+  auto wall0 = std::chrono::steady_clock::now();
+  for (int cTS = 1; cTS <= nSteps; cTS++) {
+    time += com.dt;
+    com.cTS = cTS;
+    com.time = time;
+    com.cEq = 0;
+    eq.itr = 0;
+    eq.ok = false;
+    pic::picp(&sim);
+    // strong Dirichlet values
+    const double w = 2.0 * M_PI * freq;
+    const double uc = u_mean + u_amp * std::sin(w * time);
+    const double duc = u_amp * w * std::cos(w * time);
+    for (int f = 1; f >= 0; f--) {  // wall first, inlet last: the inlet profile is 0 on the wall ring
+      auto& fa = msh.fa[f];
+      for (int a = 0; a < fa.nNo; a++) {
+        int Ac = fa.gN(a);
+        for (int i = 0; i < 3; i++) { com.An(i, Ac) = 0.0; com.Yn(i, Ac) = 0.0; }
+        if (f == 0) {
+          com.An(2, Ac) = duc * prof[a];
+          com.Yn(2, Ac) = uc * prof[a];
+        }
+      }
+    }
+    int inner = 1;
+    while (true) {
+      pic::pici(&sim, Ag, Yg, Dg);
+      ls_ns::ls_alloc(com, eq);
+      auto t0 = std::chrono::steady_clock::now();
+      eq_assem::global_eq_assem(com, sim.get_cep_mod(), msh, Ag, Yg, Dg);
+      hg = 0.0;
+      eq_assem::b_assem_neu_bc(com, msh.fa[2], hg, Yg);
+      auto t1 = std::chrono::steady_clock::now();
+      incL = 1;
+      res = 0.0;
+      if (cTS == dump_step && inner == dump_iter) {
+        write_raw(out + "/R_asm.bin", com.R.data(), (size_t)com.R.size());
+        write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
+        write_raw(out + "/Ag.bin", Ag.data(), (size_t)Ag.size());
+        write_raw(out + "/Yg.bin", Yg.data(), (size_t)Yg.size());
+        write_raw(out + "/rowPtr.bin", com.rowPtr.data(), (size_t)com.rowPtr.size());
+        write_raw(out + "/colPtr.bin", com.colPtr.data(), (size_t)com.colPtr.size());
+      }
+      ls_ns::ls_solve(com, eq, incL, res);
+      auto t2 = std::chrono::steady_clock::now();
+      t_asm += std::chrono::duration<double>(t1 - t0).count();
+      t_solve += std::chrono::duration<double>(t2 - t1).count();
+      auto& RI = eq.FSILS.RI;
+      log << "step " << cTS << " iter " << inner << " iNorm " << RI.iNorm << " fNorm " << RI.fNorm
+          << " itr " << RI.itr << " suc " << RI.suc << "\n";
+      if (cTS == dump_step && inner == dump_iter) {
+        write_raw(out + "/dX.bin", com.R.data(), (size_t)com.R.size());
+        write_raw(out + "/Val_scaled.bin", com.Val.data(), (size_t)com.Val.size());
+      }
+      pic::picc(&sim);
+      bool all_ok = true;
+      for (auto& e : com.eq) all_ok = all_ok && e.ok;
+      if (all_ok) break;
+      inner++;
+    }
+    write_raw(out + "/An_" + std::to_string(cTS) + ".bin", com.An.data(), (size_t)com.An.size());
+    write_raw(out + "/Yn_" + std::to_string(cTS) + ".bin", com.Yn.data(), (size_t)com.Yn.size());
+    com.Ao = com.An;
+    com.Yo = com.Yn;
+  }
+  double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+  log << "timing steps " << nSteps << " wall_s " << wall << " assembly_s " << t_asm << " solve_s " << t_solve << "\n";
+  return 0;
+}

@@ -1,0 +1,112 @@
+/* CPU oracle of the svMultiPhysics fluid Newton-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the checker the GPU kernels are compared with and
+ * the CPU baseline timed beside them.  The GPU product never links or calls it.
+ *
+ * A plain-C restatement of the reference's FP64 algorithm, each function citing the
+ * reference file:line it follows (paths relative to Code/Source/).  It is pinned
+ * against golden vectors produced by running the reference solver itself
+ * (tests/golden/ref_*.npz, see tests/golden/make_golden.py).
+ *
+ * Layouts follow the reference's column-major Array<T> (solver/Array.h:374-388):
+ *   x   (3, nNo)   x[3*a + i]            Ag, Yg, An, ... (4, nNo)  v[4*a + i]
+ *   IEN (4, nEl)   ien[4*e + a]          R  (dof, nNo)  R[dof*a + i]
+ *   Val (dof*dof, nnz) Val[dof*dof*k + r*dof + c]  (block row-major, spar_mul.cpp:228-236)
+ *   rowPtr (nNo+1), colPtr (nnz): 0-based CSR with sorted columns (lhsa.cpp:366-379)
+ */
+#ifndef SVORACLE_H
+#define SVORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  double rho, mu, fx, fy, fz;     /* fluid density, constant viscosity, body force */
+  double k_inv_darcy;             /* Brinkman inverse permeability (0 = plain NS) */
+  double backflow_beta;           /* backflow stabilisation coefficient */
+  double dt, am, af, gam, beta;   /* time step and generalised-alpha constants */
+} or_fluid_params;
+
+/* generalised-alpha constants of a first-order equation (initialize.cpp:426-465) */
+void or_genalpha_first_order(double rho_inf, double* am, double* af, double* gam, double* beta);
+
+/* CSR pattern of the element cliques: returns nnz; rowPtr must hold nNo+1 ints and
+ * colPtr at least the returned count (call once with colPtr=NULL to size it).
+ * Follows lhsa (lhsa.cpp:153-380) without the undefNeu remap. */
+long or_lhsa(int nNo, int nEl, int eNoN, const int* ien, int* rowPtr, int* colPtr);
+
+/* Element residual lR (4,4) and tangent lK (16,4,4) of one P1 VMS fluid tet:
+ * construct_fluid's per-element body (fluid.cpp:527-700) with gnn (nn.cpp:455-550),
+ * fluid_3d_m (fluid.cpp:1697-2139) and fluid_3d_c (fluid.cpp:1389-1689).
+ * xl (3,4), al (4,4), yl (4,4), bfl (3,4). Returns 0, or -1 on a zero Jacobian. */
+int or_fluid_element(const or_fluid_params* p, const double* xl, const double* al,
+                     const double* yl, const double* bfl, double* lR, double* lK);
+
+/* construct_fluid + do_assem (lhsa.cpp:97-141) over all elements: adds into R (4,nNo)
+ * and Val (16,nnz).  Returns -1 - e for a zero Jacobian in element e, else 0. */
+int or_construct_fluid(const or_fluid_params* p, int nNo, int nEl, const int* ien,
+                       const double* x, const double* Ag, const double* Yg, const double* Bf,
+                       const int* rowPtr, const int* colPtr, double* R, double* Val);
+
+/* Outlet Neumann (value h on every face node, 0 for traction-free) with backflow
+ * stabilisation: b_assem_neu_bc (eq_assem.cpp:58-172) -> b_fluid (fluid.cpp:46-133)
+ * with the outward normal of gnnb (nn.cpp:552-760) and TRI3 quadrature
+ * (nn_elem_gip.h:747-764).  fien (3,nFa), gE (nFa) owner tets. */
+void or_neu_backflow(const or_fluid_params* p, int nFa, const int* fien, const int* gE,
+                     const int* ien, const double* x, const double* Yg, double h,
+                     const int* rowPtr, const int* colPtr, double* R, double* Val);
+
+typedef struct {
+  int sD, mItr;            /* Krylov dimension, restart cycles */
+  double relTol, absTol;
+  /* outputs, the reference's FSILS_subLsType fields (fils_struct.hpp:211-257) */
+  double iNorm, fNorm, dB;
+  int itr, suc;
+} or_ls;
+
+/* fsils_solve (solve.cpp:50-193) for GMRES + FSILS diagonal preconditioning with
+ * one rank: precond_diag (precond.cpp:122-257), gmres_v (gmres.cpp:450-629),
+ * R <- Wc * R.  dirMask (dof, nNo): 1 keeps a dof, 0 removes it (the product of the
+ * Dirichlet faces' val, bc.cpp:74-95).  R in: residual, out: increment.  Val is
+ * overwritten by its scaled copy, as in the reference. */
+void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
+                          double* Val, double* R, const double* dirMask, or_ls* ls);
+
+/* Block SpMV KU = K U (spar_mul.cpp:191-258, any dof). */
+void or_spar_mul(int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
+                 const double* U, double* KU);
+
+/* One fluid time step through the reference's Newton loop (main.cpp:292-762 with
+ * picp pic.cpp:591, pici :486, picc :74), strong Dirichlet values given per node.
+ * State arrays (4, nNo). dirNodes: node ids whose velocity is prescribed, dirY/dirA
+ * their (3, nDir) velocity / acceleration. Returns the number of Newton iterations;
+ * per-iteration solver stats go to stats[5*it + {iNorm,fNorm,itr,suc,dB}] when
+ * stats != NULL (room for maxItr entries). */
+typedef struct {
+  int nNo, nEl, nFa;
+  const int* ien;
+  const double* x;
+  const int *fien, *fgE;          /* outlet faces */
+  const int *rowPtr, *colPtr;
+  long nnz;
+  int nDir;
+  const int* dirNodes;
+  const double* dirMask;          /* (4, nNo) */
+  int minItr, maxItr;
+  double tol;
+} or_fluid_problem;
+
+typedef struct {
+  double iNorm, pNorm;            /* eqType::iNorm, pNorm (persist across steps) */
+  double t_assembly, t_solve;     /* accumulated seconds */
+} or_newton_state;
+
+int or_fluid_step(const or_fluid_problem* pb, const or_fluid_params* p, or_ls* ls,
+                  or_newton_state* ns, const double* dirY, const double* dirA,
+                  double* Ao, double* Yo, double* Do, double* An, double* Yn, double* Dn,
+                  double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

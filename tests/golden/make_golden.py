@@ -1,0 +1,107 @@
+"""Generate the golden fixtures by running the reference solver itself.
+
+The reference's own fluid hot path (construct_fluid, b_assem_neu_bc, fsils_solve,
+pic*) is compiled from the reference tree by ``oracle/build_ref.sh`` into
+``oracle/_ref/ref_harness``; this script writes a procedural pipe case for it, runs
+it, and stores what it produced as compressed ``.npz`` fixtures next to this file.
+It needs the reference tree and is run only where that exists; the fixtures are
+committed so the tests do not need it.
+
+Usage: python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from svfsiplus_gb300.mesh import named_pipe  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# Physics and solver settings of the pipe cases (fluid rho=1.06, mu=0.04, backflow 0.2,
+# gen-alpha rho_inf=0.5, dt=1e-3, GMRES + diagonal preconditioner).
+BASE = dict(rho=1.06, mu=0.04, backflow_beta=0.2, dt=1e-3, rho_inf=0.5,
+            ls_rel_tol=1e-8, ls_abs_tol=1e-17, ls_max_itr=100, ls_krylov_dim=50,
+            newton_min=3, newton_max=3, newton_tol=1e-11,
+            u_mean=10.0, u_amp=0.0, u_freq=1.0)
+
+CASES = {
+    # element-level assembly + one solve on a tiny pipe: Val/R committed in full
+    "tiny": dict(mesh="tiny", n_steps=2, dump_step=2, dump_iter=2),
+    "small": dict(mesh="small", n_steps=3, dump_step=1, dump_iter=1, u_amp=5.0),
+    # the CPU-runnable 50k-tet pipe, 10 time steps, fields after every step
+    "pipe50k": dict(mesh="pipe50k", n_steps=10, dump_step=1, dump_iter=1),
+}
+
+
+def write_case(mesh, d, params):
+    os.makedirs(d, exist_ok=True)
+    mesh.x.astype(np.float64).tofile(os.path.join(d, "x.bin"))
+    mesh.ien.astype(np.int32).tofile(os.path.join(d, "ien.bin"))
+    for name, f in mesh.faces.items():
+        f.ien.astype(np.int32).tofile(os.path.join(d, f"{name}_ien.bin"))
+        f.gE.astype(np.int32).tofile(os.path.join(d, f"{name}_gE.bin"))
+        f.gN.astype(np.int32).tofile(os.path.join(d, f"{name}_gN.bin"))
+    mesh.inlet_profile.astype(np.float64).tofile(os.path.join(d, "inlet_prof.bin"))
+    with open(os.path.join(d, "params.txt"), "w") as fh:
+        for k, v in params.items():
+            fh.write(f"{k}={v!r}\n" if isinstance(v, float) else f"{k}={v}\n")
+
+
+def run_case(name):
+    spec = dict(CASES[name])
+    mesh = named_pipe(spec.pop("mesh"))
+    params = dict(BASE)
+    params.update(spec)
+    tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        cdir, odir = os.path.join(tmp, "case"), os.path.join(tmp, "out")
+        write_case(mesh, cdir, params)
+        os.makedirs(odir)
+        subprocess.run([HARNESS, cdir, odir], check=True)
+        nNo = mesh.nNo
+        out = {"params": np.array(repr(params))}
+        with open(os.path.join(odir, "log.txt")) as fh:
+            log = fh.read()
+        out["log"] = np.array(log)
+        its = []
+        for line in log.splitlines():
+            t = line.split()
+            if t[0] == "step":
+                its.append([int(t[1]), int(t[3]), float(t[5]), float(t[7]), int(t[9]), int(t[11])])
+        out["newton_log"] = np.array(its, dtype=np.float64)
+        rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
+        out["rowPtr"] = rd("rowPtr.bin", np.int32)
+        out["colPtr"] = rd("colPtr.bin", np.int32)
+        out["Ag"] = rd("Ag.bin", np.float64).reshape(nNo, 4)
+        out["Yg"] = rd("Yg.bin", np.float64).reshape(nNo, 4)
+        out["R_asm"] = rd("R_asm.bin", np.float64).reshape(nNo, 4)
+        out["dX"] = rd("dX.bin", np.float64).reshape(nNo, 4)
+        nnz = out["colPtr"].size
+        if name != "pipe50k":
+            out["Val_asm"] = rd("Val_asm.bin", np.float64).reshape(nnz, 16)
+        for s in range(1, params["n_steps"] + 1):
+            if name != "pipe50k" or s in (1, 10):
+                out[f"Yn_{s}"] = rd(f"Yn_{s}.bin", np.float64).reshape(nNo, 4)
+                out[f"An_{s}"] = rd(f"An_{s}.bin", np.float64).reshape(nNo, 4)
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+        print(name, "nNo", nNo, "nEl", mesh.nEl, "nnz", nnz)
+        print(log.strip().splitlines()[-1])
+    finally:
+        shutil.rmtree(tmp)
+
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: oracle/build_ref.sh")
+    for n in (sys.argv[1:] or list(CASES)):
+        run_case(n)
