@@ -1,0 +1,146 @@
+/*
+ * svgpu -- GB300 (sm_103a) implementation of the svMultiPhysics Newton-step hot path.
+ *
+ * C ABI: plain pointers and sizes.  Every array argument may be a host pointer or a
+ * CUDA device pointer; the library tells them apart with cudaPointerGetAttributes
+ * and copies host arrays through its own device buffers.  Array layouts are the
+ * reference's column-major Array<T> (solver/Array.h:374-388):
+ *   x (3,nNo), Ag/Yg/An/... (tDof,nNo), R (dof,nNo), Val (dof*dof,nnz) with block k
+ *   row-major (Val[dof*dof*k + r*dof + c]), IEN (eNoN,nEl), 0-based CSR rowPtr (nNo+1),
+ *   colPtr (nnz) with sorted columns (lhsa.cpp:366-379).
+ * Functions return SVGPU_OK (0) or a negative status; svgpu_last_error() gives text.
+ * A context is bound to one GPU and one CUDA stream; calls on one context are not
+ * thread-safe (the reference's FSILS handles are not either).
+ */
+#ifndef SVGPU_H
+#define SVGPU_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum svgpu_status {
+  SVGPU_OK = 0,
+  SVGPU_EINVAL = -1,   /* bad argument (replaces the reference's std::runtime_error) */
+  SVGPU_ECUDA = -2,    /* CUDA runtime error */
+  SVGPU_EJAC = -3,     /* zero element Jacobian (fluid.cpp:612-614) */
+  SVGPU_ESTATE = -4,   /* call order: e.g. solve before svgpu_lhs_create */
+  SVGPU_ENAN = -5,     /* non-finite residual or Krylov breakdown */
+  SVGPU_ENOMEM = -6
+};
+
+/* reference enums kept with their meaning (fils_struct.hpp:40-76, consts.h) */
+enum svgpu_bc_type { SVGPU_BC_DIR = 0, SVGPU_BC_NEU = 1 };            /* BcType */
+enum svgpu_ls_type { SVGPU_LS_GMRES = 2, SVGPU_LS_CG = 3, SVGPU_LS_FGMRES_LEARNED = 100 };
+enum svgpu_prec_type { SVGPU_PREC_NONE = 0, SVGPU_PREC_FSILS = 1 };  /* PreconditionerType */
+enum svgpu_precision { SVGPU_FP64 = 0, SVGPU_MIXED = 1 };
+
+typedef struct svgpu_ctx svgpu_ctx;
+
+/* Output of one solve: the reference's FSILS_subLsType results (fils_struct.hpp:211-257). */
+typedef struct {
+  double iNorm;      /* preconditioned initial residual norm (RI.iNorm) */
+  double fNorm;      /* final residual estimate (RI.fNorm) */
+  double dB;         /* 10 log(fNorm / dB-at-last-restart) (RI.dB) */
+  double callD;      /* seconds spent in the solve (RI.callD) */
+  int itr;           /* Krylov iterations incl. restarts (RI.itr) */
+  int suc;           /* converged (RI.suc) */
+  double true_rel;   /* ||R - K dX|| / ||R|| of the unpreconditioned FP64 system (not in the reference) */
+} svgpu_ls_stats;
+
+/* Physical properties of a fluid domain: dmnType::prop (ComMod.h:431-462) with a
+ * constant viscosity (get_viscosity, fluid.cpp:2142-2160), plus the equation's
+ * generalised-alpha constants (eqType am/af/gam/beta, initialize.cpp:426-465). */
+typedef struct {
+  double rho, mu;
+  double f[3];               /* body force per unit mass (f_x, f_y, f_z) */
+  double k_inv_darcy;        /* Brinkman inverse permeability, 0 for plain NS */
+  double backflow_beta;      /* backflow_stab */
+  double dt, am, af, gam, beta;
+} svgpu_fluid_props;
+
+/* ---- context ------------------------------------------------------------------- */
+int svgpu_create(svgpu_ctx** ctx, int device);
+int svgpu_destroy(svgpu_ctx* ctx);
+const char* svgpu_last_error(const svgpu_ctx* ctx);
+/* Kernels this library launched on the context so far (a counter). */
+long long svgpu_kernel_launches(const svgpu_ctx* ctx);
+/* Use a caller-owned cudaStream_t (passed as void*) instead of the context's own. */
+int svgpu_set_stream(svgpu_ctx* ctx, void* stream);
+
+/* ---- FSILS set-up (Code/Source/liner_solver/fsils_api.hpp:41-61) --------------- */
+/* Replaces fsils_lhs_create (liner_solver/lhs.cpp:57) for one rank: gnNo == nNo,
+ * gNodes the identity.  Keeps rowPtr/colPtr, derives diagPtr. */
+int svgpu_lhs_create(svgpu_ctx* ctx, int gnNo, int nNo, int nnz, const int* gNodes,
+                     const int* rowPtr, const int* colPtr, int nFaces);
+/* Replaces fsils_bc_create (liner_solver/bc.cpp:45): face faIn with nNo nodes gNodes,
+ * dof values per node (val (dof,nNo); NULL means all zero). For SVGPU_BC_DIR the val
+ * entries multiply the diagonal scaling W (precond.cpp:204-225). */
+int svgpu_bc_create(svgpu_ctx* ctx, int faIn, int nNo, int dof, int bcType,
+                    const int* gNodes, const double* val);
+/* Replaces fsils_ls_create (liner_solver/ls.cpp:40) for GMRES/CG: relTol, absTol,
+ * maxItr (restart cycles), dimKry (Krylov dimension).  Pass a negative value to keep
+ * the reference default (GMRES: 0.1, 1e-10, 4, 250; CG: 1e-2, 1e-10, 1000). */
+int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, int maxItr, int dimKry);
+
+/* ---- solve --------------------------------------------------------------------- */
+/* Replaces fsils_solve (liner_solver/solve.cpp:50).  Ri (dof,nNo): in the residual,
+ * out the increment.  Val (dof*dof,nnz) is scaled in place by the preconditioner, as
+ * in the reference.  incL (nFaces): 0 switches a face off; res (nFaces): coupled
+ * resistances (must be 0: coupled Neumann faces are not supported yet).
+ * Ri == NULL and Val == NULL solve the system resident in the context (the one the
+ * svgpu_construct_* calls assembled) and leave the increment there. */
+int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec,
+                      const int* incL, const double* res, svgpu_ls_stats* stats);
+
+/* Block SpMV KU = K U for any dof (fsils_spar_mul_vv, spar_mul.cpp:191-258). */
+int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, double* KU);
+
+/* ---- mesh and assembly ----------------------------------------------------------- */
+/* Volume mesh: linear tets, IEN (4,nEl), x (3,nNo).  Builds the element colouring
+ * used by the race-free scatter.  Equivalent state: mshType IEN/x (ComMod.h:831). */
+int svgpu_mesh_create(svgpu_ctx* ctx, int nNo, int nEl, int eNoN, const int* IEN, const double* x);
+/* Boundary face (faceType, ComMod.h:520): TRI3 connectivity fIEN (3,nFaEl) and owner
+ * tets gE (nFaEl).  faceId is the caller's handle. */
+int svgpu_face_create(svgpu_ctx* ctx, int faceId, int nFaEl, const int* fIEN, const int* gE);
+
+/* Replaces construct_fluid (solver/fluid.cpp:464) + do_assem (lhsa.cpp:97) for P1
+ * VMS tets: adds the element residuals and tangents into R (4,nNo) and Val (16,nnz).
+ * Ag, Yg (4,nNo); Bf (3,nNo) or NULL.  R == NULL and Val == NULL assemble into the
+ * context's resident system (zeroed first, like ls_alloc, ls.cpp:51).
+ * precision SVGPU_FP64 or SVGPU_MIXED (FP32 element integrals and tangent).
+ * Returns SVGPU_EJAC for a zero Jacobian. */
+int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag,
+                          const double* Yg, const double* Bf, double* R, double* Val, int precision);
+/* Replaces b_assem_neu_bc (solver/eq_assem.cpp:58) -> b_fluid (fluid.cpp:46) on one
+ * face: Neumann value h on every face node plus backflow stabilisation. */
+int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h,
+                       const double* Yg, double* R, double* Val);
+
+/* ---- Newton time step (solver/main.cpp:292-762 for one fluid equation) ----------- */
+typedef struct {
+  int minItr, maxItr;        /* eqType minItr / maxItr */
+  double tol;                /* eqType tol */
+  int precision;             /* SVGPU_FP64 or SVGPU_MIXED */
+  int outletFace;            /* face id of the traction-free outlet, -1 for none */
+  double outletH;            /* Neumann value on it */
+} svgpu_newton_opts;
+
+/* Strong-Dirichlet node set (the velocity rows removed by the Dirichlet faces). */
+int svgpu_set_dirichlet(svgpu_ctx* ctx, int nDir, const int* nodes);
+
+/* One time step: picp (pic.cpp:591) + strong Dirichlet values dirY/dirA (3,nDir) +
+ * Newton loop [pici (pic.cpp:486), construct_fluid, Neumann/backflow, fsils_solve,
+ * picc (pic.cpp:74)].  Ao,Yo,Do (4,nNo) in; An,Yn,Dn (4,nNo) out.  iNorm/pNorm carry
+ * the equation's eqType::iNorm / pNorm across steps (in/out).  stats receives one
+ * entry per Newton iteration (room for maxItr); returns the Newton iteration count or
+ * a negative status. */
+int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu_newton_opts* opts,
+                     const double* dirY, const double* dirA,
+                     const double* Ao, const double* Yo, const double* Do,
+                     double* An, double* Yn, double* Dn,
+                     double* iNorm, double* pNorm, svgpu_ls_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,265 @@
+"""Python mirror of the reference interface over the svgpu C ABI (include/svgpu.h).
+
+Names, argument meaning and error behaviour follow the reference:
+``fsils_lhs_create`` (liner_solver/lhs.cpp:57), ``fsils_bc_create`` (bc.cpp:45),
+``fsils_ls_create`` (ls.cpp:40), ``fsils_solve`` (solve.cpp:50), ``construct_fluid``
+(solver/fluid.cpp:464), ``b_assem_neu_bc`` (eq_assem.cpp:58) and one fluid time step
+of ``iterate_solution`` (main.cpp:292-762).  Errors raise ``RuntimeError`` with the
+library's message, as the reference throws ``std::runtime_error``.
+
+Arrays are numpy (host) or torch CUDA tensors (device); the library accepts either.
+Layouts: node-major ``(nNo, dof)`` arrays are the reference's column-major
+``Array<double>(dof, nNo)``; ``Val`` is ``(nnz, dof*dof)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import mesh as _mesh
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsvgpu.so")
+
+SVGPU_OK = 0
+SVGPU_FP64, SVGPU_MIXED = 0, 1
+BC_TYPE_Dir, BC_TYPE_Neu = 0, 1
+LS_TYPE_GMRES = 2
+PREC_NONE, PREC_FSILS = 0, 1
+
+_lib = None
+
+
+def lib():
+    """Load libsvgpu.so.  There is no fallback: without the CUDA library nothing runs."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"svgpu CUDA library not built ({LIB_PATH}); run __graft_entry__.build()")
+        _lib = C.CDLL(LIB_PATH)
+        _lib.svgpu_last_error.restype = C.c_char_p
+        _lib.svgpu_kernel_launches.restype = C.c_longlong
+    return _lib
+
+
+class LsStats(C.Structure):
+    _fields_ = [("iNorm", C.c_double), ("fNorm", C.c_double), ("dB", C.c_double), ("callD", C.c_double),
+                ("itr", C.c_int), ("suc", C.c_int), ("true_rel", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class FluidProps(C.Structure):
+    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("f", C.c_double * 3), ("k_inv_darcy", C.c_double),
+                ("backflow_beta", C.c_double), ("dt", C.c_double), ("am", C.c_double), ("af", C.c_double),
+                ("gam", C.c_double), ("beta", C.c_double)]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [("minItr", C.c_int), ("maxItr", C.c_int), ("tol", C.c_double), ("precision", C.c_int),
+                ("outletFace", C.c_int), ("outletH", C.c_double)]
+
+
+def genalpha_first_order(rho_inf: float):
+    """eq.am/af/gam/beta of a first-order equation (initialize.cpp:426-465)."""
+    am = 0.5 * (3.0 - rho_inf) / (1.0 + rho_inf)
+    af = 1.0 / (1.0 + rho_inf)
+    beta = 0.25 * (1.0 + am - af) ** 2
+    gam = 0.5 + am - af
+    return am, af, gam, beta
+
+
+def fluid_props(rho=1.06, mu=0.04, dt=1e-3, rho_inf=0.5, backflow_beta=0.2, k_inv_darcy=0.0, f=(0.0, 0.0, 0.0)):
+    am, af, gam, beta = genalpha_first_order(rho_inf)
+    return FluidProps(rho, mu, (C.c_double * 3)(*f), k_inv_darcy, backflow_beta, dt, am, af, gam, beta)
+
+
+def _ptr(a):
+    """Data pointer of a numpy array or a torch tensor (host or CUDA)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return C.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One svgpu context (a GPU and a stream): holds the FSILS handles, the mesh and
+    the resident linear system."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().svgpu_create(C.byref(self._h), int(device))
+        if rc != SVGPU_OK:
+            raise RuntimeError(f"svgpu_create failed ({rc}): no usable CUDA device")
+
+    def close(self):
+        if self._h:
+            lib().svgpu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc < 0:
+            msg = lib().svgpu_last_error(self._h).decode()
+            raise RuntimeError(f"{what}: {msg} (status {rc})")
+        return rc
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().svgpu_kernel_launches(self._h))
+
+    # ---- FSILS set-up
+    def fsils_lhs_create(self, nNo, rowPtr, colPtr, nFaces):
+        rowPtr = np.ascontiguousarray(rowPtr, dtype=np.int32)
+        colPtr = np.ascontiguousarray(colPtr, dtype=np.int32)
+        self.nNo, self.nnz = int(nNo), int(colPtr.size)
+        self._check(lib().svgpu_lhs_create(self._h, self.nNo, self.nNo, self.nnz, None, _ptr(rowPtr), _ptr(colPtr),
+                                           int(nFaces)), "fsils_lhs_create")
+
+    def fsils_bc_create(self, faIn, gNodes, dof, bc_type, val=None):
+        gNodes = np.ascontiguousarray(gNodes, dtype=np.int32)
+        if val is not None:
+            val = np.ascontiguousarray(val, dtype=np.float64)
+        self._check(lib().svgpu_bc_create(self._h, int(faIn), int(gNodes.size), int(dof), int(bc_type),
+                                          _ptr(gNodes), _ptr(val)), "fsils_bc_create")
+
+    def fsils_ls_create(self, ls_type=LS_TYPE_GMRES, relTol=-1.0, absTol=-1.0, maxItr=-1, dimKry=-1):
+        self._check(lib().svgpu_ls_create(self._h, int(ls_type), C.c_double(relTol), C.c_double(absTol),
+                                          int(maxItr), int(dimKry)), "fsils_ls_create")
+
+    def fsils_solve(self, dof, Ri, Val, prec=PREC_FSILS, incL=None, res=None) -> LsStats:
+        """In place, as the reference: Ri residual -> increment, Val -> scaled Val."""
+        st = LsStats()
+        incL_a = None if incL is None else np.ascontiguousarray(incL, dtype=np.int32)
+        res_a = None if res is None else np.ascontiguousarray(res, dtype=np.float64)
+        self._check(lib().svgpu_fsils_solve(self._h, int(dof), _ptr(Ri), _ptr(Val), int(prec), _ptr(incL_a),
+                                            _ptr(res_a), C.byref(st)), "fsils_solve")
+        return st
+
+    def spar_mul(self, dof, K, U, KU):
+        self._check(lib().svgpu_spar_mul(self._h, int(dof), _ptr(K), _ptr(U), _ptr(KU)), "spar_mul")
+
+    # ---- mesh and assembly
+    def mesh_create(self, x, ien):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        ien = np.ascontiguousarray(ien, dtype=np.int32)
+        self._check(lib().svgpu_mesh_create(self._h, int(x.shape[0]), int(ien.shape[0]), 4, _ptr(ien), _ptr(x)),
+                    "mesh_create")
+
+    def face_create(self, face_id, fien, gE):
+        fien = np.ascontiguousarray(fien, dtype=np.int32)
+        gE = np.ascontiguousarray(gE, dtype=np.int32)
+        self._check(lib().svgpu_face_create(self._h, int(face_id), int(gE.size), _ptr(fien), _ptr(gE)), "face_create")
+
+    def construct_fluid(self, props, Ag, Yg, Bf=None, R=None, Val=None, precision=SVGPU_FP64):
+        self._check(lib().svgpu_construct_fluid(self._h, C.byref(props), _ptr(Ag), _ptr(Yg), _ptr(Bf), _ptr(R),
+                                                _ptr(Val), int(precision)), "construct_fluid")
+
+    def b_assem_neu_bc(self, face_id, props, h, Yg, R=None, Val=None):
+        self._check(lib().svgpu_neu_bc_fluid(self._h, int(face_id), C.byref(props), C.c_double(h), _ptr(Yg),
+                                             _ptr(R), _ptr(Val)), "b_assem_neu_bc")
+
+    def set_dirichlet(self, nodes):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        self._check(lib().svgpu_set_dirichlet(self._h, int(nodes.size), _ptr(nodes)), "set_dirichlet")
+
+    def fluid_step(self, props, opts, dirY, dirA, Ao, Yo, Do, An, Yn, Dn, norms):
+        stats = (LsStats * max(1, opts.maxItr))()
+        iN = C.c_double(norms[0])
+        pN = C.c_double(norms[1])
+        it = self._check(lib().svgpu_fluid_step(self._h, C.byref(props), C.byref(opts), _ptr(dirY), _ptr(dirA),
+                                                _ptr(Ao), _ptr(Yo), _ptr(Do), _ptr(An), _ptr(Yn), _ptr(Dn),
+                                                C.byref(iN), C.byref(pN), stats), "fluid_step")
+        norms[0], norms[1] = iN.value, pN.value
+        return [stats[i].as_dict() for i in range(it)]
+
+
+# ------------------------------------------------------------------ host driver
+FACE_INLET, FACE_WALL, FACE_OUTLET = 0, 1, 2
+
+
+def csr_pattern(nNo: int, ien: np.ndarray):
+    """lhsa (lhsa.cpp:153): rowPtr/colPtr of the element cliques, sorted columns."""
+    ien = np.asarray(ien, dtype=np.int64)
+    e = ien.shape[1]
+    rows = np.repeat(ien, e, axis=1).ravel()
+    cols = np.tile(ien, (1, e)).ravel()
+    key = np.unique(rows * nNo + cols)
+    r = (key // nNo).astype(np.int64)
+    c = (key % nNo).astype(np.int32)
+    rowPtr = np.zeros(nNo + 1, dtype=np.int32)
+    np.add.at(rowPtr, r + 1, 1)
+    return np.cumsum(rowPtr, dtype=np.int64).astype(np.int32), c
+
+
+def dirichlet_nodes(mesh):
+    """Velocity-Dirichlet nodes (inlet + wall) and the inlet profile (0 on walls)."""
+    inlet, wall = mesh.faces["inlet"], mesh.faces["wall"]
+    nodes = np.union1d(inlet.gN, wall.gN).astype(np.int32)
+    prof = np.zeros(nodes.size)
+    prof[np.searchsorted(nodes, inlet.gN)] = mesh.inlet_profile
+    return nodes, prof
+
+
+def inflow(prof, time, u_mean, u_amp, freq):
+    """u_z = u_c(t) * profile on the inlet, u_c = u_mean + u_amp sin(2 pi f t); acceleration du_c/dt * profile."""
+    w = 2.0 * np.pi * freq
+    uc = u_mean + u_amp * np.sin(w * time)
+    duc = u_amp * w * np.cos(w * time)
+    dirY = np.zeros((prof.size, 3))
+    dirA = np.zeros((prof.size, 3))
+    dirY[:, 2] = uc * prof
+    dirA[:, 2] = duc * prof
+    return dirY, dirA
+
+
+class PipeFluidSolver:
+    """The fluid pipe case on the GPU: CSR set-up (lhsa + fsils_lhs_create), Dirichlet
+    faces (fsils_bc_create, baf_ini.cpp:719-744), the outlet face, GMRES settings, and
+    time stepping through svgpu_fluid_step."""
+
+    def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, sD=50, mItr=100, relTol=1e-8, absTol=1e-17,
+                 newton_min=3, newton_max=3, newton_tol=1e-11, precision=SVGPU_FP64, rowPtr=None, colPtr=None):
+        self.mesh = mesh
+        self.props = props or fluid_props()
+        self.ctx = Context(device)
+        nNo = mesh.nNo
+        if rowPtr is None:
+            rowPtr, colPtr = csr_pattern(nNo, mesh.ien)
+        self.rowPtr, self.colPtr = rowPtr, colPtr
+        self.ctx.fsils_lhs_create(nNo, rowPtr, colPtr, 2)
+        self.ctx.fsils_bc_create(0, mesh.faces["inlet"].gN, 3, BC_TYPE_Dir)
+        self.ctx.fsils_bc_create(1, mesh.faces["wall"].gN, 3, BC_TYPE_Dir)
+        self.ctx.fsils_ls_create(LS_TYPE_GMRES, relTol, absTol, mItr, sD)
+        self.ctx.mesh_create(mesh.x, mesh.ien)
+        out = mesh.faces["outlet"]
+        self.ctx.face_create(FACE_OUTLET, out.ien, out.gE)
+        self.dir_nodes, self.dir_prof = dirichlet_nodes(mesh)
+        self.ctx.set_dirichlet(self.dir_nodes)
+        self.opts = NewtonOpts(newton_min, newton_max, newton_tol, precision, FACE_OUTLET, 0.0)
+        z = lambda: np.zeros((nNo, 4))  # noqa: E731
+        self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
+        self.norms = [0.0, 0.0]
+        self.time = 0.0
+
+    def step(self, u_mean=10.0, u_amp=0.0, freq=1.0):
+        self.time += self.props.dt
+        dirY, dirA = inflow(self.dir_prof, self.time, u_mean, u_amp, freq)
+        stats = self.ctx.fluid_step(self.props, self.opts, dirY, dirA, self.Ao, self.Yo, self.Do,
+                                    self.An, self.Yn, self.Dn, self.norms)
+        self.Ao[:] = self.An
+        self.Yo[:] = self.Yn
+        return stats

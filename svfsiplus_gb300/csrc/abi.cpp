@@ -1,0 +1,838 @@
+// C-ABI entry points of the svgpu library (include/svgpu.h): FSILS-style set-up,
+// the GMRES solve, fluid assembly dispatch and the Newton time step.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "internal.h"
+
+namespace svgpu {
+
+int set_err(svgpu_ctx* ctx, int status, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return status;
+}
+
+int cuda_fail(svgpu_ctx* ctx, cudaError_t e, const char* what) {
+  return set_err(ctx, SVGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Device arrays are read with 128-bit loads: they must start on a 16-byte boundary.
+bool misaligned_device(const void* p) {
+  return p && is_device_ptr(p) && (reinterpret_cast<uintptr_t>(p) & 15u) != 0;
+}
+
+// launchers defined in k_krylov.cu without a header entry
+void launch_spmv4_f64_flag(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr,
+                           const double* Val, const double* x, double* y, const int* flags);
+int launch_multidot_flag(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
+                         double* partial, int sm_count, const int* flags);
+void launch_reduce_partials_flag(cudaStream_t s, int nparts, int m, const double* partial, double* out,
+                                 const int* flags);
+int multidot_ctas(long n, int sm_count);
+
+}  // namespace svgpu
+
+using namespace svgpu;
+
+namespace {
+
+// Copies n elements from a host-or-device pointer into a device buffer.
+template <typename T>
+int to_device(svgpu_ctx* ctx, DevBuf<T>& dst, const T* src, size_t n) {
+  SVGPU_CUDA(ctx, dst.resize(n));
+  if (n == 0) return SVGPU_OK;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.p, src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
+  return SVGPU_OK;
+}
+
+template <typename T>
+int to_host(svgpu_ctx* ctx, std::vector<T>& dst, const T* src, size_t n) {
+  dst.resize(n);
+  if (n == 0) return SVGPU_OK;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+// Greedy colouring of elements (eNoN nodes each) so that no two elements of a colour
+// share a node; returns the permutation (colour-major, original order inside a
+// colour) and the colour offsets.
+int color_elements(int nNo, int nEl, int eNoN, const int* ien, std::vector<int>& perm,
+                   std::vector<int>& start) {
+  const int W = 4;  // up to 256 colours
+  std::vector<uint64_t> used((size_t)nNo * W, 0);
+  std::vector<int> col(nEl);
+  int ncol = 0;
+  for (int e = 0; e < nEl; e++) {
+    uint64_t m[W] = {0, 0, 0, 0};
+    for (int a = 0; a < eNoN; a++) {
+      const uint64_t* u = &used[(size_t)ien[(size_t)eNoN * e + a] * W];
+      for (int w = 0; w < W; w++) m[w] |= u[w];
+    }
+    int c = -1;
+    for (int w = 0; w < W && c < 0; w++)
+      if (~m[w]) c = 64 * w + __builtin_ctzll(~m[w]);
+    if (c < 0) return -1;
+    col[e] = c;
+    ncol = std::max(ncol, c + 1);
+    for (int a = 0; a < eNoN; a++) used[(size_t)ien[(size_t)eNoN * e + a] * W + c / 64] |= (1ull << (c % 64));
+  }
+  start.assign(ncol + 1, 0);
+  for (int e = 0; e < nEl; e++) start[col[e] + 1]++;
+  for (int c = 0; c < ncol; c++) start[c + 1] += start[c];
+  std::vector<int> fill(start.begin(), start.end() - 1);
+  perm.resize(nEl);
+  for (int e = 0; e < nEl; e++) perm[fill[col[e]]++] = e;
+  return ncol;
+}
+
+// Offset of column `col` inside row `row` of the CSR pattern, -1 if absent.
+inline int row_offset(const std::vector<int>& rowPtr, const std::vector<int>& colPtr, int row, int col) {
+  const int* b = colPtr.data() + rowPtr[row];
+  const int* e = colPtr.data() + rowPtr[row + 1];
+  const int* f = std::lower_bound(b, e, col);
+  if (f == e || *f != col) return -1;
+  return (int)(f - b);
+}
+
+int ensure_krylov(svgpu_ctx* ctx, long n, int sD) {
+  KrylovWork& kw = ctx->kw;
+  if (kw.n == (size_t)n && kw.sD == sD && kw.V.p) return SVGPU_OK;
+  kw.n = n;
+  kw.sD = sD;
+  SVGPU_CUDA(ctx, kw.V.resize((size_t)n * (sD + 1)));
+  SVGPU_CUDA(ctx, kw.X.resize(n));
+  SVGPU_CUDA(ctx, kw.Wc.resize(n));
+  SVGPU_CUDA(ctx, kw.mask.resize(n));
+  SVGPU_CUDA(ctx, kw.tmp.resize(n));
+  SVGPU_CUDA(ctx, kw.hess.resize((size_t)(sD + 1) * sD));
+  SVGPU_CUDA(ctx, kw.givens.resize(5 * (size_t)sD + 3));
+  SVGPU_CUDA(ctx, kw.partial.resize((size_t)multidot_ctas(n, ctx->sm_count) * (sD + 2) + 16));
+  SVGPU_CUDA(ctx, kw.scal.resize(16));
+  SVGPU_CUDA(ctx, kw.flags.resize(4));
+  return SVGPU_OK;
+}
+
+struct CycleGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* val = nullptr;
+  long n = 0;
+  int sD = 0, dof = 0;
+  ~CycleGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+// One graph per context: the sD Arnoldi iterations of a restart cycle.
+std::map<const svgpu_ctx*, std::unique_ptr<CycleGraph>>& graphs() {
+  static std::map<const svgpu_ctx*, std::unique_ptr<CycleGraph>> g;
+  return g;
+}
+
+void spmv_any(svgpu_ctx* ctx, int dof, const double* Val, const double* x, double* y, const int* flags) {
+  if (dof == 4)
+    launch_spmv4_f64_flag(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val, x, y, flags);
+  else
+    launch_spmv_generic(ctx->stream, ctx->nNo, dof, ctx->rowPtr.p, ctx->colPtr.p, Val, x, y);
+  ctx->launches++;
+}
+
+// Enqueues the Arnoldi iterations i = 0..sD-1 (gmres.cpp:529-593).
+void enqueue_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
+  KrylovWork& kw = ctx->kw;
+  const long n = (long)kw.n;
+  const int sD = kw.sD;
+  double* hraw = kw.givens.p + 4 * sD + 1;
+  for (int i = 0; i < sD; i++) {
+    double* ui = kw.V.p + (long)i * n;
+    double* ui1 = kw.V.p + (long)(i + 1) * n;
+    spmv_any(ctx, dof, Val, ui, ui1, kw.flags.p);
+    const int ctas = launch_multidot_flag(ctx->stream, n, i + 2, kw.V.p, n, ui1, kw.partial.p, ctx->sm_count,
+                                          kw.flags.p);
+    launch_reduce_partials_flag(ctx->stream, ctas, i + 2, kw.partial.p, hraw, kw.flags.p);
+    launch_givens(ctx->stream, i, sD, kw.hess.p, kw.givens.p, kw.scal.p, kw.flags.p);
+    launch_cgs_update(ctx->stream, n, i, kw.V.p, n, hraw, kw.flags.p);
+    ctx->launches += 4;
+  }
+}
+
+int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
+  auto& slot = graphs()[ctx];
+  if (!slot) slot.reset(new CycleGraph());
+  CycleGraph& g = *slot;
+  const long n = (long)ctx->kw.n;
+  if (!g.exec || g.val != Val || g.n != n || g.sD != ctx->kw.sD || g.dof != dof) {
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
+    cudaGraph_t graph;
+    const long long before = ctx->launches;
+    SVGPU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_cycle(ctx, dof, Val);
+    SVGPU_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+    ctx->launches = before;
+    SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    g.val = Val;
+    g.n = n;
+    g.sD = ctx->kw.sD;
+    g.dof = dof;
+  }
+  SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+  ctx->launches += 5LL * ctx->kw.sD;
+  return SVGPU_OK;
+}
+
+double device_norm(svgpu_ctx* ctx, long n, const double* a, int& st) {
+  KrylovWork& kw = ctx->kw;
+  launch_norm2(ctx->stream, n, a, kw.partial.p, kw.scal.p + 1, ctx->sm_count);
+  ctx->launches += 2;
+  double v = 0.0;
+  cudaError_t e = cudaMemcpyAsync(&v, kw.scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  st = (e == cudaSuccess) ? SVGPU_OK : cuda_fail(ctx, e, "norm");
+  return std::sqrt(v);
+}
+
+// gmres_v (gmres.cpp:450-629) on device arrays: R in (preconditioned residual), out X.
+int gmres_device(svgpu_ctx* ctx, int dof, const double* Val, double* R, svgpu_ls_stats* st) {
+  KrylovWork& kw = ctx->kw;
+  const long n = (long)ctx->nNo * dof;
+  int rc = SVGPU_OK;
+  st->suc = 0;
+  double eps = device_norm(ctx, n, R, rc);
+  if (rc) return rc;
+  st->iNorm = eps;
+  st->fNorm = eps;
+  eps = std::max(ctx->absTol, ctx->relTol * eps);
+  st->itr = 0;
+  if (st->iNorm <= ctx->absTol) {
+    st->dB = 0.0;
+    return SVGPU_OK;  // R is left as is, like the reference's early return
+  }
+  if (!std::isfinite(st->iNorm)) return set_err(ctx, SVGPU_ENAN, "non-finite residual");
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
+  double dB = 0.0;
+  const int sD = kw.sD;
+  for (int l = 0; l < ctx->mItr; l++) {
+    dB = st->fNorm;
+    st->itr++;
+    // u0 = R - K X
+    if (l == 0) {
+      launch_residual_init(ctx->stream, n, R, kw.V.p, kw.X.p, true, nullptr);
+      ctx->launches++;
+    } else {
+      spmv_any(ctx, dof, Val, kw.X.p, kw.tmp.p, nullptr);
+      launch_residual_init(ctx->stream, n, R, kw.V.p, kw.X.p, false, kw.tmp.p);
+      ctx->launches++;
+    }
+    launch_norm2(ctx->stream, n, kw.V.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
+    launch_scale_by_inv_norm(ctx->stream, n, kw.V.p, kw.scal.p + 2, kw.givens.p + 2 * sD, kw.flags.p);
+    ctx->launches += 3;
+    if ((rc = run_cycle(ctx, dof, Val))) return rc;
+    launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
+    launch_xupdate(ctx->stream, n, sD, kw.V.p, n, kw.givens.p, kw.flags.p, kw.X.p);
+    ctx->launches += 2;
+    int flags[4];
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> err(sD + 1);
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(err.data(), kw.givens.p + 2 * sD, (sD + 1) * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int last = std::min(flags[1], sD - 1);
+    st->itr += last + 1;
+    st->fNorm = std::fabs(err[last + 1]);
+    if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
+    if (flags[0]) {
+      st->suc = 1;
+      break;
+    }
+  }
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(R, kw.X.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  st->dB = 10.0 * std::log(st->fNorm / dB);
+  return SVGPU_OK;
+}
+
+// fsils_solve on device arrays (solve.cpp:50-193).
+int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, const int* incL,
+                 svgpu_ls_stats* st) {
+  auto t0 = std::chrono::steady_clock::now();
+  const long n = (long)ctx->nNo * dof;
+  int rc = ensure_krylov(ctx, n, ctx->sD);
+  if (rc) return rc;
+  KrylovWork& kw = ctx->kw;
+  // Dirichlet mask from the included faces (precond.cpp:204-225)
+  launch_fill(ctx->stream, n, 1.0, kw.mask.p);
+  ctx->launches++;
+  for (int f = 0; f < ctx->nFaces; f++) {
+    LsFace& fa = ctx->faces[f];
+    if (!fa.created || fa.bGrp != SVGPU_BC_DIR) continue;
+    if (incL && incL[f] == 0) continue;
+    launch_mask_face(ctx->stream, fa.nNo, fa.dof, dof, fa.d_glob.p, fa.d_val.p, kw.mask.p);
+    ctx->launches++;
+  }
+  if (prec == SVGPU_PREC_FSILS) {
+    launch_diag_w(ctx->stream, ctx->nNo, dof, ctx->diagPtr.p, Val, kw.mask.p, kw.Wc.p);
+    launch_scale_val(ctx->stream, ctx->nnz, dof, ctx->blkRow.p, ctx->colPtr.p, kw.Wc.p, Val);
+    launch_vmul(ctx->stream, n, kw.Wc.p, R);
+    ctx->launches += 3;
+  } else {
+    launch_fill(ctx->stream, n, 1.0, kw.Wc.p);
+    ctx->launches++;
+  }
+  if (ctx->lsType != SVGPU_LS_GMRES) return set_err(ctx, SVGPU_EINVAL, "only GMRES is available in fsils_solve");
+  rc = gmres_device(ctx, dof, Val, R, st);
+  if (rc) return rc;
+  launch_vmul(ctx->stream, n, kw.Wc.p, R);
+  ctx->launches++;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  st->callD = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  st->true_rel = -1.0;
+  return SVGPU_OK;
+}
+
+FluidConsts fluid_consts(const svgpu_fluid_props* p) {
+  FluidConsts c;
+  c.rho = p->rho;
+  c.mu = p->mu;
+  c.f0 = p->f[0];
+  c.f1 = p->f[1];
+  c.f2 = p->f[2];
+  c.kd = p->k_inv_darcy;
+  c.beta_bf = p->backflow_beta;
+  c.dt = p->dt;
+  c.am = p->am;
+  c.af = p->af;
+  c.gam = p->gam;
+  return c;
+}
+
+int check_errflag(svgpu_ctx* ctx) {
+  int h[2];
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(h, ctx->errflag.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h[0] == SVGPU_EJAC)
+    return set_err(ctx, SVGPU_EJAC, "[construct_fluid] Jacobian for element " + std::to_string(h[1]) + " is < 0.");
+  return SVGPU_OK;
+}
+
+// Assembly into device R (4,nNo) and Val64 or Val32.
+int assemble_fluid_device(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag, const double* Yg,
+                          const double* Bf, double* R, double* Val64, float* Val32, int precision) {
+  MeshData& m = *ctx->mesh;
+  FluidConsts c = fluid_consts(props);
+  for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+    launch_fluid_assembly(ctx->stream, precision, c, m.color_start[k], m.color_start[k + 1] - m.color_start[k],
+                          m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, Ag, Yg, Bf, ctx->rowPtr.p, R, Val64, Val32,
+                          ctx->errflag.p);
+    ctx->launches++;
+  }
+  return SVGPU_OK;
+}
+
+int backflow_device(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h, const double* Yg,
+                    double* R, double* Val64, float* Val32) {
+  auto it = ctx->mfaces.find(faceId);
+  if (it == ctx->mfaces.end()) return set_err(ctx, SVGPU_EINVAL, "unknown face id");
+  MeshFace& f = *it->second;
+  FluidConsts c = fluid_consts(props);
+  for (size_t k = 0; k + 1 < f.color_start.size(); k++) {
+    launch_neu_backflow(ctx->stream, c, h, f.color_start[k], f.color_start[k + 1] - f.color_start[k], f.fien.p,
+                        f.inner.p, f.boff.p, ctx->mesh->x4.p, Yg, ctx->rowPtr.p, R, Val64, Val32);
+    ctx->launches++;
+  }
+  return SVGPU_OK;
+}
+
+}  // namespace
+
+// =============================================================================== ABI
+extern "C" {
+
+int svgpu_create(svgpu_ctx** out, int device) {
+  if (!out) return SVGPU_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SVGPU_ECUDA;
+  if (device < 0 || device >= ndev) return SVGPU_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return SVGPU_ECUDA;
+  svgpu_ctx* ctx = new svgpu_ctx();
+  ctx->device = device;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return SVGPU_ECUDA;
+  }
+  ctx->own_stream = true;
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (ctx->errflag.resize(2) != cudaSuccess) {
+    delete ctx;
+    return SVGPU_ECUDA;
+  }
+  cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream);
+  *out = ctx;
+  return SVGPU_OK;
+}
+
+int svgpu_destroy(svgpu_ctx* ctx) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  graphs().erase(ctx);
+  cudaStream_t s = ctx->stream;
+  bool own = ctx->own_stream;
+  delete ctx;
+  if (own && s) cudaStreamDestroy(s);
+  return SVGPU_OK;
+}
+
+const char* svgpu_last_error(const svgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+long long svgpu_kernel_launches(const svgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int svgpu_set_stream(svgpu_ctx* ctx, void* stream) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  graphs().erase(ctx);
+  return SVGPU_OK;
+}
+
+int svgpu_lhs_create(svgpu_ctx* ctx, int gnNo, int nNo, int nnz, const int* gNodes, const int* rowPtr,
+                     const int* colPtr, int nFaces) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (nNo <= 0 || nnz <= 0 || !rowPtr || !colPtr || nFaces < 0)
+    return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: bad sizes or null arrays");
+  if (gnNo != nNo) return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: one rank only (gnNo must equal nNo)");
+  int rc;
+  if ((rc = to_host(ctx, ctx->h_rowPtr, rowPtr, nNo + 1))) return rc;
+  if ((rc = to_host(ctx, ctx->h_colPtr, colPtr, nnz))) return rc;
+  if (gNodes) {
+    std::vector<int> g;
+    if ((rc = to_host(ctx, g, gNodes, nNo))) return rc;
+    for (int a = 0; a < nNo; a++)
+      if (g[a] != a) return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: gNodes must be the identity on one rank");
+  }
+  if (ctx->h_rowPtr[0] != 0 || ctx->h_rowPtr[nNo] != nnz)
+    return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: rowPtr must run from 0 to nnz");
+  std::vector<int> diag(nNo, -1), blkRow(nnz);
+  for (int a = 0; a < nNo; a++) {
+    for (int k = ctx->h_rowPtr[a]; k < ctx->h_rowPtr[a + 1]; k++) {
+      blkRow[k] = a;
+      if (ctx->h_colPtr[k] == a && diag[a] < 0) diag[a] = k;
+      if (ctx->h_colPtr[k] < 0 || ctx->h_colPtr[k] >= nNo)
+        return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: column index out of range");
+    }
+    if (diag[a] < 0) return set_err(ctx, SVGPU_EINVAL, "fsils_lhs_create: row without a diagonal block");
+  }
+  ctx->nNo = nNo;
+  ctx->nnz = nnz;
+  ctx->nFaces = nFaces;
+  ctx->faces.clear();
+  ctx->faces.resize(nFaces);
+  if ((rc = to_device(ctx, ctx->rowPtr, ctx->h_rowPtr.data(), nNo + 1))) return rc;
+  if ((rc = to_device(ctx, ctx->colPtr, ctx->h_colPtr.data(), nnz))) return rc;
+  if ((rc = to_device(ctx, ctx->diagPtr, diag.data(), nNo))) return rc;
+  if ((rc = to_device(ctx, ctx->blkRow, blkRow.data(), nnz))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  graphs().erase(ctx);
+  return SVGPU_OK;
+}
+
+int svgpu_bc_create(svgpu_ctx* ctx, int faIn, int nNo, int dof, int bcType, const int* gNodes,
+                    const double* val) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->nNo == 0) return set_err(ctx, SVGPU_ESTATE, "fsils_bc_create before fsils_lhs_create");
+  if (faIn >= ctx->nFaces)
+    return set_err(ctx, SVGPU_EINVAL, "FSILS: faIn is exceeding lhs structure maximum number of faces");
+  if (faIn < 0) return set_err(ctx, SVGPU_EINVAL, "FSILS: faIn is smaller than zero");
+  if (nNo < 0 || dof <= 0 || (nNo > 0 && !gNodes)) return set_err(ctx, SVGPU_EINVAL, "fsils_bc_create: bad face");
+  LsFace& f = ctx->faces[faIn];
+  int rc;
+  f.nNo = nNo;
+  f.dof = dof;
+  f.bGrp = bcType;
+  if ((rc = to_host(ctx, f.glob, gNodes, nNo))) return rc;
+  for (int a = 0; a < nNo; a++)
+    if (f.glob[a] < 0 || f.glob[a] >= ctx->nNo) return set_err(ctx, SVGPU_EINVAL, "fsils_bc_create: node out of range");
+  if (val) {
+    if ((rc = to_host(ctx, f.val, val, (size_t)dof * nNo))) return rc;
+  } else {
+    f.val.assign((size_t)dof * nNo, 0.0);
+  }
+  if ((rc = to_device(ctx, f.d_glob, f.glob.data(), nNo))) return rc;
+  if ((rc = to_device(ctx, f.d_val, f.val.data(), (size_t)dof * nNo))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  f.created = true;
+  return SVGPU_OK;
+}
+
+int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, int maxItr, int dimKry) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (lsType != SVGPU_LS_GMRES) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: only GMRES is supported");
+  // defaults of fsils_ls_create (liner_solver/ls.cpp:62-79)
+  ctx->lsType = lsType;
+  ctx->relTol = relTol >= 0 ? relTol : 0.1;
+  ctx->absTol = absTol >= 0 ? absTol : 1e-10;
+  ctx->mItr = maxItr > 0 ? maxItr : 4;
+  ctx->sD = dimKry > 0 ? dimKry : 250;
+  if (ctx->sD > 250) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: Krylov dimension above 250");
+  ctx->ls_created = true;
+  return SVGPU_OK;
+}
+
+int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec, const int* incL,
+                      const double* res, svgpu_ls_stats* stats) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (misaligned_device(Ri) || misaligned_device(Val))
+    return set_err(ctx, SVGPU_EINVAL, "fsils_solve: device arrays must be 16-byte aligned");
+  if (ctx->nNo == 0 || !ctx->ls_created) return set_err(ctx, SVGPU_ESTATE, "fsils_solve before lhs/ls create");
+  if (dof < 1 || dof > 8) return set_err(ctx, SVGPU_EINVAL, "fsils_solve: dof must be 1..8");
+  if (res)
+    for (int f = 0; f < ctx->nFaces; f++)
+      if (res[f] != 0.0 && ctx->faces[f].bGrp == SVGPU_BC_NEU && (!incL || incL[f] != 0))
+        return set_err(ctx, SVGPU_EINVAL, "fsils_solve: coupled Neumann faces are not supported");
+  svgpu_ls_stats local;
+  svgpu_ls_stats* st = stats ? stats : &local;
+  std::memset(st, 0, sizeof(*st));
+  const long n = (long)ctx->nNo * dof;
+  const size_t nv = (size_t)ctx->nnz * dof * dof;
+  int rc;
+  if (!Ri && !Val) {
+    if (dof != 4 || !ctx->R.p || !ctx->Val.p) return set_err(ctx, SVGPU_ESTATE, "no resident system to solve");
+    return solve_device(ctx, dof, ctx->R.p, ctx->Val.p, prec, incL, st);
+  }
+  if (!Ri || !Val) return set_err(ctx, SVGPU_EINVAL, "fsils_solve: Ri and Val must both be given");
+  const bool dR = is_device_ptr(Ri), dV = is_device_ptr(Val);
+  double* Rd = Ri;
+  double* Vd = Val;
+  if (!dR) {
+    if ((rc = to_device(ctx, ctx->stage1, Ri, n))) return rc;
+    Rd = ctx->stage1.p;
+  }
+  if (!dV) {
+    if ((rc = to_device(ctx, ctx->stage2, Val, nv))) return rc;
+    Vd = ctx->stage2.p;
+  }
+  rc = solve_device(ctx, dof, Rd, Vd, prec, incL, st);
+  if (rc) return rc;
+  if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(Ri, Rd, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, double* KU) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->nNo == 0) return set_err(ctx, SVGPU_ESTATE, "spar_mul before fsils_lhs_create");
+  if (dof < 1 || dof > 8 || !K || !U || !KU) return set_err(ctx, SVGPU_EINVAL, "spar_mul: bad arguments");
+  if (misaligned_device(K) || misaligned_device(U) || misaligned_device(KU))
+    return set_err(ctx, SVGPU_EINVAL, "spar_mul: device arrays must be 16-byte aligned");
+  const long n = (long)ctx->nNo * dof;
+  const size_t nv = (size_t)ctx->nnz * dof * dof;
+  int rc;
+  DevBuf<double> k, u, ku;
+  const double* Kd = K;
+  const double* Ud = U;
+  double* KUd = KU;
+  if (!is_device_ptr(K)) { if ((rc = to_device(ctx, k, K, nv))) return rc; Kd = k.p; }
+  if (!is_device_ptr(U)) { if ((rc = to_device(ctx, u, U, n))) return rc; Ud = u.p; }
+  const bool dKU = is_device_ptr(KU);
+  if (!dKU) { SVGPU_CUDA(ctx, ku.resize(n)); KUd = ku.p; }
+  spmv_any(ctx, dof, Kd, Ud, KUd, nullptr);
+  if (!dKU) SVGPU_CUDA(ctx, cudaMemcpyAsync(KU, KUd, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_mesh_create(svgpu_ctx* ctx, int nNo, int nEl, int eNoN, const int* IEN, const double* x) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (eNoN != 4) return set_err(ctx, SVGPU_EINVAL, "mesh_create: linear tets (eNoN = 4) only");
+  if (ctx->nNo == 0) return set_err(ctx, SVGPU_ESTATE, "mesh_create before fsils_lhs_create");
+  if (nNo != ctx->nNo || nEl <= 0 || !IEN || !x) return set_err(ctx, SVGPU_EINVAL, "mesh_create: bad sizes");
+  int rc;
+  std::vector<int> ien;
+  std::vector<double> xh;
+  if ((rc = to_host(ctx, ien, IEN, (size_t)4 * nEl))) return rc;
+  if ((rc = to_host(ctx, xh, x, (size_t)3 * nNo))) return rc;
+  for (size_t i = 0; i < ien.size(); i++)
+    if (ien[i] < 0 || ien[i] >= nNo) return set_err(ctx, SVGPU_EINVAL, "mesh_create: IEN entry out of range");
+  auto m = std::make_unique<MeshData>();
+  m->nNo = nNo;
+  m->nEl = nEl;
+  std::vector<int> perm;
+  const int ncol = color_elements(nNo, nEl, 4, ien.data(), perm, m->color_start);
+  if (ncol < 0) return set_err(ctx, SVGPU_EINVAL, "mesh_create: more than 256 colours needed");
+  std::vector<int> pien((size_t)4 * nEl);
+  std::vector<uint8_t> boff((size_t)16 * nEl);
+  for (int k = 0; k < nEl; k++) {
+    const int e = perm[k];
+    for (int a = 0; a < 4; a++) pien[4 * (size_t)k + a] = ien[4 * (size_t)e + a];
+    for (int a = 0; a < 4; a++)
+      for (int b = 0; b < 4; b++) {
+        const int off = row_offset(ctx->h_rowPtr, ctx->h_colPtr, ien[4 * (size_t)e + a], ien[4 * (size_t)e + b]);
+        if (off < 0 || off > 255)
+          return set_err(ctx, SVGPU_EINVAL, "mesh_create: CSR pattern lacks an element block (or row > 256 blocks)");
+        boff[16 * (size_t)k + 4 * a + b] = (uint8_t)off;
+      }
+  }
+  std::vector<double> x4((size_t)4 * nNo, 0.0);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < 3; i++) x4[4 * (size_t)a + i] = xh[3 * (size_t)a + i];
+  if ((rc = to_device(ctx, m->ien, pien.data(), pien.size()))) return rc;
+  if ((rc = to_device(ctx, m->elem_id, perm.data(), perm.size()))) return rc;
+  if ((rc = to_device(ctx, m->boff, boff.data(), boff.size()))) return rc;
+  if ((rc = to_device(ctx, m->x4, x4.data(), x4.size()))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->mesh = std::move(m);
+  return SVGPU_OK;
+}
+
+int svgpu_face_create(svgpu_ctx* ctx, int faceId, int nFaEl, const int* fIEN, const int* gE) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "face_create before mesh_create");
+  if (nFaEl < 0 || (nFaEl > 0 && (!fIEN || !gE))) return set_err(ctx, SVGPU_EINVAL, "face_create: bad arguments");
+  int rc;
+  std::vector<int> fi, ge, ien;
+  if ((rc = to_host(ctx, fi, fIEN, (size_t)3 * nFaEl))) return rc;
+  if ((rc = to_host(ctx, ge, gE, nFaEl))) return rc;
+  // owner tets are needed in original numbering: rebuild from the permuted copy
+  const int nEl = ctx->mesh->nEl;
+  std::vector<int> pien, perm;
+  if ((rc = to_host(ctx, pien, ctx->mesh->ien.p, (size_t)4 * nEl))) return rc;
+  if ((rc = to_host(ctx, perm, ctx->mesh->elem_id.p, nEl))) return rc;
+  ien.resize((size_t)4 * nEl);
+  for (int k = 0; k < nEl; k++)
+    for (int a = 0; a < 4; a++) ien[4 * (size_t)perm[k] + a] = pien[4 * (size_t)k + a];
+  auto f = std::make_unique<MeshFace>();
+  f->nEl = nFaEl;
+  std::vector<int> inner(nFaEl);
+  for (int e = 0; e < nFaEl; e++) {
+    if (ge[e] < 0 || ge[e] >= nEl) return set_err(ctx, SVGPU_EINVAL, "face_create: owner element out of range");
+    int in = -1, matched = 0;
+    for (int b = 0; b < 4; b++) {
+      const int nb = ien[4 * (size_t)ge[e] + b];
+      bool on = false;
+      for (int a = 0; a < 3; a++) on = on || (nb == fi[3 * (size_t)e + a]);
+      if (on) matched++;
+      else if (in < 0) in = nb;
+    }
+    if (matched != 3 || in < 0)
+      return set_err(ctx, SVGPU_EINVAL, "[gnnb] face node could not be matched to a node of its volume element");
+    inner[e] = in;
+  }
+  std::vector<int> perm_f;
+  const int ncol = color_elements(ctx->nNo, nFaEl, 3, fi.data(), perm_f, f->color_start);
+  if (ncol < 0 && nFaEl > 0) return set_err(ctx, SVGPU_EINVAL, "face_create: colouring failed");
+  std::vector<int> pfi((size_t)3 * nFaEl), pin(nFaEl);
+  std::vector<uint8_t> boff((size_t)9 * nFaEl);
+  for (int k = 0; k < nFaEl; k++) {
+    const int e = perm_f[k];
+    pin[k] = inner[e];
+    for (int a = 0; a < 3; a++) pfi[3 * (size_t)k + a] = fi[3 * (size_t)e + a];
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        const int off = row_offset(ctx->h_rowPtr, ctx->h_colPtr, fi[3 * (size_t)e + a], fi[3 * (size_t)e + b]);
+        if (off < 0 || off > 255) return set_err(ctx, SVGPU_EINVAL, "face_create: CSR pattern lacks a face block");
+        boff[9 * (size_t)k + 3 * a + b] = (uint8_t)off;
+      }
+  }
+  if (nFaEl == 0) f->color_start.assign(1, 0);
+  if ((rc = to_device(ctx, f->fien, pfi.data(), pfi.size()))) return rc;
+  if ((rc = to_device(ctx, f->inner, pin.data(), pin.size()))) return rc;
+  if ((rc = to_device(ctx, f->boff, boff.data(), boff.size()))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->mfaces[faceId] = std::move(f);
+  return SVGPU_OK;
+}
+
+int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag, const double* Yg,
+                          const double* Bf, double* R, double* Val, int precision) {
+  if (!ctx || !props || !Ag || !Yg) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "construct_fluid before mesh_create");
+  if (precision != SVGPU_FP64 && precision != SVGPU_MIXED) return set_err(ctx, SVGPU_EINVAL, "bad precision");
+  if ((R == nullptr) != (Val == nullptr)) return set_err(ctx, SVGPU_EINVAL, "R and Val must both be given or both NULL");
+  if (misaligned_device(Ag) || misaligned_device(Yg) || misaligned_device(R) || misaligned_device(Val))
+    return set_err(ctx, SVGPU_EINVAL, "construct_fluid: device arrays must be 16-byte aligned");
+  const long n4 = 4L * ctx->nNo;
+  const size_t nv = (size_t)ctx->nnz * 16;
+  int rc;
+  const double* Agd = Ag;
+  const double* Ygd = Yg;
+  const double* Bfd = Bf;
+  if (!is_device_ptr(Ag)) { if ((rc = to_device(ctx, ctx->Ag, Ag, n4))) return rc; Agd = ctx->Ag.p; }
+  if (!is_device_ptr(Yg)) { if ((rc = to_device(ctx, ctx->Yg, Yg, n4))) return rc; Ygd = ctx->Yg.p; }
+  if (Bf && !is_device_ptr(Bf)) { if ((rc = to_device(ctx, ctx->Bf, Bf, 3L * ctx->nNo))) return rc; Bfd = ctx->Bf.p; }
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
+  if (!R) {  // resident system, zeroed first (ls_alloc)
+    SVGPU_CUDA(ctx, ctx->R.resize(n4));
+    SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, n4 * sizeof(double), ctx->stream));
+    if (precision == SVGPU_FP64) {
+      SVGPU_CUDA(ctx, ctx->Val.resize(nv));
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val.p, 0, nv * sizeof(double), ctx->stream));
+    } else {
+      SVGPU_CUDA(ctx, ctx->Val32.resize(nv));
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val32.p, 0, nv * sizeof(float), ctx->stream));
+    }
+    if ((rc = assemble_fluid_device(ctx, props, Agd, Ygd, Bfd, ctx->R.p, ctx->Val.p, ctx->Val32.p, precision)))
+      return rc;
+    return check_errflag(ctx);
+  }
+  if (precision != SVGPU_FP64) return set_err(ctx, SVGPU_EINVAL, "caller-owned Val is FP64; use the resident system for mixed precision");
+  const bool dR = is_device_ptr(R), dV = is_device_ptr(Val);
+  double* Rd = R;
+  double* Vd = Val;
+  if (!dR) { if ((rc = to_device(ctx, ctx->stage1, (const double*)R, n4))) return rc; Rd = ctx->stage1.p; }
+  if (!dV) { if ((rc = to_device(ctx, ctx->stage2, (const double*)Val, nv))) return rc; Vd = ctx->stage2.p; }
+  if ((rc = assemble_fluid_device(ctx, props, Agd, Ygd, Bfd, Rd, Vd, nullptr, SVGPU_FP64))) return rc;
+  if ((rc = check_errflag(ctx))) return rc;
+  if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, n4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h, const double* Yg,
+                       double* R, double* Val) {
+  if (!ctx || !props || !Yg) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "neu_bc before mesh_create");
+  if ((R == nullptr) != (Val == nullptr)) return set_err(ctx, SVGPU_EINVAL, "R and Val must both be given or both NULL");
+  if (misaligned_device(Yg) || misaligned_device(R) || misaligned_device(Val))
+    return set_err(ctx, SVGPU_EINVAL, "neu_bc: device arrays must be 16-byte aligned");
+  const long n4 = 4L * ctx->nNo;
+  const size_t nv = (size_t)ctx->nnz * 16;
+  int rc;
+  const double* Ygd = Yg;
+  if (!is_device_ptr(Yg)) { if ((rc = to_device(ctx, ctx->Yg, Yg, n4))) return rc; Ygd = ctx->Yg.p; }
+  if (!R) {
+    if (!ctx->R.p) return set_err(ctx, SVGPU_ESTATE, "no resident system");
+    rc = backflow_device(ctx, faceId, props, h, Ygd, ctx->R.p, ctx->Val.p ? ctx->Val.p : nullptr,
+                         ctx->Val.p ? nullptr : ctx->Val32.p);
+    if (rc) return rc;
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVGPU_OK;
+  }
+  const bool dR = is_device_ptr(R), dV = is_device_ptr(Val);
+  double* Rd = R;
+  double* Vd = Val;
+  if (!dR) { if ((rc = to_device(ctx, ctx->stage1, (const double*)R, n4))) return rc; Rd = ctx->stage1.p; }
+  if (!dV) { if ((rc = to_device(ctx, ctx->stage2, (const double*)Val, nv))) return rc; Vd = ctx->stage2.p; }
+  if ((rc = backflow_device(ctx, faceId, props, h, Ygd, Rd, Vd, nullptr))) return rc;
+  if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, n4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_set_dirichlet(svgpu_ctx* ctx, int nDir, const int* nodes) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (nDir < 0 || (nDir > 0 && !nodes)) return set_err(ctx, SVGPU_EINVAL, "set_dirichlet: bad arguments");
+  int rc;
+  std::vector<int> h;
+  if ((rc = to_host(ctx, h, nodes, nDir))) return rc;
+  for (int k = 0; k < nDir; k++)
+    if (h[k] < 0 || h[k] >= ctx->nNo) return set_err(ctx, SVGPU_EINVAL, "set_dirichlet: node out of range");
+  if ((rc = to_device(ctx, ctx->dirNodes, h.data(), nDir))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->nDir = nDir;
+  return SVGPU_OK;
+}
+
+int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu_newton_opts* opts,
+                     const double* dirY, const double* dirA, const double* Ao, const double* Yo, const double* Do,
+                     double* An, double* Yn, double* Dn, double* iNorm, double* pNorm, svgpu_ls_stats* stats) {
+  if (!ctx || !props || !opts || !Ao || !Yo || !Do || !An || !Yn || !Dn || !iNorm || !pNorm) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh || !ctx->ls_created) return set_err(ctx, SVGPU_ESTATE, "fluid_step before mesh/ls set-up");
+  if (opts->maxItr < 1) return set_err(ctx, SVGPU_EINVAL, "fluid_step: maxItr < 1");
+  const long n4 = 4L * ctx->nNo;
+  int rc;
+  // Ao..Dn are copied into the context's own (aligned) buffers; no alignment rule here.
+  if ((rc = to_device(ctx, ctx->Ao, Ao, n4))) return rc;
+  if ((rc = to_device(ctx, ctx->Yo, Yo, n4))) return rc;
+  if ((rc = to_device(ctx, ctx->Do, Do, n4))) return rc;
+  SVGPU_CUDA(ctx, ctx->An.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Yn.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Dn.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Ag.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Yg.resize(n4));
+  if (ctx->nDir > 0) {
+    if (!dirY || !dirA) return set_err(ctx, SVGPU_EINVAL, "fluid_step: Dirichlet values missing");
+    if ((rc = to_device(ctx, ctx->dirY, dirY, 3L * ctx->nDir))) return rc;
+    if ((rc = to_device(ctx, ctx->dirA, dirA, 3L * ctx->nDir))) return rc;
+  }
+  // picp (pic.cpp:591-767) and the strong Dirichlet values (set_bc_dir)
+  launch_pic_predict(ctx->stream, n4, (props->gam - 1.0) / props->gam, ctx->Ao.p, ctx->Yo.p, ctx->Do.p, ctx->An.p,
+                     ctx->Yn.p, ctx->Dn.p);
+  launch_set_dirichlet(ctx->stream, ctx->nDir, ctx->dirNodes.p, ctx->dirY.p, ctx->dirA.p, ctx->An.p, ctx->Yn.p);
+  ctx->launches += 2;
+  std::vector<int> incL(ctx->nFaces, 1);
+  int itr = 0;
+  for (;;) {
+    itr++;
+    launch_pic_initiate(ctx->stream, n4, props->am, props->af, ctx->Ao.p, ctx->An.p, ctx->Yo.p, ctx->Yn.p, ctx->Ag.p,
+                        ctx->Yg.p);
+    ctx->launches++;
+    if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr, opts->precision)))
+      return rc;
+    if (opts->outletFace >= 0) {
+      rc = backflow_device(ctx, opts->outletFace, props, opts->outletH, ctx->Yg.p, ctx->R.p,
+                           opts->precision == SVGPU_FP64 ? ctx->Val.p : nullptr,
+                           opts->precision == SVGPU_FP64 ? nullptr : ctx->Val32.p);
+      if (rc) return rc;
+    }
+    svgpu_ls_stats st;
+    std::memset(&st, 0, sizeof(st));
+    if (opts->precision != SVGPU_FP64) return set_err(ctx, SVGPU_EINVAL, "mixed-precision solve not built yet");
+    if ((rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st))) return rc;
+    if (stats) stats[itr - 1] = st;
+    // picc (pic.cpp:74-281)
+    launch_pic_correct(ctx->stream, n4, props->gam * props->dt, props->beta * props->dt * props->dt, ctx->R.p,
+                       ctx->An.p, ctx->Yn.p, ctx->Dn.p);
+    ctx->launches++;
+    const double eps = 2.220446049250313e-16;
+    auto is_zero = [&](double v) { double a = std::fabs(v); return a / std::fmax(a, eps) < 10.0 * eps; };
+    double iN = st.iNorm;
+    if (is_zero(iN)) iN = eps;
+    if (is_zero(*iNorm)) *iNorm = iN;
+    if (itr == 1) *pNorm = iN / *iNorm;
+    const double r1 = iN / *iNorm;
+    const bool l1 = itr >= opts->maxItr, l2 = r1 <= opts->tol, l3 = r1 <= opts->tol * *pNorm,
+               l4 = itr >= opts->minItr;
+    if (l1 || ((l2 || l3) && l4)) break;
+  }
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(An, ctx->An.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, ctx->Yn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, ctx->Dn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return itr;
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+// Internal declarations of the svgpu library: the context object behind the C ABI,
+// device buffers, launch helpers and the kernel entry points of each .cu file.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/svgpu.h"
+
+namespace svgpu {
+
+// Owning device allocation of n elements of T.
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  // (Re)allocates when the size changes; contents are undefined afterwards.
+  cudaError_t resize(size_t count) {
+    if (count == n && p) return cudaSuccess;
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// A face of the linear system (FSILS_faceType, fils_struct.hpp:117-160).
+struct LsFace {
+  bool created = false;
+  int nNo = 0, dof = 0, bGrp = SVGPU_BC_DIR;
+  std::vector<int> glob;
+  std::vector<double> val;  // (dof, nNo)
+  DevBuf<int> d_glob;
+  DevBuf<double> d_val;
+};
+
+// A boundary face of the mesh (faceType, ComMod.h:520) with its scatter data.
+struct MeshFace {
+  int nEl = 0;
+  DevBuf<int> fien;      // (3, nEl) in colour order
+  DevBuf<int> inner;     // interior node of the owner tet, per face element
+  DevBuf<uint8_t> boff;  // (nEl, 9) block offsets within the CSR rows
+  std::vector<int> color_start;
+};
+
+// Element colouring and block offsets of the volume mesh.
+struct MeshData {
+  int nNo = 0, nEl = 0;
+  DevBuf<int> ien;       // (4, nEl), elements permuted into colour order
+  DevBuf<int> elem_id;   // original element id of each permuted element
+  DevBuf<double> x4;     // (4, nNo): x, y, z, 0 -- 32-byte aligned node records
+  DevBuf<uint8_t> boff;  // (nEl, 16) offset of block (a,b) within row ien[a]
+  std::vector<int> color_start;  // nColors + 1
+};
+
+struct KrylovWork {
+  int sD = 0;
+  size_t n = 0;
+  DevBuf<double> V;        // (sD+1) basis vectors of length n
+  DevBuf<double> X, Wc, mask, tmp;
+  DevBuf<double> hess;     // (sD+1, sD) column-major, + c, s, err, y
+  DevBuf<double> givens;   // c[sD], s[sD], err[sD+1], y[sD]
+  DevBuf<double> partial;  // per-CTA partial dot products
+  DevBuf<double> scal;     // small scalars: eps, norms
+  DevBuf<int> flags;       // [0] converged, [1] last_i, [2] breakdown
+};
+
+}  // namespace svgpu
+
+struct svgpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  long long launches = 0;
+  int sm_count = 0;
+
+  // linear-system layout (fsils_lhs_create)
+  int nNo = 0, nnz = 0, nFaces = 0;
+  std::vector<int> h_rowPtr, h_colPtr;
+  svgpu::DevBuf<int> rowPtr, colPtr, diagPtr, blkRow;
+  std::vector<svgpu::LsFace> faces;
+
+  // solver settings (fsils_ls_create)
+  int lsType = SVGPU_LS_GMRES;
+  double relTol = 0.1, absTol = 1e-10;
+  int mItr = 4, sD = 250;
+  bool ls_created = false;
+
+  // mesh
+  std::unique_ptr<svgpu::MeshData> mesh;
+  std::map<int, std::unique_ptr<svgpu::MeshFace>> mfaces;
+  int nDir = 0;
+  svgpu::DevBuf<int> dirNodes;
+
+  // resident system and Newton state
+  svgpu::DevBuf<double> R, Val;
+  svgpu::DevBuf<float> Val32;
+  svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
+  svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
+  svgpu::KrylovWork kw;
+  // host staging
+  svgpu::DevBuf<double> stage1, stage2;
+};
+
+namespace svgpu {
+
+// Records a CUDA error into the context and returns SVGPU_ECUDA.
+int cuda_fail(svgpu_ctx* ctx, cudaError_t e, const char* what);
+int set_err(svgpu_ctx* ctx, int status, const std::string& msg);
+bool is_device_ptr(const void* p);
+
+#define SVGPU_CUDA(ctx, call)                                \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return svgpu::cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+inline int grid_for(long n, int block, int cap = 152 * 16) {
+  long g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+// ---- k_krylov.cu -------------------------------------------------------------
+void launch_spmv4_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr,
+                      const double* Val, const double* x, double* y);
+void launch_spmv_generic(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr,
+                         const double* Val, const double* x, double* y);
+void launch_diag_w(cudaStream_t s, int nNo, int dof, const int* diagPtr, const double* Val,
+                   const double* mask, double* W);
+void launch_scale_val(cudaStream_t s, long nnz, int dof, const int* blkRow, const int* colPtr,
+                      const double* W, double* Val);
+void launch_vmul(cudaStream_t s, long n, const double* a, double* b);  // b *= a
+void launch_fill(cudaStream_t s, long n, double v, double* a);
+void launch_mask_face(cudaStream_t s, int nNo, int fdof, int dof, const int* glob, const double* val, double* mask);
+// Partial dot products <V_j, w> for j in [0, m), per CTA; returns the CTA count used.
+int launch_multidot(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
+                    double* partial, int sm_count);
+void launch_reduce_partials(cudaStream_t s, int nparts, int m, const double* partial, double* out);
+void launch_residual_init(cudaStream_t s, long n, const double* R, double* u0, double* X, bool x_zero,
+                          const double* AX);
+void launch_scale_by_inv_norm(cudaStream_t s, long n, double* u, const double* nrm2, double* err0,
+                              const int* flags);
+void launch_cgs_update(cudaStream_t s, long n, int i, double* V, long ldv, const double* hcol,
+                       const int* flags);
+void launch_givens(cudaStream_t s, int i, int sD, double* hess, double* givens, const double* eps,
+                   int* flags);
+void launch_backsolve(cudaStream_t s, int sD, const double* hess, double* givens, const int* flags);
+void launch_xupdate(cudaStream_t s, long n, int sD, const double* V, long ldv, const double* givens,
+                    const int* flags, double* X);
+void launch_norm2(cudaStream_t s, long n, const double* a, double* partial, double* out, int sm_count);
+void launch_axpby(cudaStream_t s, long n, double a, const double* x, double b, double* y);
+
+// ---- k_fluid.cu ----------------------------------------------------------------
+struct FluidConsts {
+  double rho, mu, f0, f1, f2, kd, beta_bf, dt, am, af, gam;
+};
+void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, int e0, int ne,
+                           const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
+                           const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,
+                           double* R, double* Val64, float* Val32, int* errflag);
+void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
+                         const int* fien, const int* inner, const uint8_t* boff, const double* x4,
+                         const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32);
+void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
+                        const double* Do, double* An, double* Yn, double* Dn);
+void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,
+                          const double* dirA, double* An, double* Yn);
+void launch_pic_initiate(cudaStream_t s, long n4, double am, double af, const double* Ao,
+                         const double* An, const double* Yo, const double* Yn, double* Ag, double* Yg);
+void launch_pic_correct(cudaStream_t s, long n4, double c0, double c1, const double* R, double* An,
+                        double* Yn, double* Dn);
+void launch_f64_to_f32(cudaStream_t s, long n, const double* a, float* b);
+
+}  // namespace svgpu

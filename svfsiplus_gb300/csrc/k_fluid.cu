@@ -1,0 +1,484 @@
+// Fluid element assembly for sm_103a: VMS P1-P1 tets (construct_fluid,
+// solver/fluid.cpp:464-708; fluid_3d_m :1697-2139; fluid_3d_c :1389-1689; gnn
+// nn.cpp:455-550), the outlet Neumann/backflow faces (b_assem_neu_bc,
+// eq_assem.cpp:58-172; b_fluid, fluid.cpp:46-133) and the generalised-alpha
+// state updates (pic.cpp:74-767).
+//
+// One thread per element.  For linear tets the shape-function gradients are constant
+// and Nwxx = 0, so every entry of the 16 tangent blocks is a sum over the four Gauss
+// points of outer products of per-node vectors.  The kernel accumulates those sums
+// (a 4x4 matrix S for the three momentum diagonal blocks, a handful of 4-vectors and
+// scalars) while it walks the Gauss points, then forms each 4x4 block from them and
+// adds it into Val.  That is the reference's integrand, summed in a different order:
+// about a third of the reference's floating-point work per element.
+//
+// Scatter: elements arrive grouped by colour (no two elements of a colour share a
+// node), so the read-modify-write of R and Val needs no atomics and is deterministic.
+// The position of block (a,b) is rowPtr[ien[a]] + boff[e][a*4+b] (precomputed).
+#include "internal.h"
+
+namespace svgpu {
+
+namespace {
+
+// utils::is_zero(v, 0) (utils.cpp:170-189)
+template <typename T>
+__device__ __forceinline__ bool is_zero_ref(T v) {
+  const double a = fabs((double)v);
+  const double eps = 2.220446049250313e-16;
+  return a / fmax(a, eps) < 10.0 * eps;
+}
+
+template <typename T>
+struct Tet4Quad {
+  T N[4][4];  // [g][a]
+  T SN;       // sum_g N_g(a): the same for every a
+};
+
+template <typename T>
+__device__ __forceinline__ void tet4_quad(Tet4Quad<T>& q) {
+  // nn_elem_gip.h:501-515 with qmTET4 = (5 + 3 sqrt 5)/20 (ComMod.h:1011)
+  const double s = (5.0 + 3.0 * 2.23606797749978969640917366873) / 20.0;
+  const double t = (1.0 - s) / 3.0;
+  const double xi[4][3] = {{s, t, t}, {t, s, t}, {t, t, s}, {t, t, t}};
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    q.N[g][0] = (T)xi[g][0];
+    q.N[g][1] = (T)xi[g][1];
+    q.N[g][2] = (T)xi[g][2];
+    q.N[g][3] = (T)(1.0 - xi[g][0] - xi[g][1] - xi[g][2]);
+  }
+  q.SN = (T)(s + 3.0 * t);
+}
+
+template <typename TV>
+__device__ __forceinline__ void add_block(TV* __restrict__ dst, const double (&blk)[16]);
+
+template <>
+__device__ __forceinline__ void add_block<double>(double* __restrict__ dst, const double (&blk)[16]) {
+  double2* d = reinterpret_cast<double2*>(dst);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    double2 v = d[q];
+    v.x += blk[2 * q];
+    v.y += blk[2 * q + 1];
+    d[q] = v;
+  }
+}
+
+template <>
+__device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const double (&blk)[16]) {
+  float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    float4 v = d[q];
+    v.x += (float)blk[4 * q];
+    v.y += (float)blk[4 * q + 1];
+    v.z += (float)blk[4 * q + 2];
+    v.w += (float)blk[4 * q + 3];
+    d[q] = v;
+  }
+}
+
+// T: arithmetic type of the element integrals; TV: storage type of Val.
+template <typename T, typename TV>
+__global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, int ne,
+                                                       const int* __restrict__ ien,
+                                                       const uint8_t* __restrict__ boff,
+                                                       const int* __restrict__ elem_id,
+                                                       const double* __restrict__ x4,
+                                                       const double* __restrict__ Ag,
+                                                       const double* __restrict__ Yg,
+                                                       const double* __restrict__ Bf,
+                                                       const int* __restrict__ rowPtr,
+                                                       double* __restrict__ R, TV* __restrict__ Val,
+                                                       int* __restrict__ errflag) {
+  const int le = blockIdx.x * blockDim.x + threadIdx.x;
+  if (le >= ne) return;
+  const int e = e0 + le;
+  int nd[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) nd[a] = ien[4L * e + a];
+
+  // gather: coordinates, acceleration, velocity/pressure, body force
+  T xl[4][3], al[4][3], yl[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const double2 x01 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a]);
+    const double2 x23 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a] + 2);
+    const double2 a01 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a]);
+    const double2 a23 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a] + 2);
+    const double2 y01 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a]);
+    const double2 y23 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a] + 2);
+    xl[a][0] = (T)x01.x; xl[a][1] = (T)x01.y; xl[a][2] = (T)x23.x;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    if (Bf) { b0 = Bf[3L * nd[a]]; b1 = Bf[3L * nd[a] + 1]; b2 = Bf[3L * nd[a] + 2]; }
+    al[a][0] = (T)(a01.x - b0); al[a][1] = (T)(a01.y - b1); al[a][2] = (T)(a23.x - b2);
+    yl[a][0] = (T)y01.x; yl[a][1] = (T)y01.y; yl[a][2] = (T)y23.x; yl[a][3] = (T)y23.y;
+  }
+
+  // gnn (nn.cpp:489-545): xXi(i,j) = sum_a x(i,a) dN_a/dxi_j with dN/dxi = (I; -1 -1 -1)
+  T J[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    J[i][0] = xl[0][i] - xl[3][i];
+    J[i][1] = xl[1][i] - xl[3][i];
+    J[i][2] = xl[2][i] - xl[3][i];
+  }
+  const T Jac = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] + J[0][2] * J[1][0] * J[2][1] -
+                J[0][0] * J[1][2] * J[2][1] - J[0][1] * J[1][0] * J[2][2] - J[0][2] * J[1][1] * J[2][0];
+  if (is_zero_ref(Jac)) {
+    if (atomicCAS(errflag, 0, SVGPU_EJAC) == 0) errflag[1] = elem_id ? elem_id[e] : e;
+    return;
+  }
+  const T iJ = (T)1 / Jac;
+  T xiX[3][3];
+  xiX[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * iJ;
+  xiX[0][1] = (J[2][1] * J[0][2] - J[2][2] * J[0][1]) * iJ;
+  xiX[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * iJ;
+  xiX[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * iJ;
+  xiX[1][1] = (J[2][2] * J[0][0] - J[2][0] * J[0][2]) * iJ;
+  xiX[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * iJ;
+  xiX[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * iJ;
+  xiX[2][1] = (J[2][0] * J[0][1] - J[2][1] * J[0][0]) * iJ;
+  xiX[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * iJ;
+  T K[3][3];  // metric ks = xiX^T xiX (symmetric)
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) K[i][j] = xiX[0][i] * xiX[0][j] + xiX[1][i] * xiX[1][j] + xiX[2][i] * xiX[2][j];
+  T Nx[3][4];  // dN_a/dx_k
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    Nx[k][0] = xiX[0][k];
+    Nx[k][1] = xiX[1][k];
+    Nx[k][2] = xiX[2][k];
+    Nx[k][3] = -(xiX[0][k] + xiX[1][k] + xiX[2][k]);
+  }
+
+  const T rho = (T)c.rho, mu = (T)c.mu, kd = (T)c.kd;
+  const T T1c = (T)(c.af * c.gam * c.dt);
+  const T amd = (T)(c.am / (c.af * c.gam * c.dt));
+  const T w = Jac * (T)(1.0 / 24.0);
+  const T wl = w * T1c;
+  // tauM pieces that do not depend on the Gauss point (fluid.cpp:1924-1941)
+  const T kT = (T)(4.0 / (c.dt * c.dt)) + (kd * mu / rho) * (kd * mu / rho);
+  T kS = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) kS += K[i][j] * K[i][j];
+  kS = (T)36 * kS * (mu / rho) * (mu / rho);
+  const T trK = K[0][0] + K[1][1] + K[2][2];
+
+  Tet4Quad<T> q;
+  tet4_quad(q);
+
+  // element sums over the Gauss points
+  T S[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) S[a][b] = 0;
+  T sTauC = 0, sTauM = 0, Qv[4] = {0, 0, 0, 0}, Gv[4] = {0, 0, 0, 0};
+  T RV[4][3], RM[3][3], RC[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < 4; a++) RV[a][0] = RV[a][1] = RV[a][2] = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) RM[i][0] = RM[i][1] = RM[i][2] = 0;
+
+#pragma unroll 1
+  for (int g = 0; g < 4; g++) {
+    const T* N = q.N[g];
+    // kinematics at the Gauss point (fluid.cpp:1745-1790)
+    T ud[3] = {(T)-c.f0, (T)-c.f1, (T)-c.f2}, u[3] = {0, 0, 0}, ux[3][3], p = 0, px[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; k++) ux[k][0] = ux[k][1] = ux[k][2] = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        ud[i] += N[a] * al[a][i];
+        u[i] += N[a] * yl[a][i];
+#pragma unroll
+        for (int k = 0; k < 3; k++) ux[k][i] += Nx[k][a] * yl[a][i];
+      }
+      p += N[a] * yl[a][3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) px[k] += Nx[k][a] * yl[a][3];
+    }
+    const T divU = ux[0][0] + ux[1][1] + ux[2][2];
+    // stabilisation (fluid.cpp:1922-1995)
+    T kU = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) kU += u[i] * u[j] * K[i][j];
+    const T tauM = (T)1 / (rho * sqrt(kT + kU + kS));
+    T up[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const T rV = ud[i] + u[0] * ux[0][i] + u[1] * ux[1][i] + u[2] * ux[2][i];
+      up[i] = -tauM * (rho * rV + px[i] + mu * kd * u[i]);
+    }
+    const T tauC = (T)1 / (tauM * trK);
+    T tauB = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) tauB += up[i] * up[j] * K[i][j];
+    if (is_zero_ref(tauB)) tauB = (T)2.220446049250313e-16;
+    tauB = rho / sqrt(tauB);
+    const T ua[3] = {u[0] + up[0], u[1] + up[1], u[2] + up[2]};
+    const T pa = p - tauC * divU;
+    // residual pieces (fluid.cpp:2002-2036)
+    T rVb[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) rVb[i] = tauB * (up[0] * ux[0][i] + up[1] * ux[1][i] + up[2] * ux[2][i]);
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const T es = ux[k][i] + ux[i][k];
+        T r = mu * es - rho * up[i] * ua[k] + rVb[i] * up[k];
+        if (i == k) r -= pa;
+        RM[k][i] += r;
+      }
+    T rV2[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      rV2[i] = rho * (ud[i] + ua[0] * ux[0][i] + ua[1] * ux[1][i] + ua[2] * ux[2][i]) + mu * kd * ua[i];
+    T uNx[4], upNx[4], uaNx[4], T1b[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      uNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
+      upNx[a] = up[0] * Nx[0][a] + up[1] * Nx[1][a] + up[2] * Nx[2][a];
+      uaNx[a] = uNx[a] + upNx[a];
+      T1b[a] = -rho * uNx[a] - mu * kd * N[a];
+#pragma unroll
+      for (int i = 0; i < 3; i++) RV[a][i] += N[a] * rV2[i];
+      RC[a] += N[a] * divU - upNx[a];
+    }
+    // tangent sums (fluid.cpp:2058-2130 and 1662-1688)
+    const T mcoef = rho * amd + mu * kd;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const T al_a = rho * tauM * uaNx[a];
+      const T ga = rho * N[a];
+      const T ea = tauB * upNx[a];
+      const T ma = mcoef * N[a];
+#pragma unroll
+      for (int b = 0; b < 4; b++)
+        S[a][b] += ma * N[b] + al_a * (rho * amd * N[b] - T1b[b]) + ga * (uNx[b] + upNx[b]) + ea * upNx[b];
+      Qv[a] += al_a;
+      Gv[a] += tauM * (T1b[a] - rho * amd * N[a]);
+    }
+    sTauC += tauC;
+    sTauM += tauM;
+  }
+
+  // residual rows (lR, fluid.cpp:2038-2040, 1658-1660)
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    double* Ra = R + 4L * nd[a];
+    double r0 = (double)(w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]));
+    double r1 = (double)(w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]));
+    double r2 = (double)(w * (RV[a][2] + Nx[0][a] * RM[0][2] + Nx[1][a] * RM[1][2] + Nx[2][a] * RM[2][2]));
+    double r3 = (double)(w * RC[a]);
+    double2 v01 = *reinterpret_cast<double2*>(Ra);
+    double2 v23 = *reinterpret_cast<double2*>(Ra + 2);
+    v01.x += r0; v01.y += r1; v23.x += r2; v23.y += r3;
+    *reinterpret_cast<double2*>(Ra) = v01;
+    *reinterpret_cast<double2*>(Ra + 2) = v23;
+  }
+
+  // tangent blocks
+  const T c4mu = wl * (T)4 * mu, cTC = wl * sTauC, cTM = wl * sTauM, cSN = wl * q.SN;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int rowbase = rowPtr[nd[a]];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const T NxNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
+      double blk[16];
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+          T v;
+          if (r == cc)
+            v = (c4mu + cTC) * Nx[r][a] * Nx[r][b] + c4mu * NxNx + wl * S[a][b];
+          else
+            v = c4mu * Nx[cc][a] * Nx[r][b] + cTC * Nx[r][a] * Nx[cc][b];
+          blk[4 * r + cc] = (double)v;
+        }
+        blk[4 * r + 3] = (double)(-(cSN * Nx[r][a] - wl * Nx[r][b] * Qv[a]));
+      }
+#pragma unroll
+      for (int cc = 0; cc < 3; cc++) blk[12 + cc] = (double)(cSN * Nx[cc][b] - wl * Nx[cc][a] * Gv[b]);
+      blk[15] = (double)(cTM * NxNx);
+      const long pos = rowbase + boff[16L * e + 4 * a + b];
+      add_block<TV>(Val + 16 * pos, blk);
+    }
+  }
+}
+
+// Outlet faces: Neumann value h plus backflow stabilisation (b_fluid), one thread
+// per face triangle, faces grouped by colour.
+template <typename TV>
+__global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, const int* __restrict__ fien,
+                                    const int* __restrict__ inner, const uint8_t* __restrict__ boff,
+                                    const double* __restrict__ x4, const double* __restrict__ Yg,
+                                    const int* __restrict__ rowPtr, double* __restrict__ R, TV* __restrict__ Val) {
+  const int le = blockIdx.x * blockDim.x + threadIdx.x;
+  if (le >= ne) return;
+  const int e = e0 + le;
+  int nd[3];
+  for (int a = 0; a < 3; a++) nd[a] = fien[3L * e + a];
+  // TRI3 quadrature, qmTRI3 = 2/3 (nn_elem_gip.h:747-764)
+  const double s = 2.0 / 3.0, t = -0.5 * s + 0.5;
+  const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  // normal (gnnb, nn.cpp:727-760): d x/d xi_1 = x0 - x2, d x/d xi_2 = x1 - x2
+  double xa[3][3];
+  for (int a = 0; a < 3; a++)
+    for (int i = 0; i < 3; i++) xa[a][i] = x4[4L * nd[a] + i];
+  double g1[3], g2[3];
+  for (int i = 0; i < 3; i++) { g1[i] = xa[0][i] - xa[2][i]; g2[i] = xa[1][i] - xa[2][i]; }
+  double n[3] = {g1[1] * g2[2] - g1[2] * g2[1], g1[2] * g2[0] - g1[0] * g2[2], g1[0] * g2[1] - g1[1] * g2[0]};
+  const int in = inner[e];
+  double nv = 0.0;
+  for (int i = 0; i < 3; i++) nv += n[i] * (xa[0][i] - x4[4L * in + i]);
+  if (nv < 0.0) for (int i = 0; i < 3; i++) n[i] = -n[i];
+  const double Jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  for (int i = 0; i < 3; i++) n[i] /= Jac;
+  const double w = Jac / 6.0;
+  const double wl = w * c.af * c.gam * c.dt;
+  double yl[3][3];
+  for (int a = 0; a < 3; a++)
+    for (int i = 0; i < 3; i++) yl[a][i] = Yg[4L * nd[a] + i];
+  double lR[3][3] = {{0}}, lk[3][3] = {{0}};
+  for (int g = 0; g < 3; g++) {
+    const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
+    double y[3] = {0, 0, 0};
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 3; i++) y[i] += N[a] * yl[a][i];
+    double udn = y[0] * n[0] + y[1] * n[1] + y[2] * n[2];
+    udn = 0.5 * c.beta_bf * c.rho * (udn - fabs(udn));
+    const double hh = h * (N[0] + N[1] + N[2]);
+    for (int a = 0; a < 3; a++) {
+      for (int i = 0; i < 3; i++) lR[a][i] -= w * N[a] * (hh * n[i] + udn * y[i]);
+      for (int b = 0; b < 3; b++) lk[a][b] -= wl * N[a] * N[b] * udn;
+    }
+  }
+  for (int a = 0; a < 3; a++) {
+    double* Ra = R + 4L * nd[a];
+    for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
+    const int rowbase = rowPtr[nd[a]];
+    for (int b = 0; b < 3; b++) {
+      double blk[16] = {0};
+      blk[0] = blk[5] = blk[10] = lk[a][b];
+      const long pos = rowbase + boff[9L * e + 3 * a + b];
+      add_block<TV>(Val + 16 * pos, blk);
+    }
+  }
+}
+
+__global__ void pic_predict_kernel(long n4, double coef, const double* __restrict__ Ao, const double* __restrict__ Yo,
+                                   const double* __restrict__ Do, double* __restrict__ An, double* __restrict__ Yn,
+                                   double* __restrict__ Dn) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long)gridDim.x * blockDim.x) {
+    An[i] = Ao[i] * coef;
+    Yn[i] = Yo[i];
+    Dn[i] = Do[i];
+  }
+}
+
+__global__ void set_dirichlet_kernel(int nDir, const int* __restrict__ nodes, const double* __restrict__ dirY,
+                                     const double* __restrict__ dirA, double* __restrict__ An, double* __restrict__ Yn) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nDir) return;
+  const long a = nodes[k];
+  for (int i = 0; i < 3; i++) {
+    An[4 * a + i] = dirA[3L * k + i];
+    Yn[4 * a + i] = dirY[3L * k + i];
+  }
+}
+
+__global__ void pic_initiate_kernel(long n4, double am, double af, const double* __restrict__ Ao,
+                                    const double* __restrict__ An, const double* __restrict__ Yo,
+                                    const double* __restrict__ Yn, double* __restrict__ Ag, double* __restrict__ Yg) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long)gridDim.x * blockDim.x) {
+    Ag[i] = Ao[i] * (1.0 - am) + An[i] * am;
+    Yg[i] = Yo[i] * (1.0 - af) + Yn[i] * af;
+  }
+}
+
+__global__ void pic_correct_kernel(long n4, double c0, double c1, const double* __restrict__ R, double* __restrict__ An,
+                                   double* __restrict__ Yn, double* __restrict__ Dn) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long)gridDim.x * blockDim.x) {
+    const double r = R[i];
+    An[i] = An[i] - r;
+    Yn[i] = Yn[i] - r * c0;
+    Dn[i] = Dn[i] - r * c1;
+  }
+}
+
+__global__ void f64_to_f32_kernel(long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+}  // namespace
+
+void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, int e0, int ne,
+                           const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
+                           const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,
+                           double* R, double* Val64, float* Val32, int* errflag) {
+  if (ne <= 0) return;
+  const int block = 128;
+  const int grid = (ne + block - 1) / block;
+  if (precision == SVGPU_FP64)
+    fluid_p1_kernel<double, double><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr,
+                                                            R, Val64, errflag);
+  else
+    fluid_p1_kernel<float, float><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr,
+                                                          R, Val32, errflag);
+}
+
+void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
+                         const int* fien, const int* inner, const uint8_t* boff, const double* x4,
+                         const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32) {
+  if (ne <= 0) return;
+  const int grid = (ne + 127) / 128;
+  if (Val64)
+    neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, Yg, rowPtr, R, Val64);
+  else
+    neu_backflow_kernel<float><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, Yg, rowPtr, R, Val32);
+}
+
+void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
+                        const double* Do, double* An, double* Yn, double* Dn) {
+  pic_predict_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, coef, Ao, Yo, Do, An, Yn, Dn);
+}
+
+void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,
+                          const double* dirA, double* An, double* Yn) {
+  if (nDir <= 0) return;
+  set_dirichlet_kernel<<<(nDir + 255) / 256, 256, 0, s>>>(nDir, nodes, dirY, dirA, An, Yn);
+}
+
+void launch_pic_initiate(cudaStream_t s, long n4, double am, double af, const double* Ao,
+                         const double* An, const double* Yo, const double* Yn, double* Ag, double* Yg) {
+  pic_initiate_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, am, af, Ao, An, Yo, Yn, Ag, Yg);
+}
+
+void launch_pic_correct(cudaStream_t s, long n4, double c0, double c1, const double* R, double* An,
+                        double* Yn, double* Dn) {
+  pic_correct_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, c0, c1, R, An, Yn, Dn);
+}
+
+void launch_f64_to_f32(cudaStream_t s, long n, const double* a, float* b) {
+  f64_to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, b);
+}
+
+}  // namespace svgpu

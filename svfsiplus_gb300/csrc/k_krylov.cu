@@ -1,0 +1,413 @@
+// FSILS linear-solver kernels for sm_103a: block-CSR SpMV, diagonal (Jacobi)
+// preconditioning and the pieces of restarted GMRES (classical Gram-Schmidt with the
+// Pythagorean sub-diagonal, Givens rotations, back substitution).
+//
+// Reference: liner_solver/spar_mul.cpp:191-258 (SpMV), precond.cpp:122-257
+// (precond_diag, pre_mul/pos_mul), gmres.cpp:450-629 (gmres_v), dot.cpp:134-171,
+// norm.cpp:67-112, omp_la.cpp:48-144.
+//
+// Every kernel that belongs to an Arnoldi iteration takes the solver's flag word and
+// returns at once when flags[0] (converged) or flags[2] (breakdown) is set, so that a
+// whole restart cycle can be launched as one CUDA graph and stop early on the device.
+#include "internal.h"
+
+namespace svgpu {
+
+namespace {
+
+__device__ __forceinline__ bool stopped(const int* flags) {
+  return flags != nullptr && (flags[0] != 0 || flags[2] != 0);
+}
+
+// Streaming 16-byte load that does not allocate in L1: the matrix is read once per
+// product and is far larger than the caches.
+__device__ __forceinline__ double2 ld_stream2(const double* p) {
+  return __ldcs(reinterpret_cast<const double2*>(p));
+}
+
+// y = K x for 4x4 blocks.  Four threads per block row: thread r owns output row r of
+// the node and reads the 32 contiguous bytes of row r of every block (two 128-bit
+// loads); the four threads of a node together read each 128-byte block once.
+__global__ void __launch_bounds__(256) spmv4_f64_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                        const int* __restrict__ colPtr,
+                                                        const double* __restrict__ Val,
+                                                        const double* __restrict__ x,
+                                                        double* __restrict__ y, const int* flags) {
+  if (stopped(flags)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 2;
+  const int r = (int)(t & 3);
+  if (row >= nNo) return;
+  const int s = rowPtr[row], e = rowPtr[row + 1];
+  double acc = 0.0;
+  for (int k = s; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    const double2 v0 = ld_stream2(Val + 16L * k + 4 * r);
+    const double2 v1 = ld_stream2(Val + 16L * k + 4 * r + 2);
+    const double2 x0 = *reinterpret_cast<const double2*>(x + 4L * col);
+    const double2 x1 = *reinterpret_cast<const double2*>(x + 4L * col + 2);
+    acc = acc + v0.x * x0.x + v0.y * x0.y + v1.x * x1.x + v1.y * x1.y;
+  }
+  y[4 * row + r] = acc;
+}
+
+// Any dof: one thread per (node, output row).
+__global__ void spmv_generic_kernel(int nNo, int dof, const int* __restrict__ rowPtr,
+                                    const int* __restrict__ colPtr, const double* __restrict__ Val,
+                                    const double* __restrict__ x, double* __restrict__ y) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t / dof;
+  const int l = (int)(t % dof);
+  if (row >= nNo) return;
+  const long d2 = (long)dof * dof;
+  double acc = 0.0;
+  for (int k = rowPtr[row]; k < rowPtr[row + 1]; k++) {
+    const int col = colPtr[k];
+    double sum = 0.0;
+    for (int c = 0; c < dof; c++) sum += Val[d2 * k + l * dof + c] * x[(long)dof * col + c];
+    acc += sum;
+  }
+  y[(long)dof * row + l] = acc;
+}
+
+// W = |diag K|^-1/2 (a zero diagonal counts as 1), times the Dirichlet mask
+// (precond.cpp:142-225).
+__global__ void diag_w_kernel(int nNo, int dof, const int* __restrict__ diagPtr,
+                              const double* __restrict__ Val, const double* __restrict__ mask,
+                              double* __restrict__ W) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nNo * dof) return;
+  const long a = t / dof;
+  const int i = (int)(t % dof);
+  double w = Val[(long)dof * dof * diagPtr[a] + i * dof + i];
+  if (w == 0.0) w = 1.0;
+  w = 1.0 / sqrt(fabs(w));
+  if (mask) w = w * mask[t];
+  W[t] = w;
+}
+
+// Val <- diag(W) Val diag(W), row factor first then column factor, as pre_mul then
+// pos_mul do (precond.cpp:46-111, 549-624).
+__global__ void scale_val_kernel(long nnz, int dof, const int* __restrict__ blkRow,
+                                 const int* __restrict__ colPtr, const double* __restrict__ W,
+                                 double* __restrict__ Val) {
+  const long d2 = (long)dof * dof;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnz * d2) return;
+  const long k = t / d2;
+  const int rc = (int)(t % d2);
+  const int r = rc / dof, c = rc % dof;
+  const double wr = W[(long)dof * blkRow[k] + r];
+  const double wc = W[(long)dof * colPtr[k] + c];
+  Val[t] = (Val[t] * wr) * wc;
+}
+
+__global__ void vmul_kernel(long n, const double* __restrict__ a, double* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = a[i] * b[i];
+}
+
+__global__ void fill_kernel(long n, double v, double* __restrict__ a) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+__global__ void mask_face_kernel(int nNo, int fdof, int dof, const int* __restrict__ glob,
+                                 const double* __restrict__ val, double* __restrict__ mask) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nNo) return;
+  const int n = fdof < dof ? fdof : dof;
+  for (int i = 0; i < n; i++) {
+    const long idx = (long)dof * glob[a] + i;
+    mask[idx] = mask[idx] * (val ? val[(long)fdof * a + i] : 0.0);
+  }
+}
+
+// Partial products <V_j, w>, j < m: each CTA streams its slice of the vectors once
+// per group of 8 basis vectors and writes one partial per j (fixed order, so the
+// result is the same on every run).
+template <int JB>
+__global__ void __launch_bounds__(256) multidot_kernel(long n, int m, const double* __restrict__ V,
+                                                       long ldv, const double* __restrict__ w,
+                                                       double* __restrict__ partial, const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ double red[JB][8];
+  const long chunk = (n + gridDim.x - 1) / gridDim.x;
+  const long beg = (long)blockIdx.x * chunk;
+  const long end = beg + chunk < n ? beg + chunk : n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < m; j0 += JB) {
+    double acc[JB];
+#pragma unroll
+    for (int q = 0; q < JB; q++) acc[q] = 0.0;
+    for (long k = beg + threadIdx.x; k < end; k += blockDim.x) {
+      const double wk = w[k];
+#pragma unroll
+      for (int q = 0; q < JB; q++)
+        if (j0 + q < m) acc[q] += __ldcs(V + (long)(j0 + q) * ldv + k) * wk;
+    }
+#pragma unroll
+    for (int q = 0; q < JB; q++) {
+      double v = acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < JB && j0 + threadIdx.x < m) {
+      double v = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += red[threadIdx.x][q];
+      partial[(long)blockIdx.x * m + j0 + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void reduce_partials_kernel(int nparts, int m, const double* __restrict__ partial,
+                                       double* __restrict__ out, const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ double red[8];
+  const int j = blockIdx.x;
+  double v = 0.0;
+  for (int c = threadIdx.x; c < nparts; c += blockDim.x) v += partial[(long)c * m + j];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += red[q];
+    out[j] = s;
+  }
+}
+
+// u0 = R - A X (A X given, or X = 0)
+__global__ void residual_init_kernel(long n, const double* __restrict__ R, double* __restrict__ u0,
+                                     const double* __restrict__ AX) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    u0[i] = AX ? R[i] - AX[i] : R[i];
+}
+
+// u0 /= sqrt(nrm2); err[0] = sqrt(nrm2); resets the cycle flags (gmres.cpp:523-524)
+__global__ void scale_inv_norm_kernel(long n, double* __restrict__ u, const double* __restrict__ nrm2,
+                                      double* __restrict__ err0, int* flags) {
+  const double nrm = sqrt(*nrm2);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    u[i] = u[i] / nrm;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *err0 = nrm;
+    if (flags) {
+      flags[0] = 0;
+      flags[1] = 0;
+      flags[2] = (nrm == 0.0 || !isfinite(nrm)) ? 1 : 0;
+    }
+  }
+}
+
+// u_{i+1} = (u_{i+1} - sum_j h(j,i) u_j) / h(i+1,i), subtracting in j order as
+// omp_sum_v does (gmres.cpp:561-569).  hcol holds the raw dot products and, at
+// index i+1, the sub-diagonal.
+__global__ void __launch_bounds__(256) cgs_update_kernel(long n, int i, double* __restrict__ V, long ldv,
+                                                         const double* __restrict__ hcol, const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ double hs[256];
+  for (int j = threadIdx.x; j <= i + 1; j += blockDim.x) hs[j] = hcol[j];
+  __syncthreads();
+  const double rinv = 1.0 / hs[i + 1];
+  double* w = V + (long)(i + 1) * ldv;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    double acc = w[k];
+    for (int j = 0; j <= i; j++) acc = acc + (-hs[j]) * __ldcs(V + (long)j * ldv + k);
+    w[k] = rinv * acc;
+  }
+}
+
+// One Arnoldi column: Pythagorean sub-diagonal, previous rotations, new rotation,
+// residual estimate and convergence test (gmres.cpp:561-592).  givens layout:
+// c[sD], s[sD], err[sD+1], y[sD], hraw[sD+2].
+__global__ void givens_kernel(int i, int sD, double* __restrict__ hess, double* __restrict__ g,
+                              const double* __restrict__ eps, int* flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (flags[0] != 0 || flags[2] != 0) return;
+  double* c = g;
+  double* s = g + sD;
+  double* err = g + 2 * sD;
+  double* hraw = g + 4 * sD + 1;
+  double* h = hess + (long)(sD + 1) * i;  // column i
+  double hsub = hraw[i + 1];
+  for (int j = 0; j <= i; j++) {
+    h[j] = hraw[j];
+    hsub = hsub - hraw[j] * hraw[j];
+  }
+  hsub = sqrt(fabs(hsub));
+  hraw[i + 1] = hsub;  // the update kernel divides by it
+  h[i + 1] = hsub;
+  for (int j = 0; j <= i - 1; j++) {
+    const double tmp = c[j] * h[j] + s[j] * h[j + 1];
+    h[j + 1] = -s[j] * h[j] + c[j] * h[j + 1];
+    h[j] = tmp;
+  }
+  const double tmp = sqrt(h[i] * h[i] + h[i + 1] * h[i + 1]);
+  c[i] = h[i] / tmp;
+  s[i] = h[i + 1] / tmp;
+  h[i] = tmp;
+  h[i + 1] = 0.0;
+  err[i + 1] = -s[i] * err[i];
+  err[i] = c[i] * err[i];
+  flags[1] = i;
+  if (!(hsub > 0.0) || !isfinite(err[i + 1])) flags[2] = 1;
+  if (fabs(err[i + 1]) < *eps) flags[0] = 1;
+}
+
+// y = H^-1 err by back substitution (gmres.cpp:595-607).
+__global__ void backsolve_kernel(int sD, const double* __restrict__ hess, double* __restrict__ g,
+                                 const int* flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int last = flags[1];
+  if (last >= sD) last = sD - 1;
+  const double* err = g + 2 * sD;
+  double* y = g + 3 * sD + 1;
+  for (int i = 0; i <= last; i++) y[i] = err[i];
+  for (int j = last; j >= 0; j--) {
+    for (int k = j + 1; k <= last; k++) y[j] = y[j] - hess[j + (long)(sD + 1) * k] * y[k];
+    y[j] = y[j] / hess[j + (long)(sD + 1) * j];
+  }
+}
+
+// X += sum_j y_j u_j, j = 0..last_i in order (gmres.cpp:609-611)
+__global__ void __launch_bounds__(256) xupdate_kernel(long n, int sD, const double* __restrict__ V, long ldv,
+                                                      const double* __restrict__ g, const int* flags,
+                                                      double* __restrict__ X) {
+  __shared__ double ys[256];
+  int last = flags[1];
+  if (last >= sD) last = sD - 1;
+  const double* y = g + 3 * sD + 1;
+  for (int j = threadIdx.x; j <= last; j += blockDim.x) ys[j] = y[j];
+  __syncthreads();
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    double acc = X[k];
+    for (int j = 0; j <= last; j++) acc = acc + ys[j] * __ldcs(V + (long)j * ldv + k);
+    X[k] = acc;
+  }
+}
+
+__global__ void axpby_kernel(long n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_spmv4_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr,
+                      const double* Val, const double* x, double* y) {
+  const long threads = 4L * nNo;
+  spmv4_f64_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y, nullptr);
+}
+
+void launch_spmv4_f64_flag(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr,
+                           const double* Val, const double* x, double* y, const int* flags) {
+  const long threads = 4L * nNo;
+  spmv4_f64_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y, flags);
+}
+
+void launch_spmv_generic(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr,
+                         const double* Val, const double* x, double* y) {
+  const long threads = (long)dof * nNo;
+  spmv_generic_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nNo, dof, rowPtr, colPtr, Val, x, y);
+}
+
+void launch_diag_w(cudaStream_t s, int nNo, int dof, const int* diagPtr, const double* Val,
+                   const double* mask, double* W) {
+  const long n = (long)nNo * dof;
+  diag_w_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(nNo, dof, diagPtr, Val, mask, W);
+}
+
+void launch_scale_val(cudaStream_t s, long nnz, int dof, const int* blkRow, const int* colPtr,
+                      const double* W, double* Val) {
+  const long n = nnz * dof * dof;
+  scale_val_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(nnz, dof, blkRow, colPtr, W, Val);
+}
+
+void launch_vmul(cudaStream_t s, long n, const double* a, double* b) {
+  vmul_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, b);
+}
+
+void launch_fill(cudaStream_t s, long n, double v, double* a) {
+  fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, v, a);
+}
+
+void launch_mask_face(cudaStream_t s, int nNo, int fdof, int dof, const int* glob, const double* val,
+                      double* mask) {
+  if (nNo <= 0) return;
+  mask_face_kernel<<<(nNo + 255) / 256, 256, 0, s>>>(nNo, fdof, dof, glob, val, mask);
+}
+
+int multidot_ctas(long n, int sm_count) {
+  long per = 4096;  // at least this many entries per CTA
+  long c = (n + per - 1) / per;
+  long cap = 2L * sm_count;
+  if (c > cap) c = cap;
+  if (c < 1) c = 1;
+  return (int)c;
+}
+
+int launch_multidot_flag(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
+                         double* partial, int sm_count, const int* flags) {
+  const int ctas = multidot_ctas(n, sm_count);
+  multidot_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  return ctas;
+}
+
+int launch_multidot(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
+                    double* partial, int sm_count) {
+  return launch_multidot_flag(s, n, m, V, ldv, w, partial, sm_count, nullptr);
+}
+
+void launch_reduce_partials_flag(cudaStream_t s, int nparts, int m, const double* partial, double* out,
+                                 const int* flags) {
+  reduce_partials_kernel<<<m, 256, 0, s>>>(nparts, m, partial, out, flags);
+}
+
+void launch_reduce_partials(cudaStream_t s, int nparts, int m, const double* partial, double* out) {
+  launch_reduce_partials_flag(s, nparts, m, partial, out, nullptr);
+}
+
+void launch_residual_init(cudaStream_t s, long n, const double* R, double* u0, double* X, bool x_zero,
+                          const double* AX) {
+  (void)X;
+  residual_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, R, u0, x_zero ? nullptr : AX);
+}
+
+void launch_scale_by_inv_norm(cudaStream_t s, long n, double* u, const double* nrm2, double* err0,
+                              const int* flags) {
+  scale_inv_norm_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, u, nrm2, err0, const_cast<int*>(flags));
+}
+
+void launch_cgs_update(cudaStream_t s, long n, int i, double* V, long ldv, const double* hcol,
+                       const int* flags) {
+  cgs_update_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, i, V, ldv, hcol, flags);
+}
+
+void launch_givens(cudaStream_t s, int i, int sD, double* hess, double* givens, const double* eps,
+                   int* flags) {
+  givens_kernel<<<1, 32, 0, s>>>(i, sD, hess, givens, eps, flags);
+}
+
+void launch_backsolve(cudaStream_t s, int sD, const double* hess, double* givens, const int* flags) {
+  backsolve_kernel<<<1, 32, 0, s>>>(sD, hess, givens, flags);
+}
+
+void launch_xupdate(cudaStream_t s, long n, int sD, const double* V, long ldv, const double* givens,
+                    const int* flags, double* X) {
+  xupdate_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, sD, V, ldv, givens, flags, X);
+}
+
+void launch_norm2(cudaStream_t s, long n, const double* a, double* partial, double* out, int sm_count) {
+  const int ctas = launch_multidot(s, n, 1, a, 0, a, partial, sm_count);
+  launch_reduce_partials(s, ctas, 1, partial, out);
+}
+
+void launch_axpby(cudaStream_t s, long n, double a, const double* x, double b, double* y) {
+  axpby_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, x, b, y);
+}
+
+}  // namespace svgpu

@@ -1,0 +1,173 @@
+"""GPU parity of the fluid hot path against the reference (golden vectors made by the
+reference solver itself) and against the CPU oracle, through the C ABI.
+
+Tolerances:
+* assembly, FP64: relative 1e-12 on R and Val (BASELINE: assembled residual rel err
+  <= 1e-12).  The GPU sums the Gauss-point integrand in a different order and uses
+  fused multiply-add, so it is not bitwise.
+* assembly, mixed (FP32 element integrals): relative 2e-5.
+* one GMRES solve: both sides stop at ||r||/||r0|| <= 1e-8 of the preconditioned
+  system; the increments agree to 1e-5 relative (the Krylov iterates drift apart
+  slowly once the reduction order differs).
+* time stepping: velocity and pressure relative L2 <= 1e-6 after every step
+  (BASELINE: <= 1e-6 after 10 steps).
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from svfsiplus_gb300 import api
+from svfsiplus_gb300.mesh import named_pipe
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_ctx(m, rowPtr, colPtr):
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(m.nNo, rowPtr, colPtr, 2)
+    ctx.fsils_bc_create(0, m.faces["inlet"].gN, 3, api.BC_TYPE_Dir)
+    ctx.fsils_bc_create(1, m.faces["wall"].gN, 3, api.BC_TYPE_Dir)
+    ctx.mesh_create(m.x, m.ien)
+    out = m.faces["outlet"]
+    ctx.face_create(api.FACE_OUTLET, out.ien, out.gE)
+    return ctx
+
+
+@pytest.mark.parametrize("name", ["tiny", "small", "pipe50k"])
+def test_assembly_fp64_matches_reference(golden, name):
+    g = golden(name)
+    m = named_pipe(name)
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    props = api.fluid_props()
+    R = np.zeros((m.nNo, 4))
+    Val = np.zeros((g["colPtr"].size, 16))
+    ctx.construct_fluid(props, np.ascontiguousarray(g["Ag"]), np.ascontiguousarray(g["Yg"]), R=R, Val=Val)
+    ctx.b_assem_neu_bc(api.FACE_OUTLET, props, 0.0, np.ascontiguousarray(g["Yg"]), R=R, Val=Val)
+    assert ctx.kernel_launches > 0
+    assert rel(R, g["R_asm"]) <= 1e-12
+    if "Val_asm" in g:
+        assert rel(Val, g["Val_asm"]) <= 1e-12
+    else:  # large case: against the oracle, which is bitwise equal to the reference
+        P = po.fluid_params()
+        Ro, Vo = po.construct_fluid(P, m.x, m.ien, g["Ag"], g["Yg"], g["rowPtr"], g["colPtr"])
+        out = m.faces["outlet"]
+        po.neu_backflow(P, out.ien, out.gE, m.ien, m.x, g["Yg"], g["rowPtr"], g["colPtr"], Ro, Vo)
+        assert rel(Val, Vo) <= 1e-12
+
+
+def test_assembly_is_deterministic(golden):
+    g = golden("small")
+    m = named_pipe("small")
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    props = api.fluid_props()
+    outs = []
+    for _ in range(2):
+        R = np.zeros((m.nNo, 4))
+        Val = np.zeros((g["colPtr"].size, 16))
+        ctx.construct_fluid(props, np.ascontiguousarray(g["Ag"]), np.ascontiguousarray(g["Yg"]), R=R, Val=Val)
+        outs.append((R, Val))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_fsils_solve_matches_reference(golden, name):
+    g = golden(name)
+    m = named_pipe(name)
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    ps = eval(str(g["params"]))
+    ctx.fsils_ls_create(api.LS_TYPE_GMRES, ps["ls_rel_tol"], ps["ls_abs_tol"], ps["ls_max_itr"], ps["ls_krylov_dim"])
+    Ri = np.array(g["R_asm"], copy=True)
+    Val = np.array(g["Val_asm"], copy=True)
+    st = ctx.fsils_solve(4, Ri, Val, api.PREC_FSILS, incL=np.ones(2, np.int32), res=np.zeros(2))
+    _, Vs_ref, ls_ref = po.fsils_solve_gmres(g["rowPtr"], g["colPtr"], g["Val_asm"], g["R_asm"],
+                                             _mask(m), sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"],
+                                             relTol=ps["ls_rel_tol"], absTol=ps["ls_abs_tol"])
+    assert rel(Val, Vs_ref) <= 1e-14            # preconditioner scaling: same operation order
+    assert abs(st.iNorm - ls_ref.iNorm) <= 1e-12 * ls_ref.iNorm
+    assert st.suc == 1
+    assert rel(Ri, g["dX"]) <= 1e-5
+    assert abs(st.itr - ls_ref.itr) <= max(5, 0.1 * ls_ref.itr)
+
+
+def _mask(m):
+    nodes, _ = po.dirichlet_nodes(m)
+    mask = np.ones((m.nNo, 4))
+    mask[nodes, :3] = 0.0
+    return mask
+
+
+def test_spar_mul_matches_oracle(golden):
+    g = golden("small")
+    m = named_pipe("small")
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    rng = np.random.default_rng(0)
+    U = rng.standard_normal((m.nNo, 4))
+    KU = np.zeros((m.nNo, 4))
+    ctx.spar_mul(4, np.ascontiguousarray(g["Val_asm"]), U, KU)
+    ref = po.spar_mul(g["rowPtr"], g["colPtr"], g["Val_asm"], U)
+    assert rel(KU, ref) <= 1e-14
+    # generic dof path (dof = 3, the mesh equation's layout)
+    K3 = rng.standard_normal((g["colPtr"].size, 9))
+    U3 = rng.standard_normal((m.nNo, 3))
+    KU3 = np.zeros((m.nNo, 3))
+    ctx.spar_mul(3, K3, U3, KU3)
+    assert rel(KU3, po.spar_mul(g["rowPtr"], g["colPtr"], K3, U3, dof=3)) <= 1e-14
+
+
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_time_steps_match_reference(golden, name):
+    g = golden(name)
+    m = named_pipe(name)
+    ps = eval(str(g["params"]))
+    s = api.PipeFluidSolver(m, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
+                            absTol=ps["ls_abs_tol"], newton_min=ps["newton_min"], newton_max=ps["newton_max"],
+                            newton_tol=ps["newton_tol"], rowPtr=g["rowPtr"], colPtr=g["colPtr"])
+    for step in range(1, ps["n_steps"] + 1):
+        st = s.step(u_mean=ps["u_mean"], u_amp=ps["u_amp"], freq=ps["u_freq"])
+        assert len(st) == ps["newton_max"]
+        ref = g[f"Yn_{step}"]
+        assert rel(s.Yn[:, :3], ref[:, :3]) <= 1e-6
+        assert rel(s.Yn[:, 3], ref[:, 3]) <= 1e-6
+
+
+def test_pipe50k_ten_steps_match_reference(golden):
+    """The CPU-runnable 50k-tet pipe, 10 gen-alpha steps, GMRES(50) + diagonal
+    preconditioner to 1e-8: velocity and pressure within 1e-6 of the reference."""
+    g = golden("pipe50k")
+    m = named_pipe("pipe50k")
+    ps = eval(str(g["params"]))
+    s = api.PipeFluidSolver(m, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
+                            absTol=ps["ls_abs_tol"], newton_min=ps["newton_min"], newton_max=ps["newton_max"],
+                            newton_tol=ps["newton_tol"], rowPtr=g["rowPtr"], colPtr=g["colPtr"])
+    errs = []
+    for step in range(1, 11):
+        s.step(u_mean=ps["u_mean"], u_amp=ps["u_amp"], freq=ps["u_freq"])
+        if f"Yn_{step}" in g:
+            ref = g[f"Yn_{step}"]
+            errs.append((rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])))
+    print("pipe50k per-field rel L2 (velocity, pressure):", errs)
+    for ev, ep in errs:
+        assert ev <= 1e-6 and ep <= 1e-6
+
+
+def test_zero_jacobian_reported_not_faulted():
+    """A collapsed element is an input error: the kernel flags it, the ABI returns
+    SVGPU_EJAC with the element id, and the context stays usable."""
+    m = named_pipe("tiny")
+    x = m.x.copy()
+    bad = m.ien[5]
+    x[bad[3]] = x[bad[0]]  # node 3 onto node 0: zero volume for element 5 (and neighbours)
+    rowPtr, colPtr = api.csr_pattern(m.nNo, m.ien)
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(m.nNo, rowPtr, colPtr, 0)
+    ctx.mesh_create(x, m.ien)
+    props = api.fluid_props()
+    z = np.zeros((m.nNo, 4))
+    with pytest.raises(RuntimeError, match="Jacobian"):
+        ctx.construct_fluid(props, z, z, R=np.zeros((m.nNo, 4)), Val=np.zeros((colPtr.size, 16)))
+    ctx.mesh_create(m.x, m.ien)
+    ctx.construct_fluid(props, z, z, R=np.zeros((m.nNo, 4)), Val=np.zeros((colPtr.size, 16)))
