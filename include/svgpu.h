@@ -67,6 +67,13 @@ long long svgpu_kernel_launches(const svgpu_ctx* ctx);
 /* Use a caller-owned cudaStream_t (passed as void*) instead of the context's own. */
 int svgpu_set_stream(svgpu_ctx* ctx, void* stream);
 
+/* ---- CSR pattern ------------------------------------------------------------------ */
+/* Replaces lhsa (solver/lhsa.cpp:153-380, without the undefNeu remap): the block
+ * sparsity of the element cliques, rows sorted.  Host arrays.  Call with
+ * colPtr == NULL to get nnz in *nnz (rowPtr, nNo+1 ints, is filled either way); then
+ * again with colPtr sized nnz.  Errors: an isolated node (lhsa.cpp:354-356). */
+int svgpu_lhsa(int nNo, int nEl, int eNoN, const int* IEN, int* rowPtr, int* colPtr, long long* nnz);
+
 /* ---- FSILS set-up (Code/Source/liner_solver/fsils_api.hpp:41-61) --------------- */
 /* Replaces fsils_lhs_create (liner_solver/lhs.cpp:57) for one rank: gnNo == nNo,
  * gNodes the identity.  Keeps rowPtr/colPtr, derives diagPtr. */

@@ -192,17 +192,19 @@ FACE_INLET, FACE_WALL, FACE_OUTLET = 0, 1, 2
 
 
 def csr_pattern(nNo: int, ien: np.ndarray):
-    """lhsa (lhsa.cpp:153): rowPtr/colPtr of the element cliques, sorted columns."""
-    ien = np.asarray(ien, dtype=np.int64)
-    e = ien.shape[1]
-    rows = np.repeat(ien, e, axis=1).ravel()
-    cols = np.tile(ien, (1, e)).ravel()
-    key = np.unique(rows * nNo + cols)
-    r = (key // nNo).astype(np.int64)
-    c = (key % nNo).astype(np.int32)
+    """lhsa (lhsa.cpp:153): rowPtr/colPtr of the element cliques, sorted columns
+    (native svgpu_lhsa)."""
+    ien = np.ascontiguousarray(ien, dtype=np.int32)
     rowPtr = np.zeros(nNo + 1, dtype=np.int32)
-    np.add.at(rowPtr, r + 1, 1)
-    return np.cumsum(rowPtr, dtype=np.int64).astype(np.int32), c
+    nnz = C.c_longlong(0)
+    rc = lib().svgpu_lhsa(int(nNo), int(ien.shape[0]), int(ien.shape[1]), _ptr(ien), _ptr(rowPtr), None,
+                          C.byref(nnz))
+    if rc != SVGPU_OK:
+        raise RuntimeError("lhsa: bad connectivity or an isolated node")
+    colPtr = np.zeros(nnz.value, dtype=np.int32)
+    lib().svgpu_lhsa(int(nNo), int(ien.shape[0]), int(ien.shape[1]), _ptr(ien), _ptr(rowPtr), _ptr(colPtr),
+                     C.byref(nnz))
+    return rowPtr, colPtr
 
 
 def dirichlet_nodes(mesh):
