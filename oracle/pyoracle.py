@@ -61,6 +61,7 @@ def lib():
         _lib.or_construct_fluid.restype = C.c_int
         _lib.or_fluid_element.restype = C.c_int
         _lib.or_fluid_step.restype = C.c_int
+        _lib.or_dot.restype = C.c_double
     return _lib
 
 
@@ -120,6 +121,14 @@ def spar_mul(rowPtr, colPtr, K, U, dof=4):
     lib().or_spar_mul(nNo, dof, _p(rowPtr), _p(colPtr), _p(np.ascontiguousarray(K)),
                       _p(np.ascontiguousarray(U)), _p(KU))
     return KU
+
+
+def dot(u, v):
+    return lib().or_dot(C.c_long(u.size), _p(u), _p(v))
+
+
+def axpy(r, U, V):
+    lib().or_axpy(C.c_long(U.size), C.c_double(r), _p(U), _p(V))
 
 
 def fsils_solve_gmres(rowPtr, colPtr, Val, R, dirMask, sD=50, mItr=100, relTol=1e-8, absTol=1e-17, dof=4):

@@ -467,6 +467,12 @@ static double dotv(long n, const double* u, const double* v) {
   return r;
 }
 
+double or_dot(long n, const double* u, const double* v) { return dotv(n, u, v); }
+
+void or_axpy(long n, double r, double* U, const double* V) {
+  for (long k = 0; k < n; k++) U[k] = U[k] + r * V[k];
+}
+
 void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
                           double* Val, double* R, const double* dirMask, or_ls* ls) {
   const long n = (long)nNo * dof;

@@ -72,6 +72,11 @@ typedef struct {
 void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
                           double* Val, double* R, const double* dirMask, or_ls* ls);
 
+/* fsils_nc_dot_v (dot.cpp:134-171) and omp_sum_v U += r V (omp_la.cpp:102-144) over n
+ * entries, the Krylov vector kernels of gmres_v. */
+double or_dot(long n, const double* u, const double* v);
+void or_axpy(long n, double r, double* U, const double* V);
+
 /* Block SpMV KU = K U (spar_mul.cpp:191-258, any dof). */
 void or_spar_mul(int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
                  const double* U, double* KU);
