@@ -168,7 +168,8 @@ def run_ours(args):
     s = api.PipeFluidSolver(mesh, device=local, sD=KRYLOV_DIM, mItr=MAX_RESTARTS, relTol=REL_TOL, absTol=1e-17,
                             newton_min=NEWTON_ITERS, newton_max=NEWTON_ITERS, newton_tol=1e-11,
                             precision=precision, rowPtr=rowPtr, colPtr=colPtr)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
     setup_s = time.time() - t0
     nNo = mesh.nNo

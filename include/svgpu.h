@@ -118,6 +118,11 @@ int svgpu_face_create(svgpu_ctx* ctx, int faceId, int nFaEl, const int* fIEN, co
  * Returns SVGPU_EJAC for a zero Jacobian. */
 int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag,
                           const double* Yg, const double* Bf, double* R, double* Val, int precision);
+/* Copies the resident system out: R (4,nNo) and Val (16,nnz) as FP64 (an FP32
+ * tangent from SVGPU_MIXED assembly is widened).  Either pointer may be NULL.  No
+ * counterpart in the reference, where R and Val live in ComMod (ComMod.h:1563-1566). */
+int svgpu_get_system(svgpu_ctx* ctx, double* R, double* Val);
+
 /* Replaces b_assem_neu_bc (solver/eq_assem.cpp:58) -> b_fluid (fluid.cpp:46) on one
  * face: Neumann value h on every face node plus backflow stabilisation. */
 int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h,

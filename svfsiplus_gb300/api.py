@@ -168,6 +168,10 @@ class Context:
         self._check(lib().svgpu_construct_fluid(self._h, C.byref(props), _ptr(Ag), _ptr(Yg), _ptr(Bf), _ptr(R),
                                                 _ptr(Val), int(precision)), "construct_fluid")
 
+    def get_system(self, R=None, Val=None):
+        """Copy the resident R (nNo,4) and Val (nnz,16) out as FP64."""
+        self._check(lib().svgpu_get_system(self._h, _ptr(R), _ptr(Val)), "get_system")
+
     def b_assem_neu_bc(self, face_id, props, h, Yg, R=None, Val=None):
         self._check(lib().svgpu_neu_bc_fluid(self._h, int(face_id), C.byref(props), C.c_double(h), _ptr(Yg),
                                              _ptr(R), _ptr(Val)), "b_assem_neu_bc")

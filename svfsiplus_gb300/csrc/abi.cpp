@@ -115,6 +115,7 @@ int ensure_krylov(svgpu_ctx* ctx, long n, int sD) {
   kw.n = n;
   kw.sD = sD;
   SVGPU_CUDA(ctx, kw.V.resize((size_t)n * (sD + 1)));
+  SVGPU_CUDA(ctx, kw.r64.resize(n));
   SVGPU_CUDA(ctx, kw.X.resize(n));
   SVGPU_CUDA(ctx, kw.Wc.resize(n));
   SVGPU_CUDA(ctx, kw.mask.resize(n));
@@ -137,9 +138,13 @@ struct CycleGraph {
   }
 };
 
-// One graph per context: the sD Arnoldi iterations of a restart cycle.
-std::map<const svgpu_ctx*, std::unique_ptr<CycleGraph>>& graphs() {
-  static std::map<const svgpu_ctx*, std::unique_ptr<CycleGraph>> g;
+// Graphs of one context: the sD Arnoldi iterations of a restart cycle, one per kind
+// (0: FP64, 1: mixed precision).
+struct CtxGraphs {
+  std::unique_ptr<CycleGraph> g[2];
+};
+std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
+  static std::map<const svgpu_ctx*, CtxGraphs> g;
   return g;
 }
 
@@ -171,7 +176,7 @@ void enqueue_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
 }
 
 int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
-  auto& slot = graphs()[ctx];
+  auto& slot = graphs()[ctx].g[0];
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
@@ -182,10 +187,18 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
     }
     cudaGraph_t graph;
     const long long before = ctx->launches;
-    SVGPU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_cycle(ctx, dof, Val);
-    SVGPU_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+    // captured on the context's private stream (the caller's stream may be the legacy
+    // default stream, which cannot be captured); launched on ctx->stream below
+    cudaStream_t user = ctx->stream;
+    ctx->stream = ctx->capture_stream;
+    cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      enqueue_cycle(ctx, dof, Val);
+      ce = cudaStreamEndCapture(ctx->stream, &graph);
+    }
+    ctx->stream = user;
     ctx->launches = before;
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
     cudaGraphDestroy(graph);
     g.val = Val;
@@ -267,6 +280,164 @@ int gmres_device(svgpu_ctx* ctx, int dof, const double* Val, double* R, svgpu_ls
   }
   SVGPU_CUDA(ctx, cudaMemcpyAsync(R, kw.X.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   st->dB = 10.0 * std::log(st->fNorm / dB);
+  return SVGPU_OK;
+}
+
+
+// FP32 Arnoldi cycle (mixed precision): same steps as enqueue_cycle on the FP32 basis.
+void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
+  KrylovWork& kw = ctx->kw;
+  const long n = (long)kw.n;
+  const int sD = kw.sD;
+  double* hraw = kw.givens.p + 4 * sD + 1;
+  for (int i = 0; i < sD; i++) {
+    float* ui = kw.V32.p + (long)i * n;
+    float* ui1 = kw.V32.p + (long)(i + 1) * n;
+    launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, ui, ui1, kw.flags.p);
+    const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
+                                       kw.flags.p);
+    launch_reduce_partials_flag(ctx->stream, ctas, i + 2, kw.partial.p, hraw, kw.flags.p);
+    launch_givens(ctx->stream, i, sD, kw.hess.p, kw.givens.p, kw.scal.p, kw.flags.p);
+    launch_cgs_update32(ctx->stream, n, i, kw.V32.p, n, hraw, kw.flags.p);
+    ctx->launches += 5;
+  }
+}
+
+int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
+  auto& slot = graphs()[ctx].g[1];
+  if (!slot) slot.reset(new CycleGraph());
+  CycleGraph& g = *slot;
+  const long n = (long)ctx->kw.n;
+  if (!g.exec || g.val != Val32 || g.n != n || g.sD != ctx->kw.sD) {
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
+    cudaGraph_t graph;
+    const long long before = ctx->launches;
+    // captured on the context's private stream (the caller's stream may be the legacy
+    // default stream, which cannot be captured); launched on ctx->stream below
+    cudaStream_t user = ctx->stream;
+    ctx->stream = ctx->capture_stream;
+    cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      enqueue_cycle32(ctx, Val32);
+      ce = cudaStreamEndCapture(ctx->stream, &graph);
+    }
+    ctx->stream = user;
+    ctx->launches = before;
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
+    SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    g.val = Val32;
+    g.n = n;
+    g.sD = ctx->kw.sD;
+    g.dof = 4;
+  }
+  SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+  ctx->launches += 5LL * ctx->kw.sD;
+  return SVGPU_OK;
+}
+
+// Restarted GMRES with FP32 Arnoldi cycles inside an FP64 defect-correction loop:
+// every restart starts from the residual Rs - K X recomputed with FP64 arithmetic and
+// X accumulates in FP64; the test for convergence uses that FP64 residual.  Same
+// restart structure, tolerances and statistics as gmres_v (gmres.cpp:450-629).
+int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xout, svgpu_ls_stats* st) {
+  KrylovWork& kw = ctx->kw;
+  const long n = 4L * ctx->nNo;
+  const int sD = kw.sD;
+  int rc = SVGPU_OK;
+  if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
+  st->suc = 0;
+  double nrm = device_norm(ctx, n, Rs, rc);
+  if (rc) return rc;
+  st->iNorm = nrm;
+  st->fNorm = nrm;
+  st->itr = 0;
+  const double eps = std::max(ctx->absTol, ctx->relTol * nrm);
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
+  if (st->iNorm <= ctx->absTol) {
+    st->dB = 0.0;
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(Xout, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    return SVGPU_OK;
+  }
+  if (!std::isfinite(nrm)) return set_err(ctx, SVGPU_ENAN, "non-finite residual");
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  double dB = nrm;
+  for (int l = 0; l < ctx->mItr; l++) {
+    if (l > 0) {
+      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+      launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
+      ctx->launches += 2;
+      nrm = device_norm(ctx, n, kw.r64.p, rc);
+      if (rc) return rc;
+      st->fNorm = nrm;
+      if (nrm <= eps) {
+        st->suc = 1;
+        break;
+      }
+    }
+    dB = st->fNorm;
+    st->itr++;
+    launch_norm2(ctx->stream, n, kw.r64.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
+    launch_start_vector32(ctx->stream, n, kw.r64.p, kw.scal.p + 2, kw.V32.p, kw.givens.p + 2 * sD, kw.flags.p);
+    ctx->launches += 3;
+    if ((rc = run_cycle32(ctx, Val32))) return rc;
+    launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
+    launch_xupdate32(ctx->stream, n, sD, kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
+    ctx->launches += 2;
+    int flags[4];
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st->itr += std::min(flags[1], sD - 1) + 1;
+    if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
+    if (l + 1 == ctx->mItr) {  // final true residual
+      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+      launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
+      ctx->launches += 2;
+      nrm = device_norm(ctx, n, kw.r64.p, rc);
+      if (rc) return rc;
+      st->fNorm = nrm;
+      st->suc = nrm <= eps;
+    }
+  }
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(Xout, kw.X.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  st->dB = 10.0 * std::log(st->fNorm / dB);
+  return SVGPU_OK;
+}
+
+// fsils_solve for the FP32 resident matrix: diagonal preconditioning computed in FP64
+// from the FP32 diagonal, Val32 scaled in place, R scaled and solved in the FP64
+// defect-correction loop, R <- W X.
+int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st) {
+  auto t0 = std::chrono::steady_clock::now();
+  const long n = 4L * ctx->nNo;
+  int rc = ensure_krylov(ctx, n, ctx->sD);
+  if (rc) return rc;
+  KrylovWork& kw = ctx->kw;
+  launch_fill(ctx->stream, n, 1.0, kw.mask.p);
+  ctx->launches++;
+  for (int f = 0; f < ctx->nFaces; f++) {
+    LsFace& fa = ctx->faces[f];
+    if (!fa.created || fa.bGrp != SVGPU_BC_DIR) continue;
+    if (incL && incL[f] == 0) continue;
+    launch_mask_face(ctx->stream, fa.nNo, fa.dof, 4, fa.d_glob.p, fa.d_val.p, kw.mask.p);
+    ctx->launches++;
+  }
+  launch_diag_w32(ctx->stream, ctx->nNo, ctx->diagPtr.p, Val32, kw.mask.p, kw.Wc.p);
+  launch_scale_val32(ctx->stream, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, kw.Wc.p, Val32);
+  launch_vmul(ctx->stream, n, kw.Wc.p, R);
+  ctx->launches += 3;
+  rc = gmres_mixed(ctx, Val32, R, R, st);
+  if (rc) return rc;
+  launch_vmul(ctx->stream, n, kw.Wc.p, R);
+  ctx->launches++;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  st->callD = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  st->true_rel = -1.0;
   return SVGPU_OK;
 }
 
@@ -380,6 +551,11 @@ int svgpu_create(svgpu_ctx** out, int device) {
     return SVGPU_ECUDA;
   }
   ctx->own_stream = true;
+  if (cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SVGPU_ECUDA;
+  }
   cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (ctx->errflag.resize(2) != cudaSuccess) {
     delete ctx;
@@ -396,9 +572,11 @@ int svgpu_destroy(svgpu_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   graphs().erase(ctx);
   cudaStream_t s = ctx->stream;
+  cudaStream_t cs = ctx->capture_stream;
   bool own = ctx->own_stream;
   delete ctx;
   if (own && s) cudaStreamDestroy(s);
+  if (cs) cudaStreamDestroy(cs);
   return SVGPU_OK;
 }
 
@@ -520,7 +698,9 @@ int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec
   const size_t nv = (size_t)ctx->nnz * dof * dof;
   int rc;
   if (!Ri && !Val) {
-    if (dof != 4 || !ctx->R.p || !ctx->Val.p) return set_err(ctx, SVGPU_ESTATE, "no resident system to solve");
+    if (dof != 4 || !ctx->R.p || (!ctx->Val.p && !ctx->Val32.p))
+      return set_err(ctx, SVGPU_ESTATE, "no resident system to solve");
+    if (ctx->resident_mixed) return solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL, st);
     return solve_device(ctx, dof, ctx->R.p, ctx->Val.p, prec, incL, st);
   }
   if (!Ri || !Val) return set_err(ctx, SVGPU_EINVAL, "fsils_solve: Ri and Val must both be given");
@@ -699,6 +879,7 @@ int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const 
       SVGPU_CUDA(ctx, ctx->Val32.resize(nv));
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val32.p, 0, nv * sizeof(float), ctx->stream));
     }
+    ctx->resident_mixed = precision != SVGPU_FP64;
     if ((rc = assemble_fluid_device(ctx, props, Agd, Ygd, Bfd, ctx->R.p, ctx->Val.p, ctx->Val32.p, precision)))
       return rc;
     return check_errflag(ctx);
@@ -732,8 +913,8 @@ int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* prop
   if (!is_device_ptr(Yg)) { if ((rc = to_device(ctx, ctx->Yg, Yg, n4))) return rc; Ygd = ctx->Yg.p; }
   if (!R) {
     if (!ctx->R.p) return set_err(ctx, SVGPU_ESTATE, "no resident system");
-    rc = backflow_device(ctx, faceId, props, h, Ygd, ctx->R.p, ctx->Val.p ? ctx->Val.p : nullptr,
-                         ctx->Val.p ? nullptr : ctx->Val32.p);
+    rc = backflow_device(ctx, faceId, props, h, Ygd, ctx->R.p, ctx->resident_mixed ? nullptr : ctx->Val.p,
+                         ctx->resident_mixed ? ctx->Val32.p : nullptr);
     if (rc) return rc;
     SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SVGPU_OK;
@@ -746,6 +927,29 @@ int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* prop
   if ((rc = backflow_device(ctx, faceId, props, h, Ygd, Rd, Vd, nullptr))) return rc;
   if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, n4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_get_system(svgpu_ctx* ctx, double* R, double* Val) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->R.p) return set_err(ctx, SVGPU_ESTATE, "no resident system");
+  const long n4 = 4L * ctx->nNo;
+  const size_t nv = (size_t)ctx->nnz * 16;
+  if (R) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, ctx->R.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  if (Val) {
+    if (!ctx->resident_mixed) {
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, ctx->Val.p, nv * sizeof(double), cudaMemcpyDefault, ctx->stream));
+    } else {
+      DevBuf<double> wide;
+      SVGPU_CUDA(ctx, wide.resize(nv));
+      launch_f32_to_f64(ctx->stream, (long)nv, ctx->Val32.p, wide.p);
+      ctx->launches++;
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, wide.p, nv * sizeof(double), cudaMemcpyDefault, ctx->stream));
+      SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+  }
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
 }
@@ -810,8 +1014,11 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     }
     svgpu_ls_stats st;
     std::memset(&st, 0, sizeof(st));
-    if (opts->precision != SVGPU_FP64) return set_err(ctx, SVGPU_EINVAL, "mixed-precision solve not built yet");
-    if ((rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st))) return rc;
+    if (opts->precision == SVGPU_FP64)
+      rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st);
+    else
+      rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st);
+    if (rc) return rc;
     if (stats) stats[itr - 1] = st;
     // picc (pic.cpp:74-281)
     launch_pic_correct(ctx->stream, n4, props->gam * props->dt, props->beta * props->dt * props->dt, ctx->R.p,

@@ -87,7 +87,8 @@ struct KrylovWork {
   int sD = 0;
   size_t n = 0;
   DevBuf<double> V;        // (sD+1) basis vectors of length n
-  DevBuf<double> X, Wc, mask, tmp;
+  DevBuf<float> V32;       // FP32 basis of the mixed-precision path
+  DevBuf<double> X, Wc, mask, tmp, r64;
   DevBuf<double> hess;     // (sD+1, sD) column-major, + c, s, err, y
   DevBuf<double> givens;   // c[sD], s[sD], err[sD+1], y[sD]
   DevBuf<double> partial;  // per-CTA partial dot products
@@ -101,6 +102,7 @@ struct svgpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t capture_stream = nullptr;  // private stream the restart-cycle graphs are captured on
   std::string err;
   long long launches = 0;
   int sm_count = 0;
@@ -126,6 +128,7 @@ struct svgpu_ctx {
   // resident system and Newton state
   svgpu::DevBuf<double> R, Val;
   svgpu::DevBuf<float> Val32;
+  bool resident_mixed = false;  // the resident tangent is Val32
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
@@ -182,6 +185,21 @@ void launch_xupdate(cudaStream_t s, long n, int sD, const double* V, long ldv, c
                     const int* flags, double* X);
 void launch_norm2(cudaStream_t s, long n, const double* a, double* partial, double* out, int sm_count);
 void launch_axpby(cudaStream_t s, long n, double a, const double* x, double b, double* y);
+// mixed precision (FP32 matrix and basis, FP64 residual and Hessenberg)
+void launch_diag_w32(cudaStream_t s, int nNo, const int* diagPtr, const float* Val, const double* mask, double* W);
+void launch_scale_val32(cudaStream_t s, long nnz, const int* blkRow, const int* colPtr, const double* W, float* Val);
+void launch_spmv4_f32(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
+                      const float* x, float* y, const int* flags);
+void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
+                          const double* x, double* y);
+int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
+                      int sm_count, const int* flags);
+void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, const double* hcol, const int* flags);
+void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, const double* g, const int* flags,
+                      double* X);
+void launch_sub(cudaStream_t s, long n, const double* R, const double* y, double* r);
+void launch_start_vector32(cudaStream_t s, long n, const double* r, const double* nrm2, float* u0, double* err0,
+                           int* flags);
 
 // ---- k_fluid.cu ----------------------------------------------------------------
 struct FluidConsts {
@@ -203,5 +221,6 @@ void launch_pic_initiate(cudaStream_t s, long n4, double am, double af, const do
 void launch_pic_correct(cudaStream_t s, long n4, double c0, double c1, const double* R, double* An,
                         double* Yn, double* Dn);
 void launch_f64_to_f32(cudaStream_t s, long n, const double* a, float* b);
+void launch_f32_to_f64(cudaStream_t s, long n, const float* a, double* b);
 
 }  // namespace svgpu

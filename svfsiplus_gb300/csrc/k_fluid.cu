@@ -80,8 +80,10 @@ __device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const 
   }
 }
 
-// T: arithmetic type of the element integrals; TV: storage type of Val.
-template <typename T, typename TV>
+// T: arithmetic type of the element integrals; TV: storage type of Val.  WR / WK
+// select writing the residual rows / the tangent blocks (the mixed-precision path
+// runs the residual in FP64 and the tangent in FP32 as two launches).
+template <typename T, typename TV, bool WR, bool WK>
 __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, int ne,
                                                        const int* __restrict__ ien,
                                                        const uint8_t* __restrict__ boff,
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
       const T ma = mcoef * N[a];
 #pragma unroll
       for (int b = 0; b < 4; b++)
-        S[a][b] += ma * N[b] + al_a * (rho * amd * N[b] - T1b[b]) + ga * (uNx[b] + upNx[b]) + ea * upNx[b];
+        if (WK) S[a][b] += ma * N[b] + al_a * (rho * amd * N[b] - T1b[b]) + ga * (uNx[b] + upNx[b]) + ea * upNx[b];
       Qv[a] += al_a;
       Gv[a] += tauM * (T1b[a] - rho * amd * N[a]);
     }
@@ -279,7 +281,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 
   // residual rows (lR, fluid.cpp:2038-2040, 1658-1660)
 #pragma unroll
-  for (int a = 0; a < 4; a++) {
+  for (int a = 0; a < 4 && WR; a++) {
     double* Ra = R + 4L * nd[a];
     double r0 = (double)(w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]));
     double r1 = (double)(w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]));
@@ -292,6 +294,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
     *reinterpret_cast<double2*>(Ra + 2) = v23;
   }
 
+  if (!WK) return;
   // tangent blocks
   const T c4mu = wl * (T)4 * mu, cTC = wl * sTauC, cTM = wl * sTauM, cSN = wl * q.SN;
 #pragma unroll
@@ -423,6 +426,11 @@ __global__ void pic_correct_kernel(long n4, double c0, double c1, const double* 
   }
 }
 
+__global__ void f32_to_f64_kernel(long n, const float* __restrict__ a, double* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
 __global__ void f64_to_f32_kernel(long n, const double* __restrict__ a, float* __restrict__ b) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
@@ -437,12 +445,16 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
   if (ne <= 0) return;
   const int block = 128;
   const int grid = (ne + block - 1) / block;
-  if (precision == SVGPU_FP64)
-    fluid_p1_kernel<double, double><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr,
-                                                            R, Val64, errflag);
-  else
-    fluid_p1_kernel<float, float><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr,
-                                                          R, Val32, errflag);
+  if (precision == SVGPU_FP64) {
+    fluid_p1_kernel<double, double, true, true><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg,
+                                                                        Bf, rowPtr, R, Val64, errflag);
+  } else {
+    // residual rows in FP64, tangent blocks in FP32
+    fluid_p1_kernel<double, double, true, false><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg,
+                                                                         Bf, rowPtr, R, nullptr, errflag);
+    fluid_p1_kernel<float, float, false, true><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf,
+                                                                       rowPtr, R, Val32, errflag);
+  }
 }
 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
@@ -475,6 +487,10 @@ void launch_pic_initiate(cudaStream_t s, long n4, double am, double af, const do
 void launch_pic_correct(cudaStream_t s, long n4, double c0, double c1, const double* R, double* An,
                         double* Yn, double* Dn) {
   pic_correct_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, c0, c1, R, An, Yn, Dn);
+}
+
+void launch_f32_to_f64(cudaStream_t s, long n, const float* a, double* b) {
+  f32_to_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, b);
 }
 
 void launch_f64_to_f32(cudaStream_t s, long n, const double* a, float* b) {

@@ -410,4 +410,214 @@ void launch_axpby(cudaStream_t s, long n, double a, const double* x, double b, d
   axpby_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, x, b, y);
 }
 
+namespace {
+// ---------------------------------------------------------------- mixed precision
+// FP32 matrix (Val32) and FP32 Krylov basis inside an FP64 defect-correction loop:
+// every restart starts from the residual recomputed in FP64.
+
+__global__ void diag_w32_kernel(int nNo, const int* __restrict__ diagPtr, const float* __restrict__ Val,
+                                const double* __restrict__ mask, double* __restrict__ W) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4L * nNo) return;
+  const long a = t / 4;
+  const int i = (int)(t % 4);
+  double w = (double)Val[16L * diagPtr[a] + i * 4 + i];
+  if (w == 0.0) w = 1.0;
+  w = 1.0 / sqrt(fabs(w));
+  if (mask) w = w * mask[t];
+  W[t] = w;
+}
+
+__global__ void scale_val32_kernel(long nnz, const int* __restrict__ blkRow, const int* __restrict__ colPtr,
+                                   const double* __restrict__ W, float* __restrict__ Val) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnz * 16) return;
+  const long k = t >> 4;
+  const int r = (int)((t >> 2) & 3), c = (int)(t & 3);
+  Val[t] = (float)(((double)Val[t] * W[4L * blkRow[k] + r]) * W[4L * colPtr[k] + c]);
+}
+
+// y = K x, FP32 matrix and vectors, FP32 accumulation; 4 threads per block row, one
+// 128-bit load of the block row and one of x per block.
+__global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                        const int* __restrict__ colPtr,
+                                                        const float* __restrict__ Val,
+                                                        const float* __restrict__ x, float* __restrict__ y,
+                                                        const int* flags) {
+  if (stopped(flags)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 2;
+  const int r = (int)(t & 3);
+  if (row >= nNo) return;
+  const int s = rowPtr[row], e = rowPtr[row + 1];
+  float acc = 0.f;
+  for (int k = s; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
+    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
+    acc = fmaf(v.x, xv.x, acc);
+    acc = fmaf(v.y, xv.y, acc);
+    acc = fmaf(v.z, xv.z, acc);
+    acc = fmaf(v.w, xv.w, acc);
+  }
+  y[4 * row + r] = acc;
+}
+
+// y = K x with the FP32 matrix, FP64 vectors and FP64 accumulation (true residual).
+__global__ void __launch_bounds__(256) spmv4_f32_f64_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                            const int* __restrict__ colPtr,
+                                                            const float* __restrict__ Val,
+                                                            const double* __restrict__ x, double* __restrict__ y) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 2;
+  const int r = (int)(t & 3);
+  if (row >= nNo) return;
+  const int s = rowPtr[row], e = rowPtr[row + 1];
+  double acc = 0.0;
+  for (int k = s; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
+    const double2 x0 = *reinterpret_cast<const double2*>(x + 4L * col);
+    const double2 x1 = *reinterpret_cast<const double2*>(x + 4L * col + 2);
+    acc += (double)v.x * x0.x + (double)v.y * x0.y + (double)v.z * x1.x + (double)v.w * x1.y;
+  }
+  y[4 * row + r] = acc;
+}
+
+// Partial <V_j, w> over FP32 vectors: FP32 products summed per thread, FP64 across
+// threads and CTAs.
+template <int JB>
+__global__ void __launch_bounds__(256) multidot32_kernel(long n, int m, const float* __restrict__ V, long ldv,
+                                                         const float* __restrict__ w, double* __restrict__ partial,
+                                                         const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ double red[JB][8];
+  const long chunk = (n + gridDim.x - 1) / gridDim.x;
+  const long beg = (long)blockIdx.x * chunk;
+  const long end = beg + chunk < n ? beg + chunk : n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < m; j0 += JB) {
+    float acc[JB];
+#pragma unroll
+    for (int q = 0; q < JB; q++) acc[q] = 0.f;
+    for (long k = beg + threadIdx.x; k < end; k += blockDim.x) {
+      const float wk = w[k];
+#pragma unroll
+      for (int q = 0; q < JB; q++)
+        if (j0 + q < m) acc[q] = fmaf(__ldcs(V + (long)(j0 + q) * ldv + k), wk, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < JB; q++) {
+      double v = (double)acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < JB && j0 + threadIdx.x < m) {
+      double v = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += red[threadIdx.x][q];
+      partial[(long)blockIdx.x * m + j0 + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) cgs_update32_kernel(long n, int i, float* __restrict__ V, long ldv,
+                                                           const double* __restrict__ hcol, const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ float hs[256];
+  __shared__ float rinv;
+  for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (float)hcol[j];
+  if (threadIdx.x == 0) rinv = (float)(1.0 / hcol[i + 1]);
+  __syncthreads();
+  float* w = V + (long)(i + 1) * ldv;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    float acc = w[k];
+    for (int j = 0; j <= i; j++) acc = fmaf(-hs[j], __ldcs(V + (long)j * ldv + k), acc);
+    w[k] = rinv * acc;
+  }
+}
+
+// X (FP64) += sum_j y_j u_j over the FP32 basis (the sum in FP32, added in FP64)
+__global__ void __launch_bounds__(256) xupdate32_kernel(long n, int sD, const float* __restrict__ V, long ldv,
+                                                        const double* __restrict__ g, const int* flags,
+                                                        double* __restrict__ X) {
+  __shared__ float ys[256];
+  int last = flags[1];
+  if (last >= sD) last = sD - 1;
+  const double* y = g + 3 * sD + 1;
+  for (int j = threadIdx.x; j <= last; j += blockDim.x) ys[j] = (float)y[j];
+  __syncthreads();
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int j = 0; j <= last; j++) acc = fmaf(ys[j], __ldcs(V + (long)j * ldv + k), acc);
+    X[k] += (double)acc;
+  }
+}
+
+// r = R - y (FP64), u0 = float(r / ||r||) once the norm is known: two kernels.
+__global__ void sub_kernel(long n, const double* __restrict__ R, const double* __restrict__ y, double* __restrict__ r) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    r[i] = R[i] - y[i];
+}
+
+__global__ void start_vector32_kernel(long n, const double* __restrict__ r, const double* __restrict__ nrm2,
+                                      float* __restrict__ u0, double* __restrict__ err0, int* flags) {
+  const double nrm = sqrt(*nrm2);
+  const double inv = 1.0 / nrm;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    u0[i] = (float)(r[i] * inv);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *err0 = nrm;
+    flags[0] = 0;
+    flags[1] = 0;
+    flags[2] = (nrm == 0.0 || !isfinite(nrm)) ? 1 : 0;
+  }
+}
+
+}  // namespace
+
+void launch_diag_w32(cudaStream_t s, int nNo, const int* diagPtr, const float* Val, const double* mask, double* W) {
+  diag_w32_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, s>>>(nNo, diagPtr, Val, mask, W);
+}
+
+void launch_scale_val32(cudaStream_t s, long nnz, const int* blkRow, const int* colPtr, const double* W, float* Val) {
+  scale_val32_kernel<<<(unsigned)((nnz * 16 + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, W, Val);
+}
+
+void launch_spmv4_f32(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
+                      const float* x, float* y, const int* flags) {
+  spmv4_f32_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y, flags);
+}
+
+void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
+                          const double* x, double* y) {
+  spmv4_f32_f64_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y);
+}
+
+int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
+                      int sm_count, const int* flags) {
+  const int ctas = multidot_ctas(n, sm_count);
+  multidot32_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  return ctas;
+}
+
+void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, const double* hcol, const int* flags) {
+  cgs_update32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, i, V, ldv, hcol, flags);
+}
+
+void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, const double* g, const int* flags,
+                      double* X) {
+  xupdate32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, sD, V, ldv, g, flags, X);
+}
+
+void launch_sub(cudaStream_t s, long n, const double* R, const double* y, double* r) {
+  sub_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, R, y, r);
+}
+
+void launch_start_vector32(cudaStream_t s, long n, const double* r, const double* nrm2, float* u0, double* err0,
+                           int* flags) {
+  start_vector32_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, r, nrm2, u0, err0, flags);
+}
+
 }  // namespace svgpu

@@ -73,6 +73,23 @@ def test_assembly_is_deterministic(golden):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_assembly_mixed_precision(golden):
+    """SVGPU_MIXED: FP64 residual rows (within 1e-12 of the reference) and an FP32
+    tangent (within 2e-6 relative)."""
+    g = golden("small")
+    m = named_pipe("small")
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    props = api.fluid_props()
+    Ag, Yg = np.ascontiguousarray(g["Ag"]), np.ascontiguousarray(g["Yg"])
+    ctx.construct_fluid(props, Ag, Yg, precision=api.SVGPU_MIXED)
+    ctx.b_assem_neu_bc(api.FACE_OUTLET, props, 0.0, Yg)
+    R = np.zeros((m.nNo, 4))
+    Val = np.zeros((g["colPtr"].size, 16))
+    ctx.get_system(R, Val)
+    assert rel(R, g["R_asm"]) <= 1e-12
+    assert rel(Val, g["Val_asm"]) <= 2e-6
+
+
 @pytest.mark.parametrize("name", ["tiny", "small"])
 def test_fsils_solve_matches_reference(golden, name):
     g = golden(name)
@@ -134,6 +151,25 @@ def test_time_steps_match_reference(golden, name):
         assert rel(s.Yn[:, 3], ref[:, 3]) <= 1e-6
 
 
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_time_steps_mixed_precision(golden, name):
+    """FP32 tangent and Krylov basis, FP64 residual and defect correction: the fields
+    stay within 1e-6 of the reference's FP64 solution."""
+    g = golden(name)
+    m = named_pipe(name)
+    ps = eval(str(g["params"]))
+    s = api.PipeFluidSolver(m, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
+                            absTol=ps["ls_abs_tol"], newton_min=ps["newton_min"], newton_max=ps["newton_max"],
+                            newton_tol=ps["newton_tol"], rowPtr=g["rowPtr"], colPtr=g["colPtr"],
+                            precision=api.SVGPU_MIXED)
+    for step in range(1, ps["n_steps"] + 1):
+        st = s.step(u_mean=ps["u_mean"], u_amp=ps["u_amp"], freq=ps["u_freq"])
+        assert all(x["suc"] for x in st)
+        ref = g[f"Yn_{step}"]
+        assert rel(s.Yn[:, :3], ref[:, :3]) <= 1e-6
+        assert rel(s.Yn[:, 3], ref[:, 3]) <= 1e-6
+
+
 def test_pipe50k_ten_steps_match_reference(golden):
     """The CPU-runnable 50k-tet pipe, 10 gen-alpha steps, GMRES(50) + diagonal
     preconditioner to 1e-8: velocity and pressure within 1e-6 of the reference."""
@@ -171,3 +207,17 @@ def test_zero_jacobian_reported_not_faulted():
         ctx.construct_fluid(props, z, z, R=np.zeros((m.nNo, 4)), Val=np.zeros((colPtr.size, 16)))
     ctx.mesh_create(m.x, m.ien)
     ctx.construct_fluid(props, z, z, R=np.zeros((m.nNo, 4)), Val=np.zeros((colPtr.size, 16)))
+
+
+def test_solve_on_caller_default_stream(golden):
+    """The restart-cycle graphs are captured on a private stream, so a caller may hand
+    the library the legacy default stream."""
+    g = golden("tiny")
+    m = named_pipe("tiny")
+    ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
+    assert api.lib().svgpu_set_stream(ctx._h, None) == 0
+    ctx.fsils_ls_create(api.LS_TYPE_GMRES, 1e-8, 1e-17, 100, 50)
+    Ri = np.array(g["R_asm"], copy=True)
+    Val = np.array(g["Val_asm"], copy=True)
+    st = ctx.fsils_solve(4, Ri, Val, api.PREC_FSILS, incL=np.ones(2, np.int32), res=np.zeros(2))
+    assert st.suc == 1 and rel(Ri, g["dX"]) <= 1e-5
