@@ -176,6 +176,52 @@ class Context:
         self._check(lib().svgpu_neu_bc_fluid(self._h, int(face_id), C.byref(props), C.c_double(h), _ptr(Yg),
                                              _ptr(R), _ptr(Val)), "b_assem_neu_bc")
 
+    # ---- learned preconditioner
+    def gnn_create(self, node_features, seed=1):
+        f = np.ascontiguousarray(node_features, dtype=np.float32)
+        self._check(lib().svgpu_gnn_create(self._h, _ptr(f), C.c_ulonglong(seed)), "gnn_create")
+
+    def gnn_params(self):
+        n = lib().svgpu_gnn_param_count()
+        p = np.zeros(n, dtype=np.float32)
+        self._check(lib().svgpu_gnn_get_params(self._h, _ptr(p), n), "gnn_get_params")
+        return p
+
+    def gnn_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(lib().svgpu_gnn_set_params(self._h, _ptr(p), int(p.size)), "gnn_set_params")
+
+    def gnn_apply(self, r, z):
+        self._check(lib().svgpu_gnn_apply(self._h, _ptr(r), _ptr(z)), "gnn_apply")
+
+    def gnn_loss_grad(self, r, x):
+        n = lib().svgpu_gnn_param_count()
+        g = np.zeros(n, dtype=np.float32)
+        loss = C.c_double()
+        self._check(lib().svgpu_gnn_loss_grad(self._h, _ptr(np.ascontiguousarray(r)), _ptr(np.ascontiguousarray(x)),
+                                              C.byref(loss), _ptr(g)), "gnn_loss_grad")
+        return loss.value, g
+
+    def gnn_add_pair(self, r, x):
+        self._check(lib().svgpu_gnn_add_pair(self._h, _ptr(np.ascontiguousarray(r)), _ptr(np.ascontiguousarray(x))),
+                    "gnn_add_pair")
+
+    def gnn_collect(self, on=True):
+        self._check(lib().svgpu_gnn_collect(self._h, int(bool(on))), "gnn_collect")
+
+    def gnn_train(self, iters, lr=1e-3):
+        loss = C.c_double()
+        self._check(lib().svgpu_gnn_train(self._h, int(iters), C.c_float(lr), C.byref(loss)), "gnn_train")
+        return loss.value
+
+    def set_learned(self, on=True):
+        self._check(lib().svgpu_set_learned(self._h, int(bool(on))), "set_learned")
+
+    @property
+    def learned_rejects(self):
+        lib().svgpu_learned_rejects.restype = C.c_longlong
+        return int(lib().svgpu_learned_rejects(self._h))
+
     def set_dirichlet(self, nodes):
         nodes = np.ascontiguousarray(nodes, dtype=np.int32)
         self._check(lib().svgpu_set_dirichlet(self._h, int(nodes.size), _ptr(nodes)), "set_dirichlet")
@@ -232,6 +278,27 @@ def inflow(prof, time, u_mean, u_amp, freq):
     return dirY, dirA
 
 
+def pipe_node_features(mesh):
+    """Static node features of the learned preconditioner: coordinates scaled to
+    [-1, 1] (x/R, y/R, 2z/L - 1) and the normalised distance to the wall 1 - r/r_wall."""
+    x = mesh.x
+    f = np.zeros((mesh.nNo, 4), dtype=np.float32)
+    f[:, 0] = x[:, 0] / mesh.radius
+    f[:, 1] = x[:, 1] / mesh.radius
+    f[:, 2] = 2.0 * x[:, 2] / mesh.length - 1.0
+    r = np.hypot(x[:, 0], x[:, 1])
+    wall = mesh.faces["wall"].gN
+    # wall radius per axial layer and angle is not stored: use the largest radius of the
+    # node's layer as r_wall (exact for the straight pipe)
+    zkey = np.round(x[:, 2] * 1e6).astype(np.int64)
+    rmax = {}
+    for k, rr in zip(zkey[wall], r[wall]):
+        rmax[k] = max(rmax.get(k, 0.0), rr)
+    rw = np.array([rmax.get(k, mesh.radius) for k in zkey])
+    f[:, 3] = np.clip(1.0 - r / rw, 0.0, 1.0)
+    return f
+
+
 class PipeFluidSolver:
     """The fluid pipe case on the GPU: CSR set-up (lhsa + fsils_lhs_create), Dirichlet
     faces (fsils_bc_create, baf_ini.cpp:719-744), the outlet face, GMRES settings, and
@@ -260,6 +327,12 @@ class PipeFluidSolver:
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.norms = [0.0, 0.0]
         self.time = 0.0
+
+    def enable_learning(self, seed=1):
+        """Create the learned preconditioner and start collecting (residual, increment)
+        pairs from the plain solves."""
+        self.ctx.gnn_create(pipe_node_features(self.mesh), seed)
+        self.ctx.gnn_collect(True)
 
     def step(self, u_mean=10.0, u_amp=0.0, freq=1.0):
         self.time += self.props.dt

@@ -50,24 +50,6 @@ using namespace svgpu;
 
 namespace {
 
-// Copies n elements from a host-or-device pointer into a device buffer.
-template <typename T>
-int to_device(svgpu_ctx* ctx, DevBuf<T>& dst, const T* src, size_t n) {
-  SVGPU_CUDA(ctx, dst.resize(n));
-  if (n == 0) return SVGPU_OK;
-  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.p, src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
-  return SVGPU_OK;
-}
-
-template <typename T>
-int to_host(svgpu_ctx* ctx, std::vector<T>& dst, const T* src, size_t n) {
-  dst.resize(n);
-  if (n == 0) return SVGPU_OK;
-  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
-  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return SVGPU_OK;
-}
-
 // Greedy colouring of elements (eNoN nodes each) so that no two elements of a colour
 // share a node; returns the permutation (colour-major, original order inside a
 // colour) and the colour offsets.
@@ -116,6 +98,8 @@ int ensure_krylov(svgpu_ctx* ctx, long n, int sD) {
   kw.sD = sD;
   SVGPU_CUDA(ctx, kw.V.resize((size_t)n * (sD + 1)));
   SVGPU_CUDA(ctx, kw.r64.resize(n));
+  SVGPU_CUDA(ctx, kw.rbak.resize(n));
+  SVGPU_CUDA(ctx, kw.rsave.resize(n));
   SVGPU_CUDA(ctx, kw.X.resize(n));
   SVGPU_CUDA(ctx, kw.Wc.resize(n));
   SVGPU_CUDA(ctx, kw.mask.resize(n));
@@ -141,7 +125,7 @@ struct CycleGraph {
 // Graphs of one context: the sD Arnoldi iterations of a restart cycle, one per kind
 // (0: FP64, 1: mixed precision).
 struct CtxGraphs {
-  std::unique_ptr<CycleGraph> g[2];
+  std::unique_ptr<CycleGraph> g[3];  // 0: FP64, 1: mixed, 2: mixed + learned (flexible)
 };
 std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
   static std::map<const svgpu_ctx*, CtxGraphs> g;
@@ -303,6 +287,67 @@ void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
   }
 }
 
+// Flexible cycle with the learned right preconditioner: z_i = M(u_i) (the network on
+// the unit-norm basis vector, scale 1/sqrt(n)), u_{i+1} = K z_i, then the same
+// Gram-Schmidt and Givens steps; the solution is updated from the z_i (FGMRES).
+void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
+  KrylovWork& kw = ctx->kw;
+  GnnState& g = *ctx->gnn;
+  const long n = (long)kw.n;
+  const int sD = kw.sD;
+  double* hraw = kw.givens.p + 4 * sD + 1;
+  for (int i = 0; i < sD; i++) {
+    float* ui = kw.V32.p + (long)i * n;
+    float* ui1 = kw.V32.p + (long)(i + 1) * n;
+    float* zi = g.zbasis.p + (long)i * n;
+    gnn_apply_device(ctx, ui, nullptr, g.scal.p + 4, zi, nullptr, kw.flags.p);
+    launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
+    const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
+                                       kw.flags.p);
+    launch_reduce_partials_flag(ctx->stream, ctas, i + 2, kw.partial.p, hraw, kw.flags.p);
+    launch_givens(ctx->stream, i, sD, kw.hess.p, kw.givens.p, kw.scal.p, kw.flags.p);
+    launch_cgs_update32(ctx->stream, n, i, kw.V32.p, n, hraw, kw.flags.p);
+    ctx->launches += 5;
+  }
+}
+
+int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
+  auto& slot = graphs()[ctx].g[kind];
+  if (!slot) slot.reset(new CycleGraph());
+  CycleGraph& g = *slot;
+  const long n = (long)ctx->kw.n;
+  if (!g.exec || g.val != Val32 || g.n != n || g.sD != ctx->kw.sD) {
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
+    cudaGraph_t graph;
+    const long long before = ctx->launches;
+    cudaStream_t user = ctx->stream;
+    ctx->stream = ctx->capture_stream;
+    cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      if (kind == 2)
+        enqueue_cycle_flex(ctx, Val32);
+      else
+        enqueue_cycle32(ctx, Val32);
+      ce = cudaStreamEndCapture(ctx->stream, &graph);
+    }
+    ctx->stream = user;
+    ctx->launches = before;
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
+    SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    g.val = Val32;
+    g.n = n;
+    g.sD = ctx->kw.sD;
+    g.dof = 4;
+  }
+  SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+  ctx->launches += (kind == 2 ? 10LL : 5LL) * ctx->kw.sD;
+  return SVGPU_OK;
+}
+
 int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
   auto& slot = graphs()[ctx].g[1];
   if (!slot) slot.reset(new CycleGraph());
@@ -348,6 +393,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   const long n = 4L * ctx->nNo;
   const int sD = kw.sD;
   int rc = SVGPU_OK;
+  bool learned = ctx->learned_mode != 0 && ctx->gnn != nullptr;
   if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
   st->suc = 0;
   double nrm = device_norm(ctx, n, Rs, rc);
@@ -366,7 +412,32 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  if (learned) {
+    GnnState& g = *ctx->gnn;
+    if (!g.zbasis.p || g.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, g.zbasis.resize((size_t)n * sD));
+    const double sv = 1.0 / std::sqrt((double)n);  // scale of a unit-norm basis vector
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(g.scal.p + 4, &sv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    // learned initial guess X0 = M(Rs), kept only if it lowers the FP64 residual
+    launch_norm2(ctx->stream, n, Rs, g.nrmp.p, g.scal.p + 1, ctx->sm_count);
+    gnn_scale(ctx->stream, g.scal.p + 1, n, g.scal.p);
+    ctx->launches += 3;
+    if ((rc = gnn_apply_device(ctx, nullptr, Rs, g.scal.p, nullptr, kw.X.p, nullptr))) return rc;
+    launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+    launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
+    ctx->launches += 2;
+    const double n0 = device_norm(ctx, n, kw.r64.p, rc);
+    if (rc) return rc;
+    if (!(n0 < nrm)) {
+      ctx->learned_rejects++;
+      SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+      nrm = n0;
+      st->fNorm = nrm;
+    }
+  }
   double dB = nrm;
+  double before = nrm;  // FP64 residual norm when the current cycle started
   for (int l = 0; l < ctx->mItr; l++) {
     if (l > 0) {
       launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
@@ -374,6 +445,16 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
       ctx->launches += 2;
       nrm = device_norm(ctx, n, kw.r64.p, rc);
       if (rc) return rc;
+      if (learned && !(nrm < before)) {
+        // the learned cycle did not lower the true FP64 residual: undo it and finish
+        // the solve with plain GMRES cycles
+        ctx->learned_rejects++;
+        learned = false;
+        SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.X.p, kw.mask.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, kw.rbak.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                        ctx->stream));
+        nrm = before;
+      }
       st->fNorm = nrm;
       if (nrm <= eps) {
         st->suc = 1;
@@ -381,13 +462,18 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
       }
     }
     dB = st->fNorm;
+    before = nrm;
     st->itr++;
+    if (learned) {  // keep X and r of the cycle start for a possible rejection
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.mask.p, kw.X.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rbak.p, kw.r64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     launch_norm2(ctx->stream, n, kw.r64.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
     launch_start_vector32(ctx->stream, n, kw.r64.p, kw.scal.p + 2, kw.V32.p, kw.givens.p + 2 * sD, kw.flags.p);
     ctx->launches += 3;
-    if ((rc = run_cycle32(ctx, Val32))) return rc;
+    if ((rc = run_cycle_kind(ctx, Val32, learned ? 2 : 1))) return rc;
     launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
-    launch_xupdate32(ctx->stream, n, sD, kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
+    launch_xupdate32(ctx->stream, n, sD, learned ? ctx->gnn->zbasis.p : kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
     ctx->launches += 2;
     int flags[4];
     SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
@@ -431,8 +517,13 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   launch_scale_val32(ctx->stream, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, kw.Wc.p, Val32);
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches += 3;
+  const bool collect = ctx->gnn && ctx->gnn->collect;
+  if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   rc = gmres_mixed(ctx, Val32, R, R, st);
   if (rc) return rc;
+  if (collect && st->suc) {  // (preconditioned residual, preconditioned increment) pair
+    if ((rc = gnn_store_pair(ctx, kw.rsave.p, R))) return rc;
+  }
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches++;
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -2,6 +2,7 @@
 // device buffers, launch helpers and the kernel entry points of each .cu file.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -88,12 +89,33 @@ struct KrylovWork {
   size_t n = 0;
   DevBuf<double> V;        // (sD+1) basis vectors of length n
   DevBuf<float> V32;       // FP32 basis of the mixed-precision path
-  DevBuf<double> X, Wc, mask, tmp, r64;
+  DevBuf<double> X, Wc, mask, tmp, r64, rbak, rsave;
   DevBuf<double> hess;     // (sD+1, sD) column-major, + c, s, err, y
   DevBuf<double> givens;   // c[sD], s[sD], err[sD+1], y[sD]
   DevBuf<double> partial;  // per-CTA partial dot products
   DevBuf<double> scal;     // small scalars: eps, norms
   DevBuf<int> flags;       // [0] converged, [1] last_i, [2] breakdown
+};
+
+// Learned preconditioner state (k_gnn.cu kernels).
+struct GnnState {
+  int nNo = 0;
+  int nparam = 0;
+  DevBuf<float> p32, grad, adam_m, adam_v;  // FP32 master weights, gradient, Adam moments
+  DevBuf<uint16_t> pbf;                     // BF16 working copy (bit patterns)
+  DevBuf<float> stat;                       // (4, nNo) static node features
+  DevBuf<uint16_t> h[4], msave[4];          // BF16 activations (nNo x 64); msave[1..3]
+  DevBuf<uint64_t> mask;                    // relu masks, 4 x nNo
+  DevBuf<float> raw, in32, tgt32;           // decoder output, FP32 input and target
+  DevBuf<float> dA, dB, dC;                 // FP32 gradients (nNo x 64)
+  DevBuf<float> part;                       // weight-gradient partial sums
+  DevBuf<double> lossbuf, scal, nrmp;       // loss / scale scalars, norm partials
+  DevBuf<float> zbasis;                     // flexible-GMRES directions Z (sD x 4 nNo)
+  std::vector<DevBuf<float>> pair_r, pair_x;  // training pairs (scaled space)
+  int npairs = 0, next_pair = 0, max_pairs = 64;
+  int adam_step = 0;
+  bool collect = false;                     // store (residual, increment) pairs from plain solves
+  double last_loss = 0.0;
 };
 
 }  // namespace svgpu
@@ -132,6 +154,9 @@ struct svgpu_ctx {
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
+  std::unique_ptr<svgpu::GnnState> gnn;
+  int learned_mode = 0;  // 0: plain GMRES, 1: learned FGMRES (with rejection)
+  long long learned_rejects = 0;
   // host staging
   svgpu::DevBuf<double> stage1, stage2;
 };
@@ -148,6 +173,30 @@ bool is_device_ptr(const void* p);
     cudaError_t e_ = (call);                                 \
     if (e_ != cudaSuccess) return svgpu::cuda_fail(ctx, e_, #call); \
   } while (0)
+
+// Copies n elements from a host-or-device pointer into a device buffer.
+template <typename T>
+int to_device(svgpu_ctx* ctx, DevBuf<T>& dst, const T* src, size_t n) {
+  SVGPU_CUDA(ctx, dst.resize(n));
+  if (n == 0) return SVGPU_OK;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.p, src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
+  return SVGPU_OK;
+}
+
+template <typename T>
+int to_host(svgpu_ctx* ctx, std::vector<T>& dst, const T* src, size_t n) {
+  dst.resize(n);
+  if (n == 0) return SVGPU_OK;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+bool misaligned_device(const void* p);
+// GNN helpers used by the solver (gnn.cpp)
+int gnn_apply_device(svgpu_ctx* ctx, const float* r32, const double* r64, const double* scale, float* out32,
+                     double* out64, const int* flags);
+int gnn_store_pair(svgpu_ctx* ctx, const double* r, const double* x);
 
 inline int grid_for(long n, int block, int cap = 152 * 16) {
   long g = (n + block - 1) / block;
@@ -222,5 +271,21 @@ void launch_pic_correct(cudaStream_t s, long n4, double c0, double c1, const dou
                         double* Yn, double* Dn);
 void launch_f64_to_f32(cudaStream_t s, long n, const double* a, float* b);
 void launch_f32_to_f64(cudaStream_t s, long n, const float* a, double* b);
+
+// ---- k_gnn.cu ------------------------------------------------------------------
+int gnn_param_count();
+size_t gnn_part_floats(int sm_count);
+void gnn_forward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
+                 const double* r64, const float* stat, const double* sc, const __nv_bfloat16* P,
+                 __nv_bfloat16* const* h, __nv_bfloat16* const* msave, uint64_t* mask, float* out32,
+                 double* out64, float* raw, int sm_count, const int* flags);
+void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
+                  const float* stat, const double* sc, const __nv_bfloat16* P, __nv_bfloat16* const* h,
+                  __nv_bfloat16* const* msave, const uint64_t* mask, const float* raw, const float* tgt,
+                  float* dA, float* dB, float* dC, float* part, double* lossbuf, float* grad, int sm_count);
+void gnn_adam(cudaStream_t st, float lr, int step, const float* g, float* p, float* m, float* v, __nv_bfloat16* pb);
+void gnn_to_bf16(cudaStream_t st, const float* p, __nv_bfloat16* pb);
+void gnn_scale(cudaStream_t st, const double* nrm2, long n, double* sc);
+void gnn_f64_to_f32(cudaStream_t st, long n, const double* a, float* b);
 
 }  // namespace svgpu

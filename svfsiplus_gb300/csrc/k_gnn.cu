@@ -1,0 +1,517 @@
+// Learned preconditioner: a 3-layer message-passing network on the mesh graph (the
+// CSR pattern of the linear system), trained online on (residual, increment) pairs
+// the solver produces, applied as the right preconditioner of flexible GMRES.
+// The reference has no counterpart; this is new work on top of its FSILS solve.
+//
+// Network (hidden width 64, weights stored in BF16, accumulation in FP32):
+//   input  x_i = [r_i / s (4), static_i (4)]   s = ||r|| / sqrt(n), static = scaled
+//                                               coordinates and wall distance
+//   h0_i   = relu(W0^T x_i + b0)                8 -> 64
+//   layer l = 1..3:
+//     m_i  = mean_{j in N(i)} h_j               (N(i): the CSR row of node i, self included)
+//     z_i  = Wl^T [h_i; m_i] + bl               128 -> 64
+//     h_i <- h_i + relu(z_i)
+//   out_i  = Wd^T h3_i + bd                     64 -> 4,  M(r)_i = s * out_i
+// Activations h are stored in BF16 (the gathers read 128 bytes per neighbour);
+// gradients and weight-gradient partial sums are FP32.
+//
+// Parameter vector (FP32 master copy, BF16 working copy), offsets in floats:
+//   W0 [8][64] | b0 [64] | W1 [128][64] | b1 [64] | W2 | b2 | W3 | b3 | Wd [64][4] | bd [4]
+#include <cuda_bf16.h>
+
+#include "internal.h"
+
+namespace svgpu {
+
+namespace {
+
+constexpr int H = 64;
+constexpr int NIN = 8;
+constexpr int OFF_W0 = 0, OFF_B0 = NIN * H;
+constexpr int LAYER = 2 * H * H + H;
+__host__ __device__ constexpr int off_w(int l) { return OFF_B0 + H + (l - 1) * LAYER; }
+__host__ __device__ constexpr int off_b(int l) { return off_w(l) + 2 * H * H; }
+constexpr int OFF_WD = OFF_B0 + H + 3 * LAYER, OFF_BD = OFF_WD + H * 4;
+constexpr int NPARAM = OFF_BD + 4;
+
+__device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
+
+// ---- encoder: one thread per (node, 8 outputs)
+__global__ void __launch_bounds__(256) gnn_encode_kernel(int nNo, const float* __restrict__ in_r,
+                                                         const double* __restrict__ in_r64,
+                                                         const float* __restrict__ stat, const double* __restrict__ sc,
+                                                         const __nv_bfloat16* __restrict__ P,
+                                                         __nv_bfloat16* __restrict__ h0, uint64_t* __restrict__ mask,
+                                                         const int* flags) {
+  if (flags && (flags[0] != 0 || flags[2] != 0)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long i = t >> 3;
+  const int cg = (int)(t & 7);
+  const bool live = i < nNo;  // no early return: the mask is assembled with warp shuffles
+  const float inv = (float)(1.0 / sc[0]);
+  float x[NIN];
+#pragma unroll
+  for (int k = 0; k < 4; k++) x[k] = live ? (in_r ? in_r[4 * i + k] : (float)in_r64[4 * i + k]) * inv : 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) x[4 + k] = live ? stat[4 * i + k] : 0.f;
+  uint32_t bits = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int col = cg * 8 + c;
+    float z = bf(P[OFF_B0 + col]);
+#pragma unroll
+    for (int k = 0; k < NIN; k++) z = fmaf(bf(P[OFF_W0 + k * H + col]), x[k], z);
+    if (z > 0.f) bits |= 1u << c;
+    if (live) h0[(long)H * i + col] = __float2bfloat16(z > 0.f ? z : 0.f);
+  }
+  if (mask) {
+    // 8 bits per thread -> the node's 64-bit relu mask, assembled with shuffles
+    uint64_t word = (uint64_t)bits << (8 * cg);
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) word |= __shfl_xor_sync(0xffffffffu, word, o);
+    if (cg == 0 && live) mask[i] = word;
+  }
+}
+
+// ---- message-passing layer: gather mean + dense 128 -> 64 + relu + residual.
+// Persistent CTAs of 128 threads keep the layer's weights in shared memory and walk
+// tiles of 16 nodes: the 4 warps gather (lanes over features, 128-byte rows), then
+// every thread computes 2 nodes x 4 outputs from the shared tile.
+constexpr int MP_NODES = 16;
+__global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                     const int* __restrict__ colPtr,
+                                                     const __nv_bfloat16* __restrict__ hin,
+                                                     const __nv_bfloat16* __restrict__ P, int layer,
+                                                     __nv_bfloat16* __restrict__ hout,
+                                                     __nv_bfloat16* __restrict__ msave, uint64_t* __restrict__ mask,
+                                                     const int* flags) {
+  if (flags && (flags[0] != 0 || flags[2] != 0)) return;
+  __shared__ float A[MP_NODES][2 * H + 1];
+  __shared__ __align__(16) float W[2 * H][H];
+  __shared__ float B[H];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const __nv_bfloat16* Wg = P + off_w(layer);
+  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) W[k / H][k % H] = bf(Wg[k]);
+  for (int k = threadIdx.x; k < H; k += blockDim.x) B[k] = bf(P[off_b(layer) + k]);
+  const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
+  const int ng = threadIdx.x >> 4, cgp = threadIdx.x & 15;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int node0 = tile * MP_NODES;
+    __syncthreads();
+    for (int q = warp; q < MP_NODES; q += 4) {
+      const int i = node0 + q;
+      float s0 = 0.f, s1 = 0.f, o0 = 0.f, o1 = 0.f;
+      if (i < nNo) {
+        const int b = rowPtr[i], e = rowPtr[i + 1];
+        const __nv_bfloat162 own = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * i)[lane];
+        o0 = __low2float(own);
+        o1 = __high2float(own);
+        for (int k = b; k < e; k++) {
+          const int j = __ldg(colPtr + k);
+          const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * j)[lane];
+          s0 += __low2float(v);
+          s1 += __high2float(v);
+        }
+        const float inv = 1.f / (float)(e - b);
+        s0 *= inv;
+        s1 *= inv;
+        if (msave) reinterpret_cast<__nv_bfloat162*>(msave + (long)H * i)[lane] = __floats2bfloat162_rn(s0, s1);
+      }
+      A[q][2 * lane] = o0;
+      A[q][2 * lane + 1] = o1;
+      A[q][H + 2 * lane] = s0;
+      A[q][H + 2 * lane + 1] = s1;
+    }
+    __syncthreads();
+    float acc[2][4];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[a][c] = B[cgp * 4 + c];
+#pragma unroll 8
+    for (int k = 0; k < 2 * H; k++) {
+      const float4 w = *reinterpret_cast<const float4*>(&W[k][cgp * 4]);
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        const float x = A[ng * 2 + a][k];
+        acc[a][0] = fmaf(x, w.x, acc[a][0]);
+        acc[a][1] = fmaf(x, w.y, acc[a][1]);
+        acc[a][2] = fmaf(x, w.z, acc[a][2]);
+        acc[a][3] = fmaf(x, w.w, acc[a][3]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+      const int q = ng * 2 + a;
+      const int i = node0 + q;
+      uint32_t bits = 0;
+      float o[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const float z = acc[a][c];
+        if (z > 0.f) bits |= 1u << c;
+        o[c] = A[q][cgp * 4 + c] + (z > 0.f ? z : 0.f);
+      }
+      if (i < nNo) {
+        __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(hout + (long)H * i + cgp * 4);
+        dst[0] = __floats2bfloat162_rn(o[0], o[1]);
+        dst[1] = __floats2bfloat162_rn(o[2], o[3]);
+      }
+      if (mask) {
+        // the 16 threads of a node (a half warp) contribute 4 bits each; every lane
+        // takes part in the shuffles
+        uint64_t word = (uint64_t)bits << (4 * cgp);
+#pragma unroll
+        for (int off = 1; off < 16; off <<= 1) word |= __shfl_xor_sync(0xffffffffu, word, off);
+        if (cgp == 0 && i < nNo) mask[(long)layer * nNo + i] = word;
+      }
+    }
+  }
+}
+
+// ---- decoder: out_i = s (Wd^T h_i + bd); output FP32 or FP64, optional add
+__global__ void __launch_bounds__(256) gnn_decode_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
+                                                         const __nv_bfloat16* __restrict__ P,
+                                                         const double* __restrict__ sc, float* __restrict__ out32,
+                                                         double* __restrict__ out64, float* __restrict__ raw,
+                                                         const int* flags) {
+  if (flags && (flags[0] != 0 || flags[2] != 0)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long i = t >> 2;
+  const int c = (int)(t & 3);
+  if (i >= nNo) return;
+  float z = bf(P[OFF_BD + c]);
+  const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(h + (long)H * i);
+#pragma unroll 8
+  for (int k = 0; k < H / 2; k++) {
+    const __nv_bfloat162 v = hv[k];
+    z = fmaf(__low2float(v), bf(P[OFF_WD + (2 * k) * 4 + c]), z);
+    z = fmaf(__high2float(v), bf(P[OFF_WD + (2 * k + 1) * 4 + c]), z);
+  }
+  if (raw) raw[4 * i + c] = z;
+  const double s = sc[0];
+  if (out32) out32[4 * i + c] = (float)(s * z);
+  if (out64) out64[4 * i + c] = s * (double)z;
+}
+
+// ---- loss: per CTA partial of sum |out - t/s|^2 and |t/s|^2; d_out = 2 (out - t/s) / E
+__global__ void __launch_bounds__(256) gnn_loss_kernel(long n, const float* __restrict__ out,
+                                                       const float* __restrict__ tgt, const double* __restrict__ sc,
+                                                       double* __restrict__ part) {
+  __shared__ double r0[8], r1[8];
+  const float inv = (float)(1.0 / sc[0]);
+  double a = 0.0, b = 0.0;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const float tt = tgt[k] * inv;
+    const float d = out[k] - tt;
+    a += (double)d * d;
+    b += (double)tt * tt;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r0[threadIdx.x >> 5] = a;
+    r1[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0, s1 = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+      s0 += r0[q];
+      s1 += r1[q];
+    }
+    part[2 * blockIdx.x] = s0;
+    part[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+__global__ void gnn_loss_final_kernel(int nparts, const double* __restrict__ part, double* __restrict__ loss) {
+  if (threadIdx.x != 0) return;
+  double a = 0, b = 0;
+  for (int c = 0; c < nparts; c++) {
+    a += part[2 * c];
+    b += part[2 * c + 1];
+  }
+  loss[0] = a / b;  // relative squared error
+  loss[1] = b;
+}
+
+// d_out = 2 (out - t/s) / E ; decoder backward: dh3 = Wd d_out (FP32), and the
+// per-CTA partial of dWd = sum_i h_i d_out_i^T, dbd = sum d_out.
+__global__ void __launch_bounds__(128) gnn_decode_bwd_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
+                                                             const float* __restrict__ out,
+                                                             const float* __restrict__ tgt,
+                                                             const double* __restrict__ sc,
+                                                             const double* __restrict__ loss,
+                                                             const __nv_bfloat16* __restrict__ P,
+                                                             float* __restrict__ dh, float* __restrict__ gpart) {
+  __shared__ float g[H * 4 + 4];
+  for (int k = threadIdx.x; k < H * 4 + 4; k += blockDim.x) g[k] = 0.f;
+  __syncthreads();
+  const float inv = (float)(1.0 / sc[0]);
+  const float scale = (float)(2.0 / loss[1]);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nNo; i += (long)gridDim.x * blockDim.x) {
+    float d[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) d[c] = scale * (out[4 * i + c] - tgt[4 * i + c] * inv);
+    const __nv_bfloat16* hi = h + (long)H * i;
+    for (int k = 0; k < H; k++) {
+      const float hk = bf(hi[k]);
+      float acc = 0.f;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        acc = fmaf(bf(P[OFF_WD + k * 4 + c]), d[c], acc);
+        atomicAdd(&g[k * 4 + c], hk * d[c]);
+      }
+      dh[(long)H * i + k] = acc;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) atomicAdd(&g[H * 4 + c], d[c]);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < H * 4 + 4; k += blockDim.x) gpart[(long)blockIdx.x * (H * 4 + 4) + k] = g[k];
+}
+
+// ---- message-passing layer backward, dense part.  dh (FP32, gradient of the
+// layer output) -> dz = dh * relu'(z); d[h;m] = W dz; dhd = dh + d[h]; dms = d[m] / deg.
+// Weight gradient partial per CTA: [h; m]^T dz (128 x 64) and sum dz (64).
+__global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                         const __nv_bfloat16* __restrict__ hin,
+                                                         const __nv_bfloat16* __restrict__ msave,
+                                                         const uint64_t* __restrict__ mask, int layer,
+                                                         const __nv_bfloat16* __restrict__ P,
+                                                         const float* __restrict__ dh, float* __restrict__ dhd,
+                                                         float* __restrict__ dms, float* __restrict__ gpart) {
+  __shared__ float X[MP_NODES][2 * H + 1];
+  __shared__ float DZ[MP_NODES][H + 1];
+  __shared__ float W[2 * H][H];
+  const __nv_bfloat16* Wg = P + off_w(layer);
+  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) W[k / H][k % H] = bf(Wg[k]);
+  // each thread owns 64 entries of the 128 x 64 weight gradient (+ bias share)
+  float gacc[64];
+#pragma unroll
+  for (int q = 0; q < 64; q++) gacc[q] = 0.f;
+  float gb = 0.f;
+  const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int node0 = tile * MP_NODES;
+    __syncthreads();
+    for (int k = threadIdx.x; k < MP_NODES * H; k += blockDim.x) {
+      const int q = k / H, f = k % H;
+      const int i = node0 + q;
+      float x0 = 0.f, x1 = 0.f, dz = 0.f;
+      if (i < nNo) {
+        x0 = bf(hin[(long)H * i + f]);
+        x1 = bf(msave[(long)H * i + f]);
+        const uint64_t m = mask[(long)layer * nNo + i];
+        dz = ((m >> f) & 1ull) ? dh[(long)H * i + f] : 0.f;
+      }
+      X[q][f] = x0;
+      X[q][H + f] = x1;
+      DZ[q][f] = dz;
+    }
+    __syncthreads();
+    // d[h;m] = W dz: thread -> node q = t / 8, features (t % 8) * 16 .. +15
+    {
+      const int q = threadIdx.x >> 3, part = threadIdx.x & 7;
+      const int i = node0 + q;
+      if (i < nNo) {
+        const float invdeg = 1.f / (float)(rowPtr[i + 1] - rowPtr[i]);
+        for (int r = part * 16; r < part * 16 + 16; r++) {
+          float acc = 0.f;
+#pragma unroll 8
+          for (int c = 0; c < H; c++) acc = fmaf(W[r][c], DZ[q][c], acc);
+          if (r < H)
+            dhd[(long)H * i + r] = dh[(long)H * i + r] + acc;
+          else
+            dms[(long)H * i + (r - H)] = acc * invdeg;
+        }
+      }
+    }
+    // weight gradient: thread owns row r = t (0..127), all 64 columns: X[:,r]^T DZ
+    {
+      const int r = threadIdx.x;
+#pragma unroll 4
+      for (int q = 0; q < MP_NODES; q++) {
+        const float x = X[q][r];
+#pragma unroll
+        for (int c = 0; c < 64; c++) gacc[c] = fmaf(x, DZ[q][c], gacc[c]);
+      }
+      if (r < H)
+        for (int q = 0; q < MP_NODES; q++) gb += DZ[q][r];
+    }
+  }
+  float* gp = gpart + (long)blockIdx.x * LAYER;
+#pragma unroll
+  for (int c = 0; c < 64; c++) gp[threadIdx.x * H + c] = gacc[c];
+  if (threadIdx.x < H) gp[2 * H * H + threadIdx.x] = gb;
+}
+
+// dh_prev_j = dhd_j + sum_{i in N(j)} dms_i   (the pattern is symmetric)
+__global__ void __launch_bounds__(256) gnn_scatter_bwd_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                              const int* __restrict__ colPtr,
+                                                              const float* __restrict__ dhd,
+                                                              const float* __restrict__ dms,
+                                                              float* __restrict__ dprev) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long j = t >> 5;
+  const int lane = (int)(t & 31);
+  if (j >= nNo) return;
+  float2 acc = reinterpret_cast<const float2*>(dhd + (long)H * j)[lane];
+  for (int k = rowPtr[j]; k < rowPtr[j + 1]; k++) {
+    const int i = __ldg(colPtr + k);
+    const float2 v = reinterpret_cast<const float2*>(dms + (long)H * i)[lane];
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  reinterpret_cast<float2*>(dprev + (long)H * j)[lane] = acc;
+}
+
+// encoder backward: dz0 = dh0 * relu'; dW0 partial = x^T dz0, db0 = sum dz0
+__global__ void __launch_bounds__(64) gnn_encode_bwd_kernel(int nNo, const float* __restrict__ in_r,
+                                                            const float* __restrict__ stat,
+                                                            const double* __restrict__ sc,
+                                                            const uint64_t* __restrict__ mask,
+                                                            const float* __restrict__ dh, float* __restrict__ gpart) {
+  // thread c (0..63) owns column c of W0 (8 entries) and b0[c]
+  const int c = threadIdx.x;
+  float g[NIN + 1];
+#pragma unroll
+  for (int k = 0; k <= NIN; k++) g[k] = 0.f;
+  const float inv = (float)(1.0 / sc[0]);
+  for (long i = blockIdx.x; i < nNo; i += gridDim.x) {
+    const uint64_t m = mask[i];
+    if (!((m >> c) & 1ull)) continue;
+    const float dz = dh[(long)H * i + c];
+#pragma unroll
+    for (int k = 0; k < 4; k++) g[k] = fmaf(in_r[4 * i + k] * inv, dz, g[k]);
+#pragma unroll
+    for (int k = 0; k < 4; k++) g[4 + k] = fmaf(stat[4 * i + k], dz, g[4 + k]);
+    g[NIN] += dz;
+  }
+  float* gp = gpart + (long)blockIdx.x * (NIN * H + H);
+#pragma unroll
+  for (int k = 0; k < NIN; k++) gp[k * H + c] = g[k];
+  gp[NIN * H + c] = g[NIN];
+}
+
+// grad[off + k] = sum over parts of part[p * stride + k] (fixed order)
+__global__ void gnn_reduce_grad_kernel(int nparts, int stride, int len, const float* __restrict__ part,
+                                       float* __restrict__ grad) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= len) return;
+  float s = 0.f;
+  for (int p = 0; p < nparts; p++) s += part[(long)p * stride + k];
+  grad[k] = s;
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the BF16 copy.
+__global__ void gnn_adam_kernel(int n, float lr, float b1, float b2, float epsa, int step,
+                                const float* __restrict__ g, float* __restrict__ p, float* __restrict__ m,
+                                float* __restrict__ v, __nv_bfloat16* __restrict__ pb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float gk = g[k];
+  const float mk = b1 * m[k] + (1.f - b1) * gk;
+  const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+  m[k] = mk;
+  v[k] = vk;
+  const float mh = mk / (1.f - powf(b1, (float)step));
+  const float vh = vk / (1.f - powf(b2, (float)step));
+  const float pk = p[k] - lr * mh / (sqrtf(vh) + epsa);
+  p[k] = pk;
+  pb[k] = __float2bfloat16(pk);
+}
+
+__global__ void gnn_to_bf16_kernel(int n, const float* __restrict__ p, __nv_bfloat16* __restrict__ pb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) pb[k] = __float2bfloat16(p[k]);
+}
+
+__global__ void rms_scale_kernel(const double* __restrict__ nrm2, long n, double* __restrict__ sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = sqrt(*nrm2 / (double)n);
+    sc[0] = s > 0.0 ? s : 1.0;
+  }
+}
+
+__global__ void f64_to_f32_k(long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+}  // namespace
+
+int gnn_param_count() { return NPARAM; }
+
+// Forward pass.  r: FP32 (r32) or FP64 (r64) input vector (4, nNo); sc: device scale s.
+// h: 4 activation buffers (BF16, nNo x 64 each); msave/mask may be null (inference).
+void gnn_forward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
+                 const double* r64, const float* stat, const double* sc, const __nv_bfloat16* P,
+                 __nv_bfloat16* const* h, __nv_bfloat16* const* msave, uint64_t* mask, float* out32,
+                 double* out64, float* raw, int sm_count, const int* flags) {
+  const long t = 8L * nNo;
+  gnn_encode_kernel<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(nNo, r32, r64, stat, sc, P, h[0], mask, flags);
+  const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
+  const int grid = tiles < 8 * sm_count ? tiles : 8 * sm_count;
+  for (int l = 1; l <= 3; l++)
+    gnn_mp_kernel<<<grid, 128, 0, st>>>(nNo, rowPtr, colPtr, h[l - 1], P, l, h[l], msave ? msave[l] : nullptr, mask,
+                                        flags);
+  gnn_decode_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, st>>>(nNo, h[3], P, sc, out32, out64, raw, flags);
+}
+
+void gnn_scale(cudaStream_t st, const double* nrm2, long n, double* sc) { rms_scale_kernel<<<1, 32, 0, st>>>(nrm2, n, sc); }
+
+void gnn_f64_to_f32(cudaStream_t st, long n, const double* a, float* b) {
+  f64_to_f32_k<<<grid_for(n, 256), 256, 0, st>>>(n, a, b);
+}
+
+// Loss + backward + gradient.  raw: decoder outputs (before the scale s) of the
+// forward pass; tgt: FP32 target increments.  grad (NPARAM floats) is written.
+// Work buffers: dA, dB, dC (nNo x 64 FP32 each), part (partials), lossbuf (2 doubles).
+void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
+                  const float* stat, const double* sc, const __nv_bfloat16* P, __nv_bfloat16* const* h,
+                  __nv_bfloat16* const* msave, const uint64_t* mask, const float* raw, const float* tgt,
+                  float* dA, float* dB, float* dC, float* part, double* lossbuf, float* grad, int sm_count) {
+  const long n4 = 4L * nNo;
+  const int lparts = 2 * sm_count;
+  gnn_loss_kernel<<<lparts, 256, 0, st>>>(n4, raw, tgt, sc, lossbuf + 2);
+  gnn_loss_final_kernel<<<1, 32, 0, st>>>(lparts, lossbuf + 2, lossbuf);
+  // decoder
+  const int dparts = 2 * sm_count;
+  gnn_decode_bwd_kernel<<<dparts, 128, 0, st>>>(nNo, h[3], raw, tgt, sc, lossbuf, P, dA, part);
+  gnn_reduce_grad_kernel<<<(H * 4 + 4 + 255) / 256, 256, 0, st>>>(dparts, H * 4 + 4, H * 4 + 4, part, grad + OFF_WD);
+  // layers 3..1: dA holds the gradient of the layer output
+  float* dcur = dA;
+  float* dtmp = dB;
+  const int mparts = 2 * sm_count;
+  for (int l = 3; l >= 1; l--) {
+    gnn_mp_bwd_kernel<<<mparts, 128, 0, st>>>(nNo, rowPtr, h[l - 1], msave[l], mask, l, P, dcur, dtmp, dC, part);
+    gnn_reduce_grad_kernel<<<(LAYER + 255) / 256, 256, 0, st>>>(mparts, LAYER, LAYER, part, grad + off_w(l));
+    gnn_scatter_bwd_kernel<<<(unsigned)((32L * nNo + 255) / 256), 256, 0, st>>>(nNo, rowPtr, colPtr, dtmp, dC, dcur);
+  }
+  // encoder
+  const int eparts = 4 * sm_count;
+  gnn_encode_bwd_kernel<<<eparts, 64, 0, st>>>(nNo, r32, stat, sc, mask, dcur, part);
+  gnn_reduce_grad_kernel<<<(NIN * H + H + 255) / 256, 256, 0, st>>>(eparts, NIN * H + H, NIN * H + H, part,
+                                                                   grad + OFF_W0);
+}
+
+void gnn_adam(cudaStream_t st, float lr, int step, const float* g, float* p, float* m, float* v, __nv_bfloat16* pb) {
+  gnn_adam_kernel<<<(NPARAM + 255) / 256, 256, 0, st>>>(NPARAM, lr, 0.9f, 0.999f, 1e-8f, step, g, p, m, v, pb);
+}
+
+void gnn_to_bf16(cudaStream_t st, const float* p, __nv_bfloat16* pb) {
+  gnn_to_bf16_kernel<<<(NPARAM + 255) / 256, 256, 0, st>>>(NPARAM, p, pb);
+}
+
+size_t gnn_part_floats(int sm_count) {
+  size_t a = (size_t)2 * sm_count * LAYER;
+  size_t b = (size_t)4 * sm_count * (NIN * H + H);
+  size_t c = (size_t)2 * sm_count * (H * 4 + 4);
+  return std::max(a, std::max(b, c));
+}
+
+}  // namespace svgpu
