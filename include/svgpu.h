@@ -25,7 +25,8 @@ enum svgpu_status {
   SVGPU_EJAC = -3,     /* zero element Jacobian (fluid.cpp:612-614) */
   SVGPU_ESTATE = -4,   /* call order: e.g. solve before svgpu_lhs_create */
   SVGPU_ENAN = -5,     /* non-finite residual or Krylov breakdown */
-  SVGPU_ENOMEM = -6
+  SVGPU_ENOMEM = -6,
+  SVGPU_ETOOBIG = -7   /* vector longer than svgpu_fsils_dot_noalloc's fixed scratch allows */
 };
 
 /* reference enums kept with their meaning (fils_struct.hpp:40-76, consts.h) */
@@ -98,6 +99,25 @@ int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, in
  * svgpu_construct_* calls assembled) and leave the increment there. */
 int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec,
                       const int* incL, const double* res, svgpu_ls_stats* stats);
+
+/* Allocation-free dot product of two device vectors U, V of dof*nNo entries.  It has
+ * no counterpart in the reference: it is the same reduction the solver's Gram-Schmidt
+ * and norms use (the value fsils_nc_dot_v, dot.cpp:134-171, computes), for callers
+ * that cannot allocate device memory -- code recording a CUDA graph, where cudaMalloc
+ * is not permitted during stream capture, or code whose device memory belongs to
+ * another allocator or a fixed budget.  It calls no cudaMalloc/cudaFree: its per-CTA
+ * partial sums live in a file-scope __device__ array of 4097 doubles (32 KB), held by
+ * every GPU that loads the library until the process exits.  Limit: dof*nNo <=
+ * 16,777,216 entries, else SVGPU_ETOOBIG.  U and V must be device pointers (else
+ * SVGPU_EINVAL); *result may be a device or a host pointer (a host result is copied
+ * back and the stream synchronised).  The work runs on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream) of the calling thread's current device.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the array and each
+ * call overwrites the partial sums it reads, so nothing needs clearing between calls;
+ * calls whose kernels overlap on the GPU (unordered streams) race on it. */
+int svgpu_fsils_dot_noalloc(int dof, int nNo, const double* U, const double* V, double* result,
+                            void* stream);
 
 /* Block SpMV KU = K U for any dof (fsils_spar_mul_vv, spar_mul.cpp:191-258). */
 int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, double* KU);
