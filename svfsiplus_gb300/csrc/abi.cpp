@@ -521,8 +521,12 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   rc = gmres_mixed(ctx, Val32, R, R, st);
   if (rc) return rc;
-  if (collect && st->suc) {  // (preconditioned residual, preconditioned increment) pair
-    if ((rc = gnn_store_pair(ctx, kw.rsave.p, R))) return rc;
+  if (collect && st->iNorm > ctx->absTol) {
+    // exact pair (K X, X) of the preconditioned system: K X = Rs - r, with r the final
+    // FP64 residual the solve left in kw.r64 (valid whether or not it converged)
+    launch_sub(ctx->stream, n, kw.rsave.p, kw.r64.p, kw.rbak.p);
+    ctx->launches++;
+    if ((rc = gnn_store_pair(ctx, kw.rbak.p, R))) return rc;
   }
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches++;

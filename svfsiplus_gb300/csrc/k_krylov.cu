@@ -162,6 +162,52 @@ __global__ void __launch_bounds__(256) multidot_kernel(long n, int m, const doub
   }
 }
 
+
+// Tall-skinny V^T w, version 2: persistent CTAs walk tiles of MD_TILE entries; the
+// tile of w is staged in shared memory once and every warp streams whole basis
+// vectors j = warp, warp + 8, ... against it, so w is read from memory once and each
+// V_j once.  A lane keeps its running sums for its j's in registers across tiles;
+// one partial per (CTA, j) is written at the end (fixed order: deterministic).
+constexpr int MD_TILE = 2048;
+constexpr int MD_JMAX = 8;  // j's per warp: m <= 8 warps x 8 = 64
+
+template <typename TV, typename TA>
+__global__ void __launch_bounds__(256) multidot2_kernel(long n, int m, const TV* __restrict__ V, long ldv,
+                                                        const TV* __restrict__ w, double* __restrict__ partial,
+                                                        const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ TV ws[MD_TILE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double acc[MD_JMAX];
+#pragma unroll
+  for (int q = 0; q < MD_JMAX; q++) acc[q] = 0.0;
+  const long tiles = (n + MD_TILE - 1) / MD_TILE;
+  for (long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const long base = t * MD_TILE;
+    const int len = (int)(n - base < MD_TILE ? n - base : MD_TILE);
+    __syncthreads();
+    for (int k = threadIdx.x; k < len; k += blockDim.x) ws[k] = w[base + k];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < MD_JMAX; q++) {
+      const int j = warp + 8 * q;
+      if (j >= m) break;
+      const TV* vj = V + (long)j * ldv + base;
+      TA a = 0;
+      for (int k = lane; k < len; k += 32) a += (TA)__ldcs(vj + k) * (TA)ws[k];
+      acc[q] += (double)a;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < MD_JMAX; q++) {
+    const int j = warp + 8 * q;
+    if (j >= m) break;
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) partial[(long)blockIdx.x * m + j] = v;
+  }
+}
+
 __global__ void reduce_partials_kernel(int nparts, int m, const double* __restrict__ partial,
                                        double* __restrict__ out, const int* flags) {
   if (stopped(flags)) return;
@@ -342,7 +388,7 @@ void launch_mask_face(cudaStream_t s, int nNo, int fdof, int dof, const int* glo
 }
 
 int multidot_ctas(long n, int sm_count) {
-  long per = 4096;  // at least this many entries per CTA
+  long per = 2048;  // at least one tile of entries per CTA
   long c = (n + per - 1) / per;
   long cap = 2L * sm_count;
   if (c > cap) c = cap;
@@ -353,7 +399,10 @@ int multidot_ctas(long n, int sm_count) {
 int launch_multidot_flag(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
                          double* partial, int sm_count, const int* flags) {
   const int ctas = multidot_ctas(n, sm_count);
-  multidot_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  if (m <= 8 * MD_JMAX)
+    multidot2_kernel<double, double><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  else
+    multidot_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
   return ctas;
 }
 
@@ -598,7 +647,10 @@ void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int*
 int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
                       int sm_count, const int* flags) {
   const int ctas = multidot_ctas(n, sm_count);
-  multidot32_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  if (m <= 8 * MD_JMAX)
+    multidot2_kernel<float, float><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
+  else
+    multidot32_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
   return ctas;
 }
 
