@@ -138,6 +138,32 @@ int svgpu_face_create(svgpu_ctx* ctx, int faceId, int nFaEl, const int* fIEN, co
  * Returns SVGPU_EJAC for a zero Jacobian. */
 int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag,
                           const double* Yg, const double* Bf, double* R, double* Val, int precision);
+/* Neo-Hookean solid with a volumetric penalty (stModelType nHook + Kpen/volType,
+ * ComMod.h:345-390; get_svol_p volType 0 Quad, 1 ST91, 2 M94) and the equation's
+ * second-order generalised-alpha constants. */
+typedef struct {
+  double rho, damping;
+  double f[3];
+  double C10, Kpen;
+  int volType;
+  double dt, am, af, gam, beta;
+} svgpu_solid_props;
+
+/* Replaces construct_dsolid (solver/sv_struct.cpp:213, struct_3d_carray :552) for
+ * linear tets: adds into R (dof,nNo) and Val (dof*dof,nnz), dof = 3 (the struct
+ * equation) or 4 (the solid blocks of the FSI equation, fsi.cpp:213-262).  State
+ * arrays (tDof,nNo) with the displacement components at rows s..s+2.  Caller-owned
+ * R/Val (host or device), additive. */
+int svgpu_construct_dsolid(svgpu_ctx* ctx, const svgpu_solid_props* props, int dof, int tDof, int s,
+                           const double* Ag, const double* Yg, const double* Dg, double* R, double* Val);
+
+/* Replaces construct_mesh (solver/mesh.cpp:49, l_elas_3d l_elas.cpp:274): linear-elastic
+ * mesh motion in the configuration x + Do, weights without the Jacobian; dof 3;
+ * state (tDof,nNo) with the mesh equation at rows s..s+2 (Do at the same rows). */
+int svgpu_construct_mesh(svgpu_ctx* ctx, double E, double nu, double rho, double dt, double am, double af,
+                         double beta, int tDof, int s, const double* Ag, const double* Dg, const double* Do,
+                         double* R, double* Val);
+
 /* Copies the resident system out: R (4,nNo) and Val (16,nnz) as FP64 (an FP32
  * tangent from SVGPU_MIXED assembly is widened).  Either pointer may be NULL.  No
  * counterpart in the reference, where R and Val live in ComMod (ComMod.h:1563-1566). */
@@ -147,6 +173,34 @@ int svgpu_get_system(svgpu_ctx* ctx, double* R, double* Val);
  * face: Neumann value h on every face node plus backflow stabilisation. */
 int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h,
                        const double* Yg, double* R, double* Val);
+
+/* ---- learned preconditioner (no counterpart in the reference) ------------------------
+ * A 3-layer message-passing network on the CSR graph (hidden width 64, BF16 weights,
+ * FP32 accumulation) trained online on (residual, increment) pairs of the
+ * Jacobi-scaled system that the mixed-precision solves store.  node_features (4,nNo):
+ * scaled coordinates and wall distance.  Parameters are an FP32 vector of
+ * svgpu_gnn_param_count() floats. */
+int svgpu_gnn_param_count(void);
+int svgpu_gnn_create(svgpu_ctx* ctx, const float* node_features, unsigned long long seed);
+int svgpu_gnn_get_params(svgpu_ctx* ctx, float* params, int n);
+int svgpu_gnn_set_params(svgpu_ctx* ctx, const float* params, int n);
+/* z = M(r) for a (4,nNo) vector */
+int svgpu_gnn_apply(svgpu_ctx* ctx, const double* r, double* z);
+/* relative squared error of M(r) against x and its gradient (params floats) */
+int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* x, double* loss, float* grad);
+/* store a training pair; switch storing of the solver's own pairs on or off */
+int svgpu_gnn_add_pair(svgpu_ctx* ctx, const double* r, const double* x);
+int svgpu_gnn_collect(svgpu_ctx* ctx, int on);
+/* iters Adam steps (Kingma & Ba) over the stored pairs, learning rate lr; mean loss out */
+int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
+/* Solver of the mixed-precision path: 0 GMRES + diagonal preconditioner (the
+ * reference's method); 1 FGMRES with the network as right preconditioner and initial
+ * guess; 2 FGMRES with an aggregation multilevel V-cycle (block-Jacobi smoothing) as
+ * right preconditioner; 3 as 2 with the network as finest-level pre-smoother and
+ * initial guess.  Learned initial guesses and learned cycles that do not lower the
+ * FP64 residual are rejected (plain cycles finish the solve). */
+int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
+long long svgpu_learned_rejects(const svgpu_ctx* ctx);
 
 /* ---- Newton time step (solver/main.cpp:292-762 for one fluid equation) ----------- */
 typedef struct {

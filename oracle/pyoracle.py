@@ -31,6 +31,51 @@ class FluidParams(C.Structure):
                  "dt", "am", "af", "gam", "beta")]
 
 
+class StructParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("rho", "damping", "fx", "fy", "fz", "C10", "Kpen")] + \
+               [("volType", C.c_int)] + [(n, C.c_double) for n in ("dt", "am", "af", "gam", "beta")]
+
+
+def genalpha_second_order(rho_inf):
+    am = (2.0 - rho_inf) / (1.0 + rho_inf)
+    af = 1.0 / (1.0 + rho_inf)
+    beta = 0.25 * (1.0 + am - af) ** 2
+    gam = 0.5 + am - af
+    return am, af, gam, beta
+
+
+def struct_params(rho, E, nu, C10, Kpen, dt, rho_inf, volType=1):
+    am, af, gam, beta = genalpha_second_order(rho_inf)
+    return StructParams(rho, 0.0, 0.0, 0.0, 0.0, C10, Kpen, volType, dt, am, af, gam, beta)
+
+
+def construct_struct(P, x, ien, A, Y, D, rowPtr, colPtr):
+    nNo = x.shape[0]
+    R = np.zeros((nNo, 3))
+    Val = np.zeros((colPtr.size, 9))
+    rc = lib().or_construct_struct(C.byref(P), nNo, ien.shape[0], _p(np.ascontiguousarray(ien, dtype=np.int32)),
+                                   _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(A)),
+                                   _p(np.ascontiguousarray(Y)), _p(np.ascontiguousarray(D)),
+                                   _p(rowPtr), _p(colPtr), _p(R), _p(Val))
+    if rc != 0:
+        raise RuntimeError("zero Jacobian")
+    return R, Val
+
+
+def construct_mesh(E, nu, rho, dt, rho_inf, x, ien, A, D, Do, rowPtr, colPtr):
+    am, af, gam, beta = genalpha_second_order(rho_inf)
+    nNo = x.shape[0]
+    R = np.zeros((nNo, 3))
+    Val = np.zeros((colPtr.size, 9))
+    rc = lib().or_construct_mesh(*(C.c_double(v) for v in (E, nu, rho, dt, am, af, beta)), nNo, ien.shape[0],
+                                 _p(np.ascontiguousarray(ien, dtype=np.int32)), _p(np.ascontiguousarray(x)),
+                                 _p(np.ascontiguousarray(A)), _p(np.ascontiguousarray(D)),
+                                 _p(np.ascontiguousarray(Do)), _p(rowPtr), _p(colPtr), _p(R), _p(Val))
+    if rc != 0:
+        raise RuntimeError("zero Jacobian")
+    return R, Val
+
+
 class LS(C.Structure):
     _fields_ = [("sD", C.c_int), ("mItr", C.c_int), ("relTol", C.c_double), ("absTol", C.c_double),
                 ("iNorm", C.c_double), ("fNorm", C.c_double), ("dB", C.c_double),

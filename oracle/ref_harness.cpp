@@ -97,6 +97,112 @@ static void setup_face(faceType& fa, const std::string& dir, const std::string& 
   for (int g = 0; g < fa.nG; g++) nn::get_gnn(nullptr, g, fa);
 }
 
+// Assembly of one solid (construct_dsolid, sv_struct.cpp:213) or mesh-motion
+// (construct_mesh, mesh.cpp:49) system on the case mesh with the given state arrays;
+// dumps R and Val.  The mesh equation sits at rows 4..6 of a 7-dof state, as in the
+// FSI set-up the reference uses it in (construct_mesh reads Do at rows nsd+1..2nsd).
+static int assemble_only(const std::string& dir, const std::string& out, std::map<std::string, std::string>& P) {
+  auto getd = [&](const char* k) { return std::stod(P.at(k)); };
+  const bool is_mesh = P.at("mode") == "assemble_mesh";
+  Simulation sim;
+  auto& com = sim.com_mod;
+  auto xs = read_raw<double>(dir + "/x.bin");
+  auto iens = read_raw<int>(dir + "/ien.bin");
+  const int nNo = (int)xs.size() / 3;
+  const int nEl = (int)iens.size() / 4;
+  const int tDof = is_mesh ? 7 : 3;
+  com.nsd = 3;
+  com.nsymd = 6;
+  com.tnNo = nNo;
+  com.gtnNo = nNo;
+  com.nMsh = 1;
+  com.msh.resize(1);
+  com.nEq = 1;
+  com.eq.resize(1);
+  com.dt = getd("dt");
+  com.dFlag = true;
+  auto& msh = com.msh[0];
+  msh.eNoN = 4;
+  msh.nEl = nEl;
+  msh.gnEl = nEl;
+  msh.nNo = nNo;
+  msh.IEN.resize(4, nEl);
+  for (int e = 0; e < nEl; e++)
+    for (int a = 0; a < 4; a++) msh.IEN(a, e) = iens[4 * e + a];
+  msh.gN.resize(nNo);
+  for (int a = 0; a < nNo; a++) msh.gN(a) = a;
+  nn::select_ele(com, msh);
+  msh.nFs = 1;
+  fs::init_fs_msh(com, msh);
+  com.x.resize(3, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < 3; i++) com.x(i, a) = xs[3 * a + i];
+  com.Bf.resize(3, nNo);
+  auto& eq = com.eq[0];
+  eq.phys = is_mesh ? consts::EquationType::phys_mesh : consts::EquationType::phys_struct;
+  eq.dof = 3;
+  eq.roInf = getd("rho_inf");
+  eq.am = (2.0 - eq.roInf) / (1.0 + eq.roInf);  // second-order equation
+  eq.af = 1.0 / (1.0 + eq.roInf);
+  eq.beta = 0.25 * std::pow((1.0 + eq.am - eq.af), 2.0);
+  eq.gam = 0.5 + eq.am - eq.af;
+  eq.s = is_mesh ? 4 : 0;
+  eq.e = eq.s + 2;
+  eq.nDmn = 1;
+  eq.dmn.resize(1);
+  auto& dmn = eq.dmn[0];
+  dmn.Id = -1;
+  dmn.phys = eq.phys;
+  using PP = consts::PhysicalProperyType;
+  dmn.prop[PP::solid_density] = getd("rho");
+  dmn.prop[PP::elasticity_modulus] = getd("E");
+  dmn.prop[PP::poisson_ratio] = getd("nu");
+  dmn.prop[PP::damping] = 0.0;
+  dmn.prop[PP::f_x] = 0.0;
+  dmn.prop[PP::f_y] = 0.0;
+  dmn.prop[PP::f_z] = 0.0;
+  if (!is_mesh) {
+    dmn.stM.isoType = consts::ConstitutiveModelType::stIso_nHook;
+    dmn.stM.volType = consts::ConstitutiveModelType::stVol_ST91;
+    dmn.stM.C10 = getd("C10");
+    dmn.stM.Kpen = getd("Kpen");
+  }
+  com.tDof = tDof;
+  com.dof = 3;
+  int nnz = 0;
+  lhsa_ns::lhsa(&sim, nnz);
+  com.lhs.nnz = nnz;
+  FsilsLinearAlgebra fsils_la;
+  eq.linear_algebra = &fsils_la;
+  auto A = read_raw<double>(dir + "/A.bin");
+  auto Y = read_raw<double>(dir + "/Y.bin");
+  auto D = read_raw<double>(dir + "/D.bin");
+  Array<double> Ag(tDof, nNo), Yg(tDof, nNo), Dg(tDof, nNo);
+  com.Do.resize(tDof, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < tDof; i++) {
+      Ag(i, a) = A[tDof * a + i];
+      Yg(i, a) = Y[tDof * a + i];
+      Dg(i, a) = D[tDof * a + i];
+    }
+  if (is_mesh) {
+    auto Do = read_raw<double>(dir + "/Do.bin");
+    for (int a = 0; a < nNo; a++)
+      for (int i = 0; i < tDof; i++) com.Do(i, a) = Do[tDof * a + i];
+  }
+  ls_ns::ls_alloc(com, eq);
+  com.R.resize(3, nNo);
+  com.R = 0.0;
+  com.Val = 0.0;
+  com.cEq = 0;
+  eq_assem::global_eq_assem(com, sim.get_cep_mod(), msh, Ag, Yg, Dg);
+  write_raw(out + "/R_asm.bin", com.R.data(), (size_t)com.R.size());
+  write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
+  write_raw(out + "/rowPtr.bin", com.rowPtr.data(), (size_t)com.rowPtr.size());
+  write_raw(out + "/colPtr.bin", com.colPtr.data(), (size_t)com.colPtr.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::fprintf(stderr, "usage: %s CASE_DIR OUT_DIR\n", argv[0]);
@@ -104,6 +210,7 @@ int main(int argc, char** argv) {
   }
   std::string dir = argv[1], out = argv[2];
   auto P = read_params(dir);
+  if (P.count("mode") && P.at("mode").rfind("assemble_", 0) == 0) return assemble_only(dir, out, P);
   auto getd = [&](const char* k) { return std::stod(P.at(k)); };
   auto geti = [&](const char* k) { return std::stoi(P.at(k)); };
 

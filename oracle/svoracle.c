@@ -641,3 +641,244 @@ int or_fluid_step(const or_fluid_problem* pb, const or_fluid_params* P, or_ls* l
   free(Ag); free(Yg); free(R); free(Val);
   return itr;
 }
+
+/* ---------------------------------------------------------------- solid and mesh */
+void or_genalpha_second_order(double rho_inf, double* am, double* af, double* gam, double* beta) {
+  *am = (2.0 - rho_inf) / (1.0 + rho_inf);
+  *af = 1.0 / (1.0 + rho_inf);
+  *beta = 0.25 * pow((1.0 + *am - *af), 2.0);
+  *gam = 0.5 + *am - *af;
+}
+
+static double det3(double a[3][3]) {
+  return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+}
+
+static void inv3(double a[3][3], double r[3][3]) {
+  double d = det3(a);
+  r[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / d;
+  r[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / d;
+  r[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / d;
+  r[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / d;
+  r[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / d;
+  r[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / d;
+  r[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / d;
+  r[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / d;
+  r[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / d;
+}
+
+/* neo-Hookean PK2 stress S and Voigt tangent Dm (get_pk2cc nHook + get_svol_p, no fibres) */
+static void pk2cc_nhook(const or_struct_params* P, double F[3][3], double S[3][3], double Dm[6][6]) {
+  const double nd = 3.0;
+  double J = det3(F);
+  double J2d = pow(J, -2.0 / nd);
+  double C[3][3], Ci[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      C[i][j] = 0.0;
+      for (int k = 0; k < 3; k++) C[i][j] += F[k][i] * F[k][j];
+    }
+  inv3(C, Ci);
+  double trC = C[0][0] + C[1][1] + C[2][2];
+  double Inv1 = J2d * trC;
+  double p = 0.0, pl = 0.0, Kp = P->Kpen;
+  if (fabs(Kp) > 0.0) {
+    if (P->volType == 0) { p = Kp * (J - 1.0); pl = Kp * (2.0 * J - 1.0); }
+    else if (P->volType == 1) { p = 0.50 * Kp * (J - 1.0 / J); pl = Kp * J; }
+    else { p = Kp * (1.0 - 1.0 / J); pl = Kp; }
+  }
+  double g1 = 2.0 * P->C10;
+  double r1 = g1 * Inv1 / nd;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) S[i][j] = J2d * g1 * (i == j ? 1.0 : 0.0) - r1 * Ci[i][j];
+  /* CC_ijkl = -2/3 (Ci_ij S_kl + S_ij Ci_kl) + 2 (r1 - pJ) 0.5 (Ci_ik Ci_jl + Ci_il Ci_jk)
+   *           + (pl J - 2 r1 / 3) Ci_ij Ci_kl */
+  static const int vi[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
+  double c1 = 2.0 * (r1 - p * J), c2 = pl * J - 2.0 * r1 / nd;
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) {
+      int i = vi[a][0], j = vi[a][1], k = vi[b][0], l = vi[b][1];
+      Dm[a][b] = (-2.0 / nd) * (Ci[i][j] * S[k][l] + S[i][j] * Ci[k][l]) +
+                 c1 * 0.5 * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]) + c2 * Ci[i][j] * Ci[k][l];
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) S[i][j] += p * J * Ci[i][j];
+}
+
+int or_struct_element(const or_struct_params* P, int dof, const double* xl, const double* al,
+                      const double* yl, const double* dl, double* lR, double* lK) {
+  double Nq[4][4], wq;
+  tet4_quadrature(Nq, &wq);
+  double Nx[3][4], Jac, ks[3][3];
+  gnn3(xl, Nx, &Jac, ks);
+  if (is_zero(Jac)) return -1;
+  memset(lR, 0, sizeof(double) * dof * 4);
+  memset(lK, 0, sizeof(double) * dof * dof * 16);
+  const double rho = P->rho, dmp = P->damping, dt = P->dt;
+  const double afu = P->af * P->beta * dt * dt;
+  const double amd = P->am * rho + P->af * P->gam * dt * dmp;
+  /* F is constant over the element for P1 */
+  double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) F[i][j] += Nx[j][a] * dl[dof * a + i];
+  double S[3][3], Dm[6][6];
+  pk2cc_nhook(P, F, S, Dm);
+  double Pk[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      Pk[i][j] = 0.0;
+      for (int k = 0; k < 3; k++) Pk[i][j] += F[i][k] * S[k][j];
+    }
+  double Bm[6][3][4];
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++) {
+      Bm[0][i][a] = Nx[0][a] * F[i][0];
+      Bm[1][i][a] = Nx[1][a] * F[i][1];
+      Bm[2][i][a] = Nx[2][a] * F[i][2];
+      Bm[3][i][a] = Nx[0][a] * F[i][1] + F[i][0] * Nx[1][a];
+      Bm[4][i][a] = Nx[1][a] * F[i][2] + F[i][1] * Nx[2][a];
+      Bm[5][i][a] = Nx[2][a] * F[i][0] + F[i][2] * Nx[0][a];
+    }
+  const double fb[3] = {P->fx, P->fy, P->fz};
+  for (int g = 0; g < 4; g++) {
+    const double* N = Nq[g];
+    const double w = wq * Jac;
+    double ud[3];
+    for (int i = 0; i < 3; i++) {
+      ud[i] = -rho * fb[i];
+      for (int a = 0; a < 4; a++) ud[i] += N[a] * (rho * al[dof * a + i] + dmp * yl[dof * a + i]);
+    }
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++)
+        lR[dof * a + i] += w * (N[a] * ud[i] + Nx[0][a] * Pk[i][0] + Nx[1][a] * Pk[i][1] + Nx[2][a] * Pk[i][2]);
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        double NxSNx = 0.0;
+        for (int k = 0; k < 3; k++)
+          for (int l = 0; l < 3; l++) NxSNx += Nx[k][a] * S[k][l] * Nx[l][b];
+        const double T1 = amd * N[a] * N[b] + afu * NxSNx;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) {
+            double BmDBm = 0.0;
+            for (int v = 0; v < 6; v++) {
+              double DB = 0.0;
+              for (int u = 0; u < 6; u++) DB += Dm[v][u] * Bm[u][j][b];
+              BmDBm += Bm[v][i][a] * DB;
+            }
+            lK[(dof * i + j) + dof * dof * a + dof * dof * 4 * b] += w * ((i == j ? T1 : 0.0) + afu * BmDBm);
+          }
+      }
+  }
+  return 0;
+}
+
+int or_mesh_element(double E, double nu, double rho, double dt, double am, double af, double beta,
+                    const double* xl, const double* al, const double* dl, double* lR, double* lK) {
+  double Nq[4][4], wq;
+  tet4_quadrature(Nq, &wq);
+  double Nx[3][4], Jac, ks[3][3];
+  gnn3(xl, Nx, &Jac, ks);
+  if (is_zero(Jac)) return -1;
+  memset(lR, 0, sizeof(double) * 12);
+  memset(lK, 0, sizeof(double) * 144);
+  const double lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+  const double mu = E * 0.5 / (1.0 + nu);
+  const double lDm = lambda / mu;
+  const double T1c = af * beta * dt * dt;
+  const double amd = am / T1c * rho;
+  for (int g = 0; g < 4; g++) {
+    const double* N = Nq[g];
+    const double w = wq;  /* no Jacobian (mesh.cpp:147) */
+    const double wl = w * T1c * mu;
+    double ud[3] = {0, 0, 0}, ed[6] = {0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+      const double* d = dl + 3 * a;
+      for (int i = 0; i < 3; i++) ud[i] += N[a] * al[3 * a + i];
+      ed[0] += Nx[0][a] * d[0];
+      ed[1] += Nx[1][a] * d[1];
+      ed[2] += Nx[2][a] * d[2];
+      ed[3] += Nx[1][a] * d[0] + Nx[0][a] * d[1];
+      ed[4] += Nx[2][a] * d[1] + Nx[1][a] * d[2];
+      ed[5] += Nx[0][a] * d[2] + Nx[2][a] * d[0];
+    }
+    const double divD = lambda * (ed[0] + ed[1] + ed[2]);
+    const double S[6] = {divD + 2.0 * mu * ed[0], divD + 2.0 * mu * ed[1], divD + 2.0 * mu * ed[2],
+                         mu * ed[3], mu * ed[4], mu * ed[5]};
+    for (int a = 0; a < 4; a++) {
+      lR[3 * a + 0] += w * (rho * N[a] * ud[0] + Nx[0][a] * S[0] + Nx[1][a] * S[3] + Nx[2][a] * S[5]);
+      lR[3 * a + 1] += w * (rho * N[a] * ud[1] + Nx[0][a] * S[3] + Nx[1][a] * S[1] + Nx[2][a] * S[4]);
+      lR[3 * a + 2] += w * (rho * N[a] * ud[2] + Nx[0][a] * S[5] + Nx[1][a] * S[4] + Nx[2][a] * S[2]);
+      for (int b = 0; b < 4; b++) {
+        double* K = lK + 9 * a + 36 * b;
+        const double NxdNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
+        const double T1 = amd * N[a] * N[b] / mu + NxdNx;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++)
+            K[3 * i + j] += wl * ((i == j ? T1 + (1.0 + lDm) * Nx[i][a] * Nx[i][b] : 0.0) +
+                                  (i == j ? 0.0 : lDm * Nx[i][a] * Nx[j][b] + Nx[j][a] * Nx[i][b]));
+      }
+    }
+  }
+  return 0;
+}
+
+/* do_assem (lhsa.cpp:97-141) for dof 3 */
+static void do_assem3(const int* ptr, const double* lK, const double* lR, const int* rowPtr, const int* colPtr,
+                      double* R, double* Val) {
+  for (int a = 0; a < 4; a++) {
+    int rowN = ptr[a];
+    for (int i = 0; i < 3; i++) R[3 * rowN + i] += lR[3 * a + i];
+    for (int b = 0; b < 4; b++) {
+      int colN = ptr[b];
+      int left = rowPtr[rowN], right = rowPtr[rowN + 1];
+      int k = (right + left) / 2;
+      while (colN != colPtr[k]) {
+        if (colN > colPtr[k]) left = k; else right = k;
+        k = (right + left) / 2;
+      }
+      for (int i = 0; i < 9; i++) Val[9 * (long)k + i] += lK[i + 9 * a + 36 * b];
+    }
+  }
+}
+
+int or_construct_struct(const or_struct_params* P, int nNo, int nEl, const int* ien, const double* x,
+                        const double* A, const double* Y, const double* D, const int* rowPtr,
+                        const int* colPtr, double* R, double* Val) {
+  (void)nNo;
+  double xl[12], al[12], yl[12], dl[12], lR[12], lK[144];
+  for (int e = 0; e < nEl; e++) {
+    const int* ptr = ien + 4 * e;
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) {
+        xl[3 * a + i] = x[3 * ptr[a] + i];
+        al[3 * a + i] = A[3 * ptr[a] + i];
+        yl[3 * a + i] = Y[3 * ptr[a] + i];
+        dl[3 * a + i] = D[3 * ptr[a] + i];
+      }
+    if (or_struct_element(P, 3, xl, al, yl, dl, lR, lK)) return -1 - e;
+    do_assem3(ptr, lK, lR, rowPtr, colPtr, R, Val);
+  }
+  return 0;
+}
+
+int or_construct_mesh(double E, double nu, double rho, double dt, double am, double af, double beta,
+                      int nNo, int nEl, const int* ien, const double* x, const double* A, const double* D,
+                      const double* Do, const int* rowPtr, const int* colPtr, double* R, double* Val) {
+  (void)nNo;
+  double xl[12], al[12], dl[12], lR[12], lK[144];
+  for (int e = 0; e < nEl; e++) {
+    const int* ptr = ien + 4 * e;
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) {
+        const int Ac = ptr[a];
+        xl[3 * a + i] = x[3 * Ac + i] + Do[7 * Ac + 4 + i];
+        al[3 * a + i] = A[7 * Ac + 4 + i];
+        dl[3 * a + i] = D[7 * Ac + 4 + i] - Do[7 * Ac + 4 + i];
+      }
+    if (or_mesh_element(E, nu, rho, dt, am, af, beta, xl, al, dl, lR, lK)) return -1 - e;
+    do_assem3(ptr, lK, lR, rowPtr, colPtr, R, Val);
+  }
+  return 0;
+}

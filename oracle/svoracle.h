@@ -56,6 +56,42 @@ void or_neu_backflow(const or_fluid_params* p, int nFa, const int* fien, const i
                      const int* ien, const double* x, const double* Yg, double h,
                      const int* rowPtr, const int* colPtr, double* R, double* Val);
 
+/* ---- solid and mesh-motion elements (Config 5 ingredients) ---- */
+typedef struct {
+  double rho, damping, fx, fy, fz;  /* solid_density, damping, body force */
+  double C10, Kpen;                 /* neo-Hookean C10, volumetric penalty */
+  int volType;                      /* 0 Quad, 1 ST91, 2 M94 (get_svol_p, mat_models.cpp:1626) */
+  double dt, am, af, gam, beta;
+} or_struct_params;
+
+/* second-order generalised-alpha constants (initialize.cpp:426-465) */
+void or_genalpha_second_order(double rho_inf, double* am, double* af, double* gam, double* beta);
+
+/* Element residual (dof,4) and tangent (dof*dof,4,4) of a neo-Hookean tet:
+ * construct_dsolid's body (sv_struct.cpp:213-362) with struct_3d_carray
+ * (sv_struct.cpp:552-846) and get_pk2cc<3> nHook (mat_models_carray.h:183-,370-)
+ * plus get_svol_p; no viscosity, no prestress, no fibres.  dof >= 3 (3: struct
+ * equation, 4: the FSI equation); xl (3,4), al/yl/dl (dof,4) with the displacement
+ * components first. */
+int or_struct_element(const or_struct_params* p, int dof, const double* xl, const double* al,
+                      const double* yl, const double* dl, double* lR, double* lK);
+
+/* Element residual and tangent of the linear-elastic mesh motion: construct_mesh
+ * (mesh.cpp:49-161, reference configuration x + Do, weights without the Jacobian,
+ * mesh.cpp:147) and l_elas_3d (l_elas.cpp:274-387).  E, nu, rho of the mesh equation;
+ * xl (3,4) = x + Do; al, dl (3,4) = mesh acceleration and displacement minus Do. */
+int or_mesh_element(double E, double nu, double rho, double dt, double am, double af, double beta,
+                    const double* xl, const double* al, const double* dl, double* lR, double* lK);
+
+/* Element loops + do_assem (dof 3) over all tets.  struct: A/Y/D (3,nNo); mesh:
+ * A/D/Do (7,nNo) state with the mesh equation at rows 4..6 (the FSI layout). */
+int or_construct_struct(const or_struct_params* p, int nNo, int nEl, const int* ien, const double* x,
+                        const double* A, const double* Y, const double* D, const int* rowPtr,
+                        const int* colPtr, double* R, double* Val);
+int or_construct_mesh(double E, double nu, double rho, double dt, double am, double af, double beta,
+                      int nNo, int nEl, const int* ien, const double* x, const double* A, const double* D,
+                      const double* Do, const int* rowPtr, const int* colPtr, double* R, double* Val);
+
 typedef struct {
   int sD, mItr;            /* Krylov dimension, restart cycles */
   double relTol, absTol;

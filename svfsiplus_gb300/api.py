@@ -58,6 +58,29 @@ class FluidProps(C.Structure):
                 ("gam", C.c_double), ("beta", C.c_double)]
 
 
+class SolidProps(C.Structure):
+    _fields_ = [("rho", C.c_double), ("damping", C.c_double), ("f", C.c_double * 3), ("C10", C.c_double),
+                ("Kpen", C.c_double), ("volType", C.c_int), ("dt", C.c_double), ("am", C.c_double),
+                ("af", C.c_double), ("gam", C.c_double), ("beta", C.c_double)]
+
+
+def genalpha_second_order(rho_inf: float):
+    """eq.am/af/gam/beta of a second-order equation (struct, mesh; initialize.cpp:426-465)."""
+    am = (2.0 - rho_inf) / (1.0 + rho_inf)
+    af = 1.0 / (1.0 + rho_inf)
+    beta = 0.25 * (1.0 + am - af) ** 2
+    gam = 0.5 + am - af
+    return am, af, gam, beta
+
+
+def solid_props(rho=1.2, E=1.0e6, nu=0.45, dt=1e-3, rho_inf=0.5, volType=1, damping=0.0):
+    """Neo-Hookean solid from E, nu: C10 = mu/2, Kpen = bulk modulus."""
+    am, af, gam, beta = genalpha_second_order(rho_inf)
+    C10 = E / (4.0 * (1.0 + nu))
+    Kpen = E / (3.0 * (1.0 - 2.0 * nu))
+    return SolidProps(rho, damping, (C.c_double * 3)(0.0, 0.0, 0.0), C10, Kpen, volType, dt, am, af, gam, beta)
+
+
 class NewtonOpts(C.Structure):
     _fields_ = [("minItr", C.c_int), ("maxItr", C.c_int), ("tol", C.c_double), ("precision", C.c_int),
                 ("outletFace", C.c_int), ("outletH", C.c_double)]
@@ -168,6 +191,16 @@ class Context:
         self._check(lib().svgpu_construct_fluid(self._h, C.byref(props), _ptr(Ag), _ptr(Yg), _ptr(Bf), _ptr(R),
                                                 _ptr(Val), int(precision)), "construct_fluid")
 
+    def construct_dsolid(self, props, dof, tDof, s, Ag, Yg, Dg, R, Val):
+        self._check(lib().svgpu_construct_dsolid(self._h, C.byref(props), int(dof), int(tDof), int(s), _ptr(Ag),
+                                                 _ptr(Yg), _ptr(Dg), _ptr(R), _ptr(Val)), "construct_dsolid")
+
+    def construct_mesh(self, E, nu, rho, dt, rho_inf, tDof, s, Ag, Dg, Do, R, Val):
+        am, af, gam, beta = genalpha_second_order(rho_inf)
+        self._check(lib().svgpu_construct_mesh(self._h, *(C.c_double(v) for v in (E, nu, rho, dt, am, af, beta)),
+                                               int(tDof), int(s), _ptr(Ag), _ptr(Dg), _ptr(Do), _ptr(R), _ptr(Val)),
+                    "construct_mesh")
+
     def get_system(self, R=None, Val=None):
         """Copy the resident R (nNo,4) and Val (nnz,16) out as FP64."""
         self._check(lib().svgpu_get_system(self._h, _ptr(R), _ptr(Val)), "get_system")
@@ -214,8 +247,10 @@ class Context:
         self._check(lib().svgpu_gnn_train(self._h, int(iters), C.c_float(lr), C.byref(loss)), "gnn_train")
         return loss.value
 
-    def set_learned(self, on=True):
-        self._check(lib().svgpu_set_learned(self._h, int(bool(on))), "set_learned")
+    def set_solver_mode(self, mode):
+        """0 plain GMRES + diagonal, 1 learned FGMRES, 2 multilevel FGMRES, 3 multilevel
+        with the learned smoother (modes 1-3 act on the mixed-precision path)."""
+        self._check(lib().svgpu_set_solver_mode(self._h, int(mode)), "set_solver_mode")
 
     @property
     def learned_rejects(self):

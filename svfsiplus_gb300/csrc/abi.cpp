@@ -4,9 +4,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <vector>
 
+#include "amg.h"
 #include "internal.h"
 
 namespace svgpu {
@@ -125,7 +127,7 @@ struct CycleGraph {
 // Graphs of one context: the sD Arnoldi iterations of a restart cycle, one per kind
 // (0: FP64, 1: mixed precision).
 struct CtxGraphs {
-  std::unique_ptr<CycleGraph> g[3];  // 0: FP64, 1: mixed, 2: mixed + learned (flexible)
+  std::unique_ptr<CycleGraph> g[5];  // 0: FP64, 1: mixed, 2..4: mixed flexible, by solver mode 1..3
 };
 std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
   static std::map<const svgpu_ctx*, CtxGraphs> g;
@@ -292,15 +294,17 @@ void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
 // Gram-Schmidt and Givens steps; the solution is updated from the z_i (FGMRES).
 void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
   KrylovWork& kw = ctx->kw;
-  GnnState& g = *ctx->gnn;
   const long n = (long)kw.n;
   const int sD = kw.sD;
   double* hraw = kw.givens.p + 4 * sD + 1;
   for (int i = 0; i < sD; i++) {
     float* ui = kw.V32.p + (long)i * n;
     float* ui1 = kw.V32.p + (long)(i + 1) * n;
-    float* zi = g.zbasis.p + (long)i * n;
-    gnn_apply_device(ctx, ui, nullptr, g.scal.p + 4, zi, nullptr, kw.flags.p);
+    float* zi = kw.zbasis.p + (long)i * n;
+    if (ctx->learned_mode == 1)
+      gnn_apply_device(ctx, ui, nullptr, ctx->gnn->scal.p + 4, zi, nullptr, kw.flags.p);
+    else
+      amg_vcycle(ctx, ui, zi);
     launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
                                        kw.flags.p);
@@ -327,7 +331,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     ctx->stream = ctx->capture_stream;
     cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
-      if (kind == 2)
+      if (kind >= 2)
         enqueue_cycle_flex(ctx, Val32);
       else
         enqueue_cycle32(ctx, Val32);
@@ -344,7 +348,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     g.dof = 4;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
-  ctx->launches += (kind == 2 ? 10LL : 5LL) * ctx->kw.sD;
+  ctx->launches += (kind >= 2 ? 12LL : 5LL) * ctx->kw.sD;
   return SVGPU_OK;
 }
 
@@ -393,7 +397,9 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   const long n = 4L * ctx->nNo;
   const int sD = kw.sD;
   int rc = SVGPU_OK;
-  bool learned = ctx->learned_mode != 0 && ctx->gnn != nullptr;
+  const int mode = ctx->learned_mode;
+  const bool use_gnn = (mode == 1 || mode == 3) && ctx->gnn != nullptr;
+  bool learned = mode != 0 && (use_gnn || mode == 2);  // flexible cycles
   if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
   st->suc = 0;
   double nrm = device_norm(ctx, n, Rs, rc);
@@ -412,9 +418,12 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  if (learned) {
+  if (learned && !use_gnn) {
+    if (!kw.zbasis.p || kw.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, kw.zbasis.resize((size_t)n * sD));
+  }
+  if (use_gnn) {
     GnnState& g = *ctx->gnn;
-    if (!g.zbasis.p || g.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, g.zbasis.resize((size_t)n * sD));
+    if (!kw.zbasis.p || kw.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, kw.zbasis.resize((size_t)n * sD));
     const double sv = 1.0 / std::sqrt((double)n);  // scale of a unit-norm basis vector
     SVGPU_CUDA(ctx, cudaMemcpyAsync(g.scal.p + 4, &sv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     // learned initial guess X0 = M(Rs), kept only if it lowers the FP64 residual
@@ -471,9 +480,9 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     launch_norm2(ctx->stream, n, kw.r64.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
     launch_start_vector32(ctx->stream, n, kw.r64.p, kw.scal.p + 2, kw.V32.p, kw.givens.p + 2 * sD, kw.flags.p);
     ctx->launches += 3;
-    if ((rc = run_cycle_kind(ctx, Val32, learned ? 2 : 1))) return rc;
+    if ((rc = run_cycle_kind(ctx, Val32, learned ? 1 + mode : 1))) return rc;
     launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
-    launch_xupdate32(ctx->stream, n, sD, learned ? ctx->gnn->zbasis.p : kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
+    launch_xupdate32(ctx->stream, n, sD, learned ? kw.zbasis.p : kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
     ctx->launches += 2;
     int flags[4];
     SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
@@ -517,6 +526,12 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   launch_scale_val32(ctx->stream, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, kw.Wc.p, Val32);
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches += 3;
+  if (ctx->learned_mode >= 2) {
+    if (!ctx->amg && (rc = amg_build(ctx))) return rc;
+    ctx->amg->gnn_smoother = ctx->learned_mode == 3 && ctx->gnn;
+    ctx->amg_val0 = Val32;
+    if ((rc = amg_numeric(ctx, Val32))) return rc;
+  }
   const bool collect = ctx->gnn && ctx->gnn->collect;
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   rc = gmres_mixed(ctx, Val32, R, R, st);
@@ -1024,6 +1039,85 @@ int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* prop
   if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
+}
+
+// Shared driver of the dof-3/4 solid and mesh assemblies into caller-owned R/Val.
+static int assemble_generic(svgpu_ctx* ctx, int dof, int tDof, const double* const* states, int nstates, double* R,
+                            double* Val, const std::function<void(const double* const*, double*, double*, int, int)>& launch) {
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "assembly before mesh_create");
+  if (!R || !Val) return set_err(ctx, SVGPU_EINVAL, "assembly: R and Val are required");
+  for (int k = 0; k < nstates; k++)
+    if (!states[k] || misaligned_device(states[k])) return set_err(ctx, SVGPU_EINVAL, "assembly: bad state array");
+  if (misaligned_device(R) || misaligned_device(Val)) return set_err(ctx, SVGPU_EINVAL, "assembly: unaligned R/Val");
+  const long nr = (long)dof * ctx->nNo;
+  const size_t nv = (size_t)ctx->nnz * dof * dof;
+  int rc;
+  std::vector<DevBuf<double>> st(nstates);
+  std::vector<const double*> sp(nstates);
+  for (int k = 0; k < nstates; k++) {
+    if (is_device_ptr(states[k])) {
+      sp[k] = states[k];
+    } else {
+      if ((rc = to_device(ctx, st[k], states[k], (size_t)tDof * ctx->nNo))) return rc;
+      sp[k] = st[k].p;
+    }
+  }
+  const bool dR = is_device_ptr(R), dV = is_device_ptr(Val);
+  double* Rd = R;
+  double* Vd = Val;
+  if (!dR) { if ((rc = to_device(ctx, ctx->stage1, (const double*)R, nr))) return rc; Rd = ctx->stage1.p; }
+  if (!dV) { if ((rc = to_device(ctx, ctx->stage2, (const double*)Val, nv))) return rc; Vd = ctx->stage2.p; }
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
+  MeshData& m = *ctx->mesh;
+  for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+    launch(sp.data(), Rd, Vd, m.color_start[k], m.color_start[k + 1] - m.color_start[k]);
+    ctx->launches++;
+  }
+  if ((rc = check_errflag(ctx))) return rc;
+  if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, nr * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_construct_dsolid(svgpu_ctx* ctx, const svgpu_solid_props* p, int dof, int tDof, int s, const double* Ag,
+                           const double* Yg, const double* Dg, double* R, double* Val) {
+  if (!ctx || !p) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if ((dof != 3 && dof != 4) || s < 0 || s + 3 > tDof) return set_err(ctx, SVGPU_EINVAL, "construct_dsolid: bad dof/rows");
+  SolidConsts c;
+  c.rho = p->rho;
+  c.damping = p->damping;
+  for (int i = 0; i < 3; i++) c.f[i] = p->f[i];
+  c.C10 = p->C10;
+  c.Kpen = p->Kpen;
+  c.volType = p->volType;
+  c.dt = p->dt;
+  c.am = p->am;
+  c.af = p->af;
+  c.gam = p->gam;
+  c.beta = p->beta;
+  const double* states[3] = {Ag, Yg, Dg};
+  MeshData& m = *ctx->mesh;
+  return assemble_generic(ctx, dof, tDof, states, 3, R, Val, [&](const double* const* sp, double* Rd, double* Vd, int e0, int ne) {
+    launch_struct_assembly(ctx->stream, dof, c, e0, ne, m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, tDof, s, sp[0], sp[1],
+                           sp[2], ctx->rowPtr.p, Rd, Vd, ctx->errflag.p);
+  });
+}
+
+int svgpu_construct_mesh(svgpu_ctx* ctx, double E, double nu, double rho, double dt, double am, double af,
+                         double beta, int tDof, int s, const double* Ag, const double* Dg, const double* Do, double* R,
+                         double* Val) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (s < 0 || s + 3 > tDof) return set_err(ctx, SVGPU_EINVAL, "construct_mesh: bad rows");
+  MeshConsts c{E, nu, rho, dt, am, af, beta};
+  const double* states[3] = {Ag, Dg, Do};
+  MeshData& m = *ctx->mesh;
+  return assemble_generic(ctx, 3, tDof, states, 3, R, Val, [&](const double* const* sp, double* Rd, double* Vd, int e0, int ne) {
+    launch_mesh_assembly(ctx->stream, c, e0, ne, m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, tDof, s, sp[0], sp[1], sp[2],
+                         ctx->rowPtr.p, Rd, Vd, ctx->errflag.p);
+  });
 }
 
 int svgpu_get_system(svgpu_ctx* ctx, double* R, double* Val) {

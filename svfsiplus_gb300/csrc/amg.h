@@ -1,0 +1,53 @@
+// Aggregation multilevel preconditioner (used by the mixed and learned paths): level
+// data on the device and the host set-up helpers (amg_setup.cpp).
+#pragma once
+#include <vector>
+
+#include "internal.h"
+
+namespace svgpu {
+
+struct AmgLevel {
+  int n = 0, nnz = 0;
+  DevBuf<int> rowPtr, colPtr;   // levels > 0 (level 0 is the system's own pattern)
+  DevBuf<float> val;            // levels > 0: 16 floats per block
+  DevBuf<float> dinv;           // inverse of every 4x4 diagonal block
+  DevBuf<int> diagPtr;          // levels > 0
+  // map to the next coarser level
+  DevBuf<int> agg;              // fine node -> coarse node
+  DevBuf<int> aggPtr, aggList;  // coarse node -> its fine nodes
+  DevBuf<int> sumPtr, sumIdx;   // coarse block -> the fine blocks summed into it
+  DevBuf<float> x, b, r;        // work vectors, 4 n floats
+};
+
+struct AmgState {
+  std::vector<AmgLevel> lv;
+  float omega = 0.7f;           // damping of the block-Jacobi smoother
+  int coarse_sweeps = 30;       // block-Jacobi sweeps on the coarsest level
+  bool gnn_smoother = false;    // pre-smooth on level 0 with the learned network
+};
+
+int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg);
+void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::vector<int>& colPtr,
+                    const std::vector<int>& agg, std::vector<int>& cRow, std::vector<int>& cCol,
+                    std::vector<int>& sumPtr, std::vector<int>& sumIdx);
+
+// k_amg.cu
+void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal, float* coarseVal);
+void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, float* dinv);
+void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
+                bool first);
+void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r);
+void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc);
+void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x);
+void amg_coarse_solve(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* dinv,
+                      const float* b, float* x, float* y, float omega, int sweeps);
+// amg.cpp
+struct svgpu_ctx_fwd;
+int amg_build(svgpu_ctx* ctx);
+int amg_numeric(svgpu_ctx* ctx, const float* Val0);
+// z = M b on level 0 (FP32 vectors of 4 nNo); enqueued on ctx->stream, capturable
+void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z);
+void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y);
+
+}  // namespace svgpu

@@ -1,0 +1,73 @@
+// Host set-up of the aggregation hierarchy used by the multilevel preconditioner:
+// greedy node aggregation of the block-CSR graph, the coarse block pattern of the
+// Galerkin operator P^T K P with piecewise-constant P (one 4x4 identity per fine node
+// in its aggregate), and the fine-block -> coarse-block lists the GPU sums.  The
+// reference has no multilevel preconditioner in FSILS (its AMG lives in the Trilinos
+// back-end, out of scope); this serves the learned/mixed paths only.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "amg.h"
+
+namespace svgpu {
+
+// Greedy aggregation (Vanek, Mandel & Brezina 1996, phases 1-3 without strength
+// filtering): root nodes whose neighbourhood is untouched form an aggregate with all
+// their neighbours; left-over nodes join a neighbouring aggregate; the rest stand alone.
+int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg) {
+  agg.assign(n, -1);
+  int na = 0;
+  for (int i = 0; i < n; i++) {
+    bool free_nbhd = true;
+    for (int k = rowPtr[i]; k < rowPtr[i + 1] && free_nbhd; k++) free_nbhd = agg[colPtr[k]] < 0;
+    if (!free_nbhd) continue;
+    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++) agg[colPtr[k]] = na;
+    na++;
+  }
+  std::vector<int> agg2 = agg;
+  for (int i = 0; i < n; i++) {
+    if (agg[i] >= 0) continue;
+    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++)
+      if (agg[colPtr[k]] >= 0) {
+        agg2[i] = agg[colPtr[k]];
+        break;
+      }
+  }
+  for (int i = 0; i < n; i++)
+    if (agg2[i] < 0) agg2[i] = na++;
+  agg.swap(agg2);
+  return na;
+}
+
+// Coarse pattern of P^T K P and, for every coarse block, the list of fine blocks that
+// sum into it (CSR: cPtr / fineIdx), in fixed order so the sums are deterministic.
+void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::vector<int>& colPtr,
+                    const std::vector<int>& agg, std::vector<int>& cRow, std::vector<int>& cCol,
+                    std::vector<int>& sumPtr, std::vector<int>& sumIdx) {
+  const long nnz = rowPtr[n];
+  std::vector<long long> key(nnz);
+  for (int i = 0; i < n; i++)
+    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++) key[k] = (long long)agg[i] * nc + agg[colPtr[k]];
+  std::vector<int> order(nnz);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  cRow.assign(nc + 1, 0);
+  cCol.clear();
+  sumPtr.clear();
+  sumIdx.assign(order.begin(), order.end());
+  long long last = -1;
+  for (long p = 0; p < nnz; p++) {
+    const long long kk = key[order[p]];
+    if (kk != last) {
+      cCol.push_back((int)(kk % nc));
+      sumPtr.push_back((int)p);
+      cRow[(int)(kk / nc) + 1]++;
+      last = kk;
+    }
+  }
+  sumPtr.push_back((int)nnz);
+  for (int c = 0; c < nc; c++) cRow[c + 1] += cRow[c];
+}
+
+}  // namespace svgpu

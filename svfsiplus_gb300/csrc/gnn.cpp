@@ -277,10 +277,12 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss) {
   return SVGPU_OK;
 }
 
-int svgpu_set_learned(svgpu_ctx* ctx, int on) {
+int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode) {
   if (!ctx) return SVGPU_EINVAL;
-  if (on && !ctx->gnn) return set_err(ctx, SVGPU_ESTATE, "set_learned: no network (svgpu_gnn_create)");
-  ctx->learned_mode = on ? 1 : 0;
+  if (mode < 0 || mode > 3) return set_err(ctx, SVGPU_EINVAL, "set_solver_mode: mode must be 0..3");
+  if ((mode == 1 || mode == 3) && !ctx->gnn)
+    return set_err(ctx, SVGPU_ESTATE, "set_solver_mode: the learned modes need a network (svgpu_gnn_create)");
+  ctx->learned_mode = mode;
   return SVGPU_OK;
 }
 

@@ -89,6 +89,7 @@ struct KrylovWork {
   size_t n = 0;
   DevBuf<double> V;        // (sD+1) basis vectors of length n
   DevBuf<float> V32;       // FP32 basis of the mixed-precision path
+  DevBuf<float> zbasis;    // flexible-GMRES directions Z (sD x n), FP32
   DevBuf<double> X, Wc, mask, tmp, r64, rbak, rsave;
   DevBuf<double> hess;     // (sD+1, sD) column-major, + c, s, err, y
   DevBuf<double> givens;   // c[sD], s[sD], err[sD+1], y[sD]
@@ -96,6 +97,8 @@ struct KrylovWork {
   DevBuf<double> scal;     // small scalars: eps, norms
   DevBuf<int> flags;       // [0] converged, [1] last_i, [2] breakdown
 };
+
+struct AmgState;
 
 // Learned preconditioner state (k_gnn.cu kernels).
 struct GnnState {
@@ -155,7 +158,13 @@ struct svgpu_ctx {
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
   std::unique_ptr<svgpu::GnnState> gnn;
-  int learned_mode = 0;  // 0: plain GMRES, 1: learned FGMRES (with rejection)
+  std::unique_ptr<struct svgpu::AmgState> amg;
+  const float* amg_val0 = nullptr;  // level-0 matrix of the current numeric set-up
+  // 0: GMRES + diagonal preconditioner (the reference's method)
+  // 1: FGMRES, right preconditioner = the learned network (+ learned initial guess)
+  // 2: FGMRES, right preconditioner = aggregation multilevel V-cycle (block Jacobi)
+  // 3: as 2 with the learned network as the finest-level pre-smoother (+ initial guess)
+  int learned_mode = 0;
   long long learned_rejects = 0;
   // host staging
   svgpu::DevBuf<double> stage1, stage2;
@@ -261,6 +270,21 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
                          const int* fien, const int* inner, const uint8_t* boff, const double* x4,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32);
+struct SolidConsts {
+  double rho, damping, f[3], C10, Kpen;
+  int volType;
+  double dt, am, af, gam, beta;
+};
+struct MeshConsts {
+  double E, nu, rho, dt, am, af, beta;
+};
+void launch_struct_assembly(cudaStream_t st, int dof, const SolidConsts& c, int e0, int ne, const int* ien,
+                            const uint8_t* boff, const int* elem_id, const double* x4, int tDof, int s,
+                            const double* Ag, const double* Yg, const double* Dg, const int* rowPtr, double* R,
+                            double* Val, int* errflag);
+void launch_mesh_assembly(cudaStream_t st, const MeshConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
+                          const int* elem_id, const double* x4, int tDof, int s, const double* Ag, const double* Dg,
+                          const double* Do, const int* rowPtr, double* R, double* Val, int* errflag);
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn);
 void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,

@@ -43,6 +43,50 @@ CASES = {
 }
 
 
+# Solid (neo-Hookean + ST91 penalty, E=1e6, nu=0.45, rho=1.2) and mesh-motion
+# (linear elastic, nu=0.3) assembly on the small pipe with seeded random state.
+SOLID = dict(rho=1.2, E=1.0e6, nu=0.45, dt=1e-3, rho_inf=0.5)
+SOLID["C10"] = SOLID["E"] / (4.0 * (1.0 + SOLID["nu"]))            # mu / 2
+SOLID["Kpen"] = SOLID["E"] / (3.0 * (1.0 - 2.0 * SOLID["nu"]))     # bulk modulus
+MESHMOTION = dict(rho=0.5, E=1.0, nu=0.3, dt=1e-3, rho_inf=0.5)
+
+
+def run_assembly(name, physics):
+    mesh = named_pipe("small")
+    rng = np.random.default_rng(17)
+    nNo = mesh.nNo
+    tDof = 3 if physics == "struct" else 7
+    params = dict(SOLID if physics == "struct" else MESHMOTION)
+    params["mode"] = "assemble_" + physics
+    scale = 0.01 if physics == "struct" else 0.02
+    A = rng.standard_normal((nNo, tDof))
+    Y = rng.standard_normal((nNo, tDof))
+    D = scale * rng.standard_normal((nNo, tDof))
+    tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        cdir, odir = os.path.join(tmp, "case"), os.path.join(tmp, "out")
+        write_case(mesh, cdir, params)
+        A.tofile(os.path.join(cdir, "A.bin"))
+        Y.tofile(os.path.join(cdir, "Y.bin"))
+        D.tofile(os.path.join(cdir, "D.bin"))
+        out = {"params": np.array(repr(params)), "A": A, "Y": Y, "D": D}
+        if physics == "mesh":
+            Do = scale * rng.standard_normal((nNo, tDof))
+            Do.tofile(os.path.join(cdir, "Do.bin"))
+            out["Do"] = Do
+        os.makedirs(odir)
+        subprocess.run([HARNESS, cdir, odir], check=True)
+        rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
+        out["rowPtr"] = rd("rowPtr.bin", np.int32)
+        out["colPtr"] = rd("colPtr.bin", np.int32)
+        out["R_asm"] = rd("R_asm.bin", np.float64).reshape(nNo, 3)
+        out["Val_asm"] = rd("Val_asm.bin", np.float64).reshape(-1, 9)
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+        print(name, "nNo", nNo, "|R|", np.linalg.norm(out["R_asm"]), "|Val|", np.linalg.norm(out["Val_asm"]))
+    finally:
+        shutil.rmtree(tmp)
+
+
 def write_case(mesh, d, params):
     os.makedirs(d, exist_ok=True)
     mesh.x.astype(np.float64).tofile(os.path.join(d, "x.bin"))
@@ -103,5 +147,10 @@ def run_case(name):
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES)):
-        run_case(n)
+    for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small"]):
+        if n == "struct_small":
+            run_assembly(n, "struct")
+        elif n == "mesh_small":
+            run_assembly(n, "mesh")
+        else:
+            run_case(n)
