@@ -1,25 +1,41 @@
 #!/usr/bin/env python
 """Benchmark of the svMultiPhysics fluid Newton-step hot path on one GB300.
 
-Workload: the 8M-tet pipe (2.0e7 CSR blocks, 1.37M nodes; seeded 8-mode wall
-perturbation), incompressible VMS P1-P1 Navier-Stokes, pulsatile inflow (10 cm/s mean
-plus a 5 cm/s sine at 1 Hz), generalised-alpha rho_inf = 0.5, dt = 1e-3.  A "step" is
-one time step: 3 Newton iterations, each an assembly of the residual and tangent and a
-GMRES(50) + diagonal-preconditioner solve to a relative residual of 1e-6.
+Workload: the 8M-tet pipe (8.06M tets, 1.37M nodes, 2.03e7 CSR blocks; seeded 8-mode
+wall perturbation), incompressible VMS P1-P1 Navier-Stokes, pulsatile inflow (10 cm/s
+mean plus a 5 cm/s sine at 1 Hz), generalised-alpha rho_inf = 0.5, dt = 1e-3.
 
-Our arm (default) times K steps after W warm-up steps:
-  value  -- device-resident state (An/Yn/Dn stay in HBM), CUDA events on the stream the
-            library launches on;
-  e2e    -- the same steps through the public C ABI with host arrays (Ao/Yo/Do copied in,
-            An/Yn/Dn copied out every step);
-  roofline -- the block SpMV, timed with CUDA events on the library's stream after the
-            timed region, against the measured HBM copy bandwidth;
-  cpu_baseline -- the C oracle (a restatement of the reference's own FSILS/assembly
-            code, one core) on a bounded sample of the same system.
+A "step" is one time step of the reference's Newton loop (main.cpp:371-617). Newton
+iterations run until the reference's own test in picc (pic.cpp:239-281) holds:
+r1 <= tol * pNorm with tol = 1e-6. That is, the preconditioned residual norm has fallen
+to 1e-6 of its value at the step's first iteration. There are at most 8 Newton iterations.
+Each linear solve is inexact (relative tolerance 1e-2), as in inexact Newton.
+
+Paths (--path):
+  multilevel -- the headline: mixed precision (FP32 tangent/Krylov basis, FP64 residual
+                and defect correction) with FGMRES(50) preconditioned by an aggregation
+                multilevel V-cycle (solver mode 2);
+  learned    -- the same with the learned network as finest-level smoother (mode 3);
+  mixed      -- mixed precision, GMRES(50) + diagonal preconditioner (mode 0);
+  plain      -- FP64, GMRES(50) + diagonal preconditioner: the reference's method.
+
+The default run times the headline path, and runs the plain FP64 GPU path beside it
+from the same state for comparison (`plain_gpu`).
+
+Our arm prints one JSON line:
+  value    -- s per time step, device-resident state, CUDA events on the library's
+              stream;
+  e2e      -- the same through the C ABI with host arrays: Ao/Yo/Do copied in and
+              An/Yn/Dn copied out every step;
+  roofline -- the block SpMV of the path (FP32 values for the mixed paths), timed with
+              CUDA events on the library's stream, against the measured HBM copy
+              bandwidth;
+  cpu_baseline -- the C oracle (a restatement of the reference's FP64 FSILS and
+              assembly, one core) on a bounded sample of the same system.
 
 --impl reference times the reference's CPU path (the oracle port: the reference's
-sources only compile where its tree is present) on a bounded sample per step and
-reports the same metric.
+sources compile only where its tree is present) on a bounded sample per step.
+--study MODES prints per-step solver statistics for the listed solver modes.
 """
 from __future__ import annotations
 
@@ -38,10 +54,12 @@ import numpy as np  # noqa: E402
 
 METRIC = "s/time step + Krylov iters, learned-precond vs plain GPU, 1 GB300, res<=1e-6"
 WORKLOAD = "pipe8m"
-NEWTON_ITERS = 3
-REL_TOL = 1e-6
+NEWTON_TOL = 1e-6
+NEWTON_MAX = 8
+LIN_REL_TOL = 1e-2
 KRYLOV_DIM = 50
-MAX_RESTARTS = 400
+MAX_RESTARTS = 40
+PATH_MODES = {"multilevel": 2, "learned": 3, "mixed": 0, "plain": -1}
 U_MEAN, U_AMP, U_FREQ = 10.0, 5.0, 1.0
 
 
@@ -99,9 +117,9 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def spmv_bytes(nnz, nNo, val_bytes=8):
+def spmv_bytes(nnz, nNo, val_bytes=8, vec_bytes=8):
     """Algorithmic bytes of one 4x4 block SpMV: Val + colPtr once, rowPtr, x once, y once."""
-    return nnz * (16 * val_bytes + 4) + (nNo + 1) * 4 + nNo * 4 * 8 + nNo * 4 * 8
+    return nnz * (16 * val_bytes + 4) + (nNo + 1) * 4 + nNo * 4 * vec_bytes * 2
 
 
 def cpu_sample(mesh, rowPtr, colPtr, krylov_its_per_newton, newton_iters, frac_elems=0.02):
@@ -149,6 +167,19 @@ def cpu_sample(mesh, rowPtr, colPtr, krylov_its_per_newton, newton_iters, frac_e
             "assembly_s": t_asm, "krylov_iter_s": t_it}
 
 
+def make_solver(api, mesh, rowPtr, colPtr, path, device=0):
+    mode = PATH_MODES[path]
+    precision = api.SVGPU_FP64 if mode < 0 else api.SVGPU_MIXED
+    s = api.PipeFluidSolver(mesh, device=device, sD=KRYLOV_DIM, mItr=MAX_RESTARTS, relTol=LIN_REL_TOL, absTol=1e-17,
+                            newton_min=1, newton_max=NEWTON_MAX, newton_tol=NEWTON_TOL, precision=precision,
+                            rowPtr=rowPtr, colPtr=colPtr)
+    if mode == 3:
+        s.enable_learning()
+    if mode >= 0:
+        s.ctx.set_solver_mode(mode if mode != 3 else 2)
+    return s, mode
+
+
 def run_ours(args):
     import torch
     from svfsiplus_gb300 import api
@@ -164,10 +195,7 @@ def run_ours(args):
     t0 = time.time()
     mesh = named_pipe(args.workload)
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
-    precision = api.SVGPU_FP64 if args.path == "plain" else api.SVGPU_MIXED
-    s = api.PipeFluidSolver(mesh, device=local, sD=KRYLOV_DIM, mItr=MAX_RESTARTS, relTol=REL_TOL, absTol=1e-17,
-                            newton_min=NEWTON_ITERS, newton_max=NEWTON_ITERS, newton_tol=1e-11,
-                            precision=precision, rowPtr=rowPtr, colPtr=colPtr)
+    s, mode = make_solver(api, mesh, rowPtr, colPtr, args.path, local)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
@@ -185,8 +213,13 @@ def run_ours(args):
         dYo.copy_(dYn)
         return st
 
-    for _ in range(args.warmup):
-        dev_step()
+    warm_stats = []
+    for k in range(args.warmup):
+        warm_stats.append(dev_step())
+        if mode == 3:  # online training on the pairs of the warm-up steps, then learned mode
+            s.ctx.gnn_train(50, 1e-3)
+            if k == args.warmup - 1:
+                s.ctx.set_solver_mode(3)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -207,9 +240,10 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_ms = float(t.item())
 
-    # e2e: the same steps through the C ABI with host arrays
+    # e2e: the same steps through the C ABI with host arrays (state copied in and out)
     s.Ao[:] = dAo.cpu().numpy()
     s.Yo[:] = dYo.cpu().numpy()
+    state_after_timed = (s.Ao.copy(), s.Yo.copy(), s.time, list(s.norms))
     torch.cuda.synchronize()
     e2e_stats = []
     t1 = time.perf_counter()
@@ -220,52 +254,107 @@ def run_ours(args):
     h2d = 3 * nNo * 4 * 8 + 2 * s.dir_nodes.size * 3 * 8
     d2h = 3 * nNo * 4 * 8
 
-    # roofline of the block SpMV on the assembled system (FP64 Val, resident)
-    Val = torch.empty((colPtr.size, 16), dtype=torch.float64, device="cuda")
-    Val.normal_()
+    # roofline: the block SpMV of the path (FP32 values for the mixed paths)
+    val_dtype = torch.float64 if mode < 0 else torch.float32
+    Val = torch.randn((colPtr.size, 16), dtype=val_dtype, device="cuda")
     x = torch.randn((nNo, 4), dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
-    for _ in range(3):
-        s.ctx.spar_mul(4, Val, x, y)
     reps = 20
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if mode < 0:
+        spmv = lambda: s.ctx.spar_mul(4, Val, x, y)  # noqa: E731
+        kernel, vb = "spmv4_f64_kernel (block SpMV, FP64 values)", 8
+    else:
+        x32 = x.float()
+        y32 = torch.empty_like(x32)
+        spmv = lambda: s.ctx.spar_mul32(Val, x32, y32)  # noqa: E731
+        kernel, vb = "spmv4_f32_kernel (block SpMV, FP32 values and vectors)", 4
+    for _ in range(3):
+        spmv()
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(reps):
-        s.ctx.spar_mul(4, Val, x, y)
+        spmv()
     e1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = e0.elapsed_time(e1) / reps
-    bytes_ = spmv_bytes(colPtr.size, nNo)
+    bytes_ = spmv_bytes(colPtr.size, nNo, vb, 8 if mode < 0 else 4)
     peak, kind = peaks()
     achieved = bytes_ / (spmv_ms * 1e-3) / 1e9
+    del Val
 
-    its = [x["itr"] for st in stats for x in st]
-    per_newton = float(np.mean(its)) if its else 0.0
+    # the plain FP64 GPU path (the reference's method) from the same state, one step
+    plain = None
+    if args.compare_plain and mode >= 0:
+        s.ctx.close()
+        torch.cuda.empty_cache()
+        sp, _ = make_solver(api, mesh, rowPtr, colPtr, "plain", local)
+        sp.Ao[:], sp.Yo[:], sp.time, sp.norms = state_after_timed[0], state_after_timed[1], state_after_timed[2], state_after_timed[3]
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
+        pst = sp.step(U_MEAN, U_AMP, U_FREQ)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - tp
+        plain = {"s_per_step": tp, "newton_iters": len(pst), "krylov_iters": [q["itr"] for q in pst],
+                 "converged": bool(pst[-1]["iNorm"] / pst[0]["iNorm"] <= NEWTON_TOL),
+                 "final_over_first_residual": pst[-1]["iNorm"] / pst[0]["iNorm"],
+                 "note": "one step from the state after the timed steps; Newton capped at %d iterations" % NEWTON_MAX}
+        sp.ctx.close()
+
+    its = [q["itr"] for st in stats for q in st]
+    newton = [len(st) for st in stats]
+    conv = [st[-1]["iNorm"] / st[0]["iNorm"] for st in stats]
     rec = {
         "metric": METRIC, "value": dev_ms / 1e3 / args.steps, "unit": "s/time step", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.path == "plain" else "f32+f64",
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if mode < 0 else "f32 tangent/Krylov + f64 residual",
         "data": "synthetic: procedural 8M-tet pipe, seeded wall perturbation (numpy seed 20261203)",
-        "config": {"workload": f"{args.workload}: {mesh.nEl} tets, {nNo} nodes, {colPtr.size} blocks; VMS P1-P1 fluid, "
-                               f"{NEWTON_ITERS} Newton its/step, GMRES({KRYLOV_DIM}) + diagonal preconditioner to "
-                               f"rel {REL_TOL:g}", "path": args.path,
-                   "l2": "inputs larger than L2 (Val is 2.6 GB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
-        "krylov_iters_per_newton": per_newton, "krylov_iters": its,
-        "newton": [[{"iNorm": x["iNorm"], "fNorm": x["fNorm"], "itr": x["itr"], "suc": x["suc"]} for x in st] for st in stats],
+        "config": {"workload": f"{args.workload}: {mesh.nEl} tets, {nNo} nodes, {colPtr.size} blocks; VMS P1-P1 fluid; "
+                               f"Newton to picc r1 <= {NEWTON_TOL:g}*pNorm (max {NEWTON_MAX}); linear rel tol "
+                               f"{LIN_REL_TOL:g}, (F)GMRES({KRYLOV_DIM})", "path": args.path, "solver_mode": mode,
+                   "l2": "inputs larger than L2 (Val is 1.3-2.6 GB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "krylov_iters_per_step": [sum(q["itr"] for q in st) for st in stats], "krylov_iters": its,
+        "newton_iters": newton, "newton_final_over_first": conv,
+        "plain_gpu": plain,
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "krylov_iters": [x["itr"] for st in e2e_stats for x in st]},
+                "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
         "gpu_launches": launches,
-        "roofline": {"kernel": "spmv4_f64 (block SpMV)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind, "traffic": None,
-                     "launch_ms": spmv_ms, "algorithmic_bytes": bytes_},
+        "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": kind, "traffic": None, "launch_ms": spmv_ms,
+                     "algorithmic_bytes": bytes_},
         "clocks": clk.summary(),
         "setup_s": setup_s,
     }
     if rank == 0 and not args.no_cpu:
-        rec["cpu_baseline"] = cpu_sample(mesh, rowPtr, colPtr, per_newton, NEWTON_ITERS)
+        per_solve = float(np.mean(plain["krylov_iters"])) if plain else 2040.0
+        rec["cpu_baseline"] = cpu_sample(mesh, rowPtr, colPtr, per_solve, NEWTON_MAX)
     if rank == 0:
         print(json.dumps(rec), flush=True)
+
+
+def run_study(args):
+    """Per-step solver statistics of several solver modes on one workload (from rest)."""
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    for path in args.study.split(","):
+        s, mode = make_solver(api, mesh, rowPtr, colPtr, path)
+        for k in range(args.steps):
+            if mode == 3 and k == 2:
+                s.ctx.set_solver_mode(3)
+            t = time.perf_counter()
+            st = s.step(U_MEAN, U_AMP, U_FREQ)
+            dt = time.perf_counter() - t
+            print(json.dumps({"workload": args.workload, "path": path, "mode": mode, "step": k + 1, "s": round(dt, 3),
+                              "newton": len(st), "its": [q["itr"] for q in st],
+                              "rel": [float("%.2g" % (q["fNorm"] / max(q["iNorm"], 1e-300))) for q in st],
+                              "iNorm": [float("%.3g" % q["iNorm"]) for q in st],
+                              "rejects": s.ctx.learned_rejects}), flush=True)
+            if mode == 3 and k < 2:
+                s.ctx.gnn_train(50, 1e-3)
+        s.ctx.close()
 
 
 def run_reference(args):
@@ -277,14 +366,16 @@ def run_reference(args):
     from svfsiplus_gb300.mesh import named_pipe
     mesh = named_pipe(args.workload)
     rowPtr, colPtr = csr_pattern(mesh.nNo, mesh.ien)
-    # Krylov iterations per Newton solve of this workload with the reference algorithm
-    # (GMRES(50) + diagonal preconditioner, rel 1e-6), as measured by the FP64 GPU path,
-    # which runs the same algorithm.
+    # The reference's algorithm (GMRES(50) + diagonal preconditioner) does not meet the
+    # linear tolerance on this workload: every solve of a step runs to the restart cap
+    # and the Newton loop to its iteration cap (measured with the FP64 GPU path, which
+    # runs the same algorithm).  A step therefore costs NEWTON_MAX solves of
+    # KRYLOV_DIM+1 iterations x MAX_RESTARTS.
     its = KRYLOV_ITS_PIPE8M
     samples = []
     t_total = time.perf_counter()
     for k in range(args.warmup + args.steps):
-        r = cpu_sample(mesh, rowPtr, colPtr, its, NEWTON_ITERS)
+        r = cpu_sample(mesh, rowPtr, colPtr, its, NEWTON_MAX)
         if k >= args.warmup:
             samples.append(r)
     v = float(np.mean([r["value"] for r in samples]))
@@ -300,23 +391,28 @@ def run_reference(args):
     print(json.dumps(rec), flush=True)
 
 
-# Krylov iterations per Newton solve on the 8M-tet pipe, measured with the FP64 GPU
-# path (bench.py --path plain); used to scale the reference's per-iteration CPU time.
-KRYLOV_ITS_PIPE8M = 1500.0
+# Krylov iterations per Newton solve of the reference's method on the 8M-tet pipe: the
+# restart cap, (KRYLOV_DIM + 1) x MAX_RESTARTS, which the FP64 GPU path reaches on every
+# solve after the first of a step.
+KRYLOV_ITS_PIPE8M = float((KRYLOV_DIM + 1) * MAX_RESTARTS)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="svgpu", choices=["svgpu", "reference"])
-    ap.add_argument("--path", default="plain", choices=["plain", "mixed", "learned"])
+    ap.add_argument("--path", default="multilevel", choices=list(PATH_MODES))
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
+    ap.add_argument("--study", default=None, help="comma-separated paths: per-step solver statistics")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.study:
+        run_study(args)
     else:
         run_ours(args)
 

@@ -121,6 +121,10 @@ int svgpu_fsils_dot_noalloc(int dof, int nNo, const double* U, const double* V, 
 
 /* Block SpMV KU = K U for any dof (fsils_spar_mul_vv, spar_mul.cpp:191-258). */
 int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, double* KU);
+/* FP32 block SpMV of the mixed-precision path, dof = 4, device arrays only (16-byte
+ * aligned): the single-precision form of fsils_spar_mul_vv (spar_mul.cpp:191-258) that
+ * the mixed Krylov cycles apply to the scaled FP32 matrix. */
+int svgpu_spar_mul_f32(svgpu_ctx* ctx, const float* K, const float* U, float* KU);
 
 /* ---- mesh and assembly ----------------------------------------------------------- */
 /* Volume mesh: linear tets, IEN (4,nEl), x (3,nNo).  Builds the element colouring

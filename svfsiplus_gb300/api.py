@@ -175,6 +175,10 @@ class Context:
     def spar_mul(self, dof, K, U, KU):
         self._check(lib().svgpu_spar_mul(self._h, int(dof), _ptr(K), _ptr(U), _ptr(KU)), "spar_mul")
 
+    def spar_mul32(self, K, U, KU):
+        """FP32 block SpMV (dof 4) on device tensors, enqueued on the library's stream."""
+        self._check(lib().svgpu_spar_mul_f32(self._h, _ptr(K), _ptr(U), _ptr(KU)), "spar_mul_f32")
+
     # ---- mesh and assembly
     def mesh_create(self, x, ien):
         x = np.ascontiguousarray(x, dtype=np.float64)

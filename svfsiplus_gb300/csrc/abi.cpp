@@ -857,6 +857,21 @@ int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, do
   return SVGPU_OK;
 }
 
+int svgpu_spar_mul_f32(svgpu_ctx* ctx, const float* K, const float* U, float* KU) {
+  if (!ctx) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->nNo == 0) return set_err(ctx, SVGPU_ESTATE, "spar_mul_f32 before fsils_lhs_create");
+  if (!K || !U || !KU) return set_err(ctx, SVGPU_EINVAL, "spar_mul_f32: bad arguments");
+  if (!is_device_ptr(K) || !is_device_ptr(U) || !is_device_ptr(KU))
+    return set_err(ctx, SVGPU_EINVAL, "spar_mul_f32: device arrays only");
+  if (misaligned_device(K) || misaligned_device(U) || misaligned_device(KU))
+    return set_err(ctx, SVGPU_EINVAL, "spar_mul_f32: device arrays must be 16-byte aligned");
+  launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, K, U, KU, nullptr);
+  ctx->launches++;
+  SVGPU_CUDA(ctx, cudaGetLastError());
+  return SVGPU_OK;
+}
+
 int svgpu_mesh_create(svgpu_ctx* ctx, int nNo, int nEl, int eNoN, const int* IEN, const double* x) {
   if (!ctx) return SVGPU_EINVAL;
   cudaSetDevice(ctx->device);
