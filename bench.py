@@ -167,6 +167,92 @@ def cpu_sample(mesh, rowPtr, colPtr, krylov_its_per_newton, newton_iters, frac_e
             "assembly_s": t_asm, "krylov_iter_s": t_it}
 
 
+def spmv_roofline(ctx, colPtr, nNo, mode, stream, reps=20):
+    """Average duration of the path's block SpMV over `reps` launches on the library's
+    stream (CUDA events), against the measured HBM copy bandwidth."""
+    import torch
+    val_dtype = torch.float64 if mode < 0 else torch.float32
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    Val = torch.randn((colPtr.size, 16), dtype=val_dtype, device="cuda", generator=gen)
+    x = torch.randn((nNo, 4), dtype=val_dtype, device="cuda", generator=gen)
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    if mode < 0:
+        spmv = lambda: ctx.spar_mul(4, Val, x, y)  # noqa: E731
+        kernel = "spmv4_f64_kernel (block SpMV, FP64 values and vectors)"
+    else:
+        spmv = lambda: ctx.spar_mul32(Val, x, y)  # noqa: E731
+        kernel = "spmv4_f32_kernel (block SpMV, FP32 values and vectors)"
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        spmv()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        spmv()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    vb = 8 if mode < 0 else 4
+    bytes_ = spmv_bytes(colPtr.size, nNo, vb, vb)
+    peak, kind = peaks()
+    achieved = bytes_ / (ms * 1e-3) / 1e9
+    return {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": kind, "traffic": None, "launch_ms": ms,
+            "algorithmic_bytes": bytes_, "launches_timed": reps}
+
+
+def kernel_breakdown(step_fn, path):
+    """Per-kernel device time of one more time step, from the CUDA activity trace of
+    torch.profiler (CUPTI; kernels inside CUDA graphs are recorded one by one, no
+    replay).  Written to `path` as JSON; the ten largest are returned."""
+    import tempfile
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        step_fn()
+        torch.cuda.synchronize()
+    with tempfile.TemporaryDirectory() as d:
+        fn = os.path.join(d, "trace.json")
+        prof.export_chrome_trace(fn)
+        with open(fn) as f:
+            trace = json.load(f)
+    agg = {}
+    for e in trace.get("traceEvents", []):
+        if e.get("cat") == "kernel" and "dur" in e:
+            r = agg.setdefault(e.get("name", "?"), [0, 0.0])
+            r[0] += 1
+            r[1] += float(e["dur"]) / 1e3
+    rows = [{"kernel": k, "launches": v[0], "total_ms": v[1]} for k, v in agg.items()]
+    rows.sort(key=lambda r: -r["total_ms"])
+    tot = sum(r["total_ms"] for r in rows)
+    for r in rows:
+        r["share"] = r["total_ms"] / tot if tot else 0.0
+        r["avg_us"] = 1e3 * r["total_ms"] / r["launches"]
+    with open(path, "w") as f:
+        json.dump({"total_ms": tot, "kernels": rows}, f, indent=1)
+    return {"total_device_ms": tot, "launches": sum(r["launches"] for r in rows),
+            "top": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows[:10]]}
+
+
+def run_spmv_only(args):
+    """Only the SpMV roofline measurement of a path on a workload (a small, graph-free
+    program for kernel profilers)."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(mesh.nNo, rowPtr, colPtr, 0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    api.lib().svgpu_set_stream(ctx._h, api.C.c_void_p(stream.cuda_stream))
+    roof = spmv_roofline(ctx, colPtr, mesh.nNo, PATH_MODES[args.path], stream, reps=args.steps)
+    print(json.dumps({"workload": args.workload, "path": args.path, "roofline": roof}), flush=True)
+
+
 def make_solver(api, mesh, rowPtr, colPtr, path, device=0):
     mode = PATH_MODES[path]
     precision = api.SVGPU_FP64 if mode < 0 else api.SVGPU_MIXED
@@ -254,34 +340,10 @@ def run_ours(args):
     h2d = 3 * nNo * 4 * 8 + 2 * s.dir_nodes.size * 3 * 8
     d2h = 3 * nNo * 4 * 8
 
-    # roofline: the block SpMV of the path (FP32 values for the mixed paths)
-    val_dtype = torch.float64 if mode < 0 else torch.float32
-    Val = torch.randn((colPtr.size, 16), dtype=val_dtype, device="cuda")
-    x = torch.randn((nNo, 4), dtype=torch.float64, device="cuda")
-    y = torch.empty_like(x)
-    reps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if mode < 0:
-        spmv = lambda: s.ctx.spar_mul(4, Val, x, y)  # noqa: E731
-        kernel, vb = "spmv4_f64_kernel (block SpMV, FP64 values)", 8
-    else:
-        x32 = x.float()
-        y32 = torch.empty_like(x32)
-        spmv = lambda: s.ctx.spar_mul32(Val, x32, y32)  # noqa: E731
-        kernel, vb = "spmv4_f32_kernel (block SpMV, FP32 values and vectors)", 4
-    for _ in range(3):
-        spmv()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(reps):
-        spmv()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    spmv_ms = e0.elapsed_time(e1) / reps
-    bytes_ = spmv_bytes(colPtr.size, nNo, vb, 8 if mode < 0 else 4)
-    peak, kind = peaks()
-    achieved = bytes_ / (spmv_ms * 1e-3) / 1e9
-    del Val
+    roof = spmv_roofline(s.ctx, colPtr, nNo, mode, stream)
+    breakdown = None
+    if args.breakdown:
+        breakdown = kernel_breakdown(dev_step, args.breakdown)
 
     # the plain FP64 GPU path (the reference's method) from the same state, one step
     plain = None
@@ -320,12 +382,12 @@ def run_ours(args):
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
         "gpu_launches": launches,
-        "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": kind, "traffic": None, "launch_ms": spmv_ms,
-                     "algorithmic_bytes": bytes_},
+        "roofline": roof,
         "clocks": clk.summary(),
         "setup_s": setup_s,
     }
+    if breakdown:
+        rec["kernel_breakdown"] = breakdown
     if rank == 0 and not args.no_cpu:
         per_solve = float(np.mean(plain["krylov_iters"])) if plain else 2040.0
         rec["cpu_baseline"] = cpu_sample(mesh, rowPtr, colPtr, per_solve, NEWTON_MAX)
@@ -408,9 +470,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     ap.add_argument("--study", default=None, help="comma-separated paths: per-step solver statistics")
+    ap.add_argument("--spmv-only", action="store_true", help="only the SpMV roofline measurement")
+    ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.spmv_only:
+        run_spmv_only(args)
     elif args.study:
         run_study(args)
     else:

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <numeric>
@@ -119,6 +120,7 @@ struct CycleGraph {
   const void* val = nullptr;
   long n = 0;
   int sD = 0, dof = 0;
+  long long kernels = 0;  // kernel nodes in the graph (launches counted per graph launch)
   ~CycleGraph() {
     if (exec) cudaGraphExecDestroy(exec);
   }
@@ -162,6 +164,11 @@ void enqueue_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
 }
 
 int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
+  if (!ctx->use_graphs) {
+    enqueue_cycle(ctx, dof, Val);
+    SVGPU_CUDA(ctx, cudaGetLastError());
+    return SVGPU_OK;
+  }
   auto& slot = graphs()[ctx].g[0];
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
@@ -183,6 +190,7 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
       ce = cudaStreamEndCapture(ctx->stream, &graph);
     }
     ctx->stream = user;
+    g.kernels = ctx->launches - before;
     ctx->launches = before;
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
@@ -193,7 +201,7 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
     g.dof = dof;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
-  ctx->launches += 5LL * ctx->kw.sD;
+  ctx->launches += g.kernels;
   return SVGPU_OK;
 }
 
@@ -304,7 +312,7 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
     if (ctx->learned_mode == 1)
       gnn_apply_device(ctx, ui, nullptr, ctx->gnn->scal.p + 4, zi, nullptr, kw.flags.p);
     else
-      amg_vcycle(ctx, ui, zi);
+      amg_vcycle(ctx, ui, zi, kw.flags.p);
     launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
                                        kw.flags.p);
@@ -316,6 +324,14 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
 }
 
 int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
+  if (!ctx->use_graphs) {
+    if (kind >= 2)
+      enqueue_cycle_flex(ctx, Val32);
+    else
+      enqueue_cycle32(ctx, Val32);
+    SVGPU_CUDA(ctx, cudaGetLastError());
+    return SVGPU_OK;
+  }
   auto& slot = graphs()[ctx].g[kind];
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
@@ -338,6 +354,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
       ce = cudaStreamEndCapture(ctx->stream, &graph);
     }
     ctx->stream = user;
+    g.kernels = ctx->launches - before;
     ctx->launches = before;
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
@@ -348,11 +365,16 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     g.dof = 4;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
-  ctx->launches += (kind >= 2 ? 12LL : 5LL) * ctx->kw.sD;
+  ctx->launches += g.kernels;
   return SVGPU_OK;
 }
 
 int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
+  if (!ctx->use_graphs) {
+    enqueue_cycle32(ctx, Val32);
+    SVGPU_CUDA(ctx, cudaGetLastError());
+    return SVGPU_OK;
+  }
   auto& slot = graphs()[ctx].g[1];
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
@@ -374,6 +396,7 @@ int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
       ce = cudaStreamEndCapture(ctx->stream, &graph);
     }
     ctx->stream = user;
+    g.kernels = ctx->launches - before;
     ctx->launches = before;
     if (ce != cudaSuccess) return cuda_fail(ctx, ce, "restart-cycle graph capture");
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
@@ -384,7 +407,7 @@ int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
     g.dof = 4;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
-  ctx->launches += 5LL * ctx->kw.sD;
+  ctx->launches += g.kernels;
   return SVGPU_OK;
 }
 
@@ -667,6 +690,7 @@ int svgpu_create(svgpu_ctx** out, int device) {
     return SVGPU_ECUDA;
   }
   cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (const char* g = std::getenv("SVGPU_GRAPHS")) ctx->use_graphs = std::strcmp(g, "0") != 0;
   if (ctx->errflag.resize(2) != cudaSuccess) {
     delete ctx;
     return SVGPU_ECUDA;

@@ -82,7 +82,7 @@ int amg_numeric(svgpu_ctx* ctx, const float* Val0) {
 }
 
 namespace {
-void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x) {
+void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, const int* fl) {
   AmgState& st = *ctx->amg;
   AmgLevel& A = st.lv[l];
   const int* rp = l == 0 ? ctx->rowPtr.p : A.rowPtr.p;
@@ -90,7 +90,7 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x) 
   const float* val = l == 0 ? Val0 : A.val.p;
   cudaStream_t s = ctx->stream;
   if (l + 1 == (int)st.lv.size()) {
-    amg_coarse_solve(s, A.n, rp, cp, val, A.dinv.p, b, x, A.r.p, st.omega, st.coarse_sweeps);
+    amg_coarse_solve(s, A.n, rp, cp, val, A.dinv.p, b, x, A.r.p, st.omega, st.coarse_sweeps, fl);
     ctx->launches++;
     return;
   }
@@ -98,21 +98,23 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x) 
   // pre-smoothing from zero (on the finest level optionally the learned network),
   // coarse-grid correction of the residual, post-smoothing
   if (l == 0 && st.gnn_smoother && ctx->gnn)
-    gnn_apply_device(ctx, b, nullptr, ctx->gnn->scal.p + 4, x, nullptr, nullptr);
+    gnn_apply_device(ctx, b, nullptr, ctx->gnn->scal.p + 4, x, nullptr, fl);
   else
-    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, nullptr, x, true);
-  amg_spmv(s, A.n, rp, cp, val, x, A.r.p);
-  amg_residual(s, 4L * A.n, b, A.r.p, A.r.p);
-  amg_restrict(s, C.n, A.aggPtr.p, A.aggList.p, A.r.p, C.b.p);
+    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, nullptr, x, true, fl);
+  amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
+  amg_residual(s, 4L * A.n, b, A.r.p, A.r.p, fl);
+  amg_restrict(s, C.n, A.aggPtr.p, A.aggList.p, A.r.p, C.b.p, fl);
   ctx->launches += 4;
-  vcycle(ctx, l + 1, Val0, C.b.p, C.x.p);
-  amg_prolong_add(s, A.n, A.agg.p, C.x.p, x);
-  amg_spmv(s, A.n, rp, cp, val, x, A.r.p);
-  amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, false);
+  vcycle(ctx, l + 1, Val0, C.b.p, C.x.p, fl);
+  amg_prolong_add(s, A.n, A.agg.p, C.x.p, x, fl);
+  amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
+  amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, false, fl);
   ctx->launches += 3;
 }
 }  // namespace
 
-void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z) { vcycle(ctx, 0, ctx->amg_val0, b, z); }
+void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z, const int* flags) {
+  vcycle(ctx, 0, ctx->amg_val0, b, z, flags);
+}
 
 }  // namespace svgpu

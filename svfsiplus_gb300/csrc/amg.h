@@ -35,19 +35,24 @@ void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::ve
 // k_amg.cu
 void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal, float* coarseVal);
 void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, float* dinv);
+// the kernels below take the restart cycle's flag word (may be null) and return at
+// once when the cycle has stopped
 void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
-                bool first);
-void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r);
-void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc);
-void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x);
+                bool first, const int* flags);
+void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags);
+void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
+                  const int* flags);
+void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x, const int* flags);
 void amg_coarse_solve(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* dinv,
-                      const float* b, float* x, float* y, float omega, int sweeps);
+                      const float* b, float* x, float* y, float omega, int sweeps, const int* flags);
 // amg.cpp
 struct svgpu_ctx_fwd;
 int amg_build(svgpu_ctx* ctx);
 int amg_numeric(svgpu_ctx* ctx, const float* Val0);
-// z = M b on level 0 (FP32 vectors of 4 nNo); enqueued on ctx->stream, capturable
-void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z);
-void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y);
+// z = M b on level 0 (FP32 vectors of 4 nNo); enqueued on ctx->stream, capturable;
+// every kernel is skipped once flags (the cycle's flag word, may be null) says stop
+void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z, const int* flags);
+void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y,
+              const int* flags);
 
 }  // namespace svgpu

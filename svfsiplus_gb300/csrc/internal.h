@@ -131,6 +131,9 @@ struct svgpu_ctx {
   std::string err;
   long long launches = 0;
   int sm_count = 0;
+  // restart cycles as CUDA graphs (default) or as individual launches (environment
+  // SVGPU_GRAPHS=0 at context creation: per-kernel profilers see plain launches)
+  bool use_graphs = true;
 
   // linear-system layout (fsils_lhs_create)
   int nNo = 0, nnz = 0, nFaces = 0;

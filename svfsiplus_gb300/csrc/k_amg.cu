@@ -8,6 +8,13 @@ namespace svgpu {
 
 namespace {
 
+// The V-cycle kernels run inside the restart-cycle graph of the flexible GMRES: like the
+// Arnoldi kernels they return at once when the cycle has converged (flags[0]) or broken
+// down (flags[2]); flags may be null outside a cycle.
+__device__ __forceinline__ bool stopped(const int* flags) {
+  return flags != nullptr && (flags[0] != 0 || flags[2] != 0);
+}
+
 // coarse block c, entry e: sum of entry e of the fine blocks listed for c
 __global__ void galerkin_kernel(int ncb, const int* __restrict__ sumPtr, const int* __restrict__ sumIdx,
                                 const float* __restrict__ fv, float* __restrict__ cv) {
@@ -62,7 +69,9 @@ __global__ void diag_inv_kernel(int n, const int* __restrict__ diagPtr, const fl
 
 // x <- x + omega D^-1 (b - Ax)   (first: x <- omega D^-1 b)
 __global__ void jacobi_kernel(int n, float omega, const float* __restrict__ dinv, const float* __restrict__ b,
-                              const float* __restrict__ Ax, float* __restrict__ x, int first) {
+                              const float* __restrict__ Ax, float* __restrict__ x, int first,
+                              const int* flags) {
+  if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long i = t >> 2;
   const int r = (int)(t & 3);
@@ -82,13 +91,15 @@ __global__ void jacobi_kernel(int n, float omega, const float* __restrict__ dinv
 }
 
 // r = b - Ax; r may be the same array as Ax
-__global__ void residual_kernel(long n4, const float* __restrict__ b, const float* Ax, float* r) {
+__global__ void residual_kernel(long n4, const float* __restrict__ b, const float* Ax, float* r, const int* flags) {
+  if (stopped(flags)) return;
   for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (long)gridDim.x * blockDim.x)
     r[k] = b[k] - Ax[k];
 }
 
 __global__ void restrict_kernel(int nc, const int* __restrict__ aggPtr, const int* __restrict__ aggList,
-                                const float* __restrict__ r, float* __restrict__ bc) {
+                                const float* __restrict__ r, float* __restrict__ bc, const int* flags) {
+  if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long c = t >> 2;
   const int q = (int)(t & 3);
@@ -99,7 +110,8 @@ __global__ void restrict_kernel(int nc, const int* __restrict__ aggPtr, const in
 }
 
 __global__ void prolong_kernel(int n, const int* __restrict__ agg, const float* __restrict__ xc,
-                               float* __restrict__ x) {
+                               float* __restrict__ x, const int* flags) {
+  if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 4L * n) return;
   const long i = t >> 2;
@@ -108,7 +120,9 @@ __global__ void prolong_kernel(int n, const int* __restrict__ agg, const float* 
 
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict__ rowPtr,
                                                    const int* __restrict__ colPtr, const float* __restrict__ val,
-                                                   const float* __restrict__ x, float* __restrict__ y) {
+                                                   const float* __restrict__ x, float* __restrict__ y,
+                                                   const int* flags) {
+  if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
   const int r = (int)(t & 3);
@@ -138,24 +152,26 @@ void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, f
 }
 
 void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
-                bool first) {
-  jacobi_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, omega, dinv, b, Ax, x, first ? 1 : 0);
+                bool first, const int* flags) {
+  jacobi_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, omega, dinv, b, Ax, x, first ? 1 : 0, flags);
 }
 
-void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r) {
-  residual_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, b, Ax, r);
+void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags) {
+  residual_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, b, Ax, r, flags);
 }
 
-void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc) {
-  restrict_kernel<<<(unsigned)((4L * nc + 255) / 256), 256, 0, s>>>(nc, aggPtr, aggList, r, bc);
+void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
+                  const int* flags) {
+  restrict_kernel<<<(unsigned)((4L * nc + 255) / 256), 256, 0, s>>>(nc, aggPtr, aggList, r, bc, flags);
 }
 
-void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x) {
-  prolong_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, agg, xc, x);
+void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x, const int* flags) {
+  prolong_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, agg, xc, x, flags);
 }
 
-void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y) {
-  spmv_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, rowPtr, colPtr, val, x, y);
+void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y,
+              const int* flags) {
+  spmv_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, rowPtr, colPtr, val, x, y, flags);
 }
 
 }  // namespace svgpu
@@ -170,7 +186,9 @@ __global__ void __launch_bounds__(1024) coarse_solve_kernel(int n, const int* __
                                                             const float* __restrict__ val,
                                                             const float* __restrict__ dinv,
                                                             const float* __restrict__ b, float* __restrict__ x,
-                                                            float* __restrict__ y, float omega, int sweeps) {
+                                                            float* __restrict__ y, float omega, int sweeps,
+                                                            const int* flags) {
+  if (stopped(flags)) return;
   const int n4 = 4 * n;
   for (int k = threadIdx.x; k < n4; k += blockDim.x) x[k] = 0.f;
   __syncthreads();
@@ -198,8 +216,8 @@ __global__ void __launch_bounds__(1024) coarse_solve_kernel(int n, const int* __
 }  // namespace
 
 void amg_coarse_solve(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* dinv,
-                      const float* b, float* x, float* y, float omega, int sweeps) {
-  coarse_solve_kernel<<<1, 1024, 0, s>>>(n, rowPtr, colPtr, val, dinv, b, x, y, omega, sweeps);
+                      const float* b, float* x, float* y, float omega, int sweeps, const int* flags) {
+  coarse_solve_kernel<<<1, 1024, 0, s>>>(n, rowPtr, colPtr, val, dinv, b, x, y, omega, sweeps, flags);
 }
 
 }  // namespace svgpu
