@@ -15,7 +15,10 @@ Paths (--path):
   multilevel -- the headline: mixed precision (FP32 tangent/Krylov basis, FP64 residual
                 and defect correction) with FGMRES(50) preconditioned by an aggregation
                 multilevel V-cycle (solver mode 2);
-  learned    -- the same with the learned network as finest-level smoother (mode 3);
+  learned    -- the same with the learned network as the initial guess of every solve
+                (mode 4), trained online on the solver's own pairs during the warm-up
+                steps;
+  learned-smoother -- the network also as finest-level pre-smoother (mode 3);
   mixed      -- mixed precision, GMRES(50) + diagonal preconditioner (mode 0);
   plain      -- FP64, GMRES(50) + diagonal preconditioner: the reference's method.
 
@@ -59,7 +62,7 @@ NEWTON_MAX = 8
 LIN_REL_TOL = 1e-2
 KRYLOV_DIM = 50
 MAX_RESTARTS = 40
-PATH_MODES = {"multilevel": 2, "learned": 3, "mixed": 0, "plain": -1}
+PATH_MODES = {"multilevel": 2, "learned": 4, "learned-smoother": 3, "mixed": 0, "plain": -1}
 U_MEAN, U_AMP, U_FREQ = 10.0, 5.0, 1.0
 
 
@@ -210,7 +213,7 @@ def kernel_breakdown(step_fn, path):
     import torch
     from torch.profiler import ProfilerActivity, profile
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
         step_fn()
         torch.cuda.synchronize()
     with tempfile.TemporaryDirectory() as d:
@@ -218,9 +221,11 @@ def kernel_breakdown(step_fn, path):
         prof.export_chrome_trace(fn)
         with open(fn) as f:
             trace = json.load(f)
-    agg = {}
+    agg, cats = {}, {}
     for e in trace.get("traceEvents", []):
-        if e.get("cat") == "kernel" and "dur" in e:
+        c = str(e.get("cat"))
+        cats[c] = cats.get(c, 0) + 1
+        if c.lower() == "kernel" and "dur" in e:
             r = agg.setdefault(e.get("name", "?"), [0, 0.0])
             r[0] += 1
             r[1] += float(e["dur"]) / 1e3
@@ -231,7 +236,7 @@ def kernel_breakdown(step_fn, path):
         r["share"] = r["total_ms"] / tot if tot else 0.0
         r["avg_us"] = 1e3 * r["total_ms"] / r["launches"]
     with open(path, "w") as f:
-        json.dump({"total_ms": tot, "kernels": rows}, f, indent=1)
+        json.dump({"total_ms": tot, "event_categories": cats, "kernels": rows}, f, indent=1)
     return {"total_device_ms": tot, "launches": sum(r["launches"] for r in rows),
             "top": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows[:10]]}
 
@@ -259,10 +264,10 @@ def make_solver(api, mesh, rowPtr, colPtr, path, device=0):
     s = api.PipeFluidSolver(mesh, device=device, sD=KRYLOV_DIM, mItr=MAX_RESTARTS, relTol=LIN_REL_TOL, absTol=1e-17,
                             newton_min=1, newton_max=NEWTON_MAX, newton_tol=NEWTON_TOL, precision=precision,
                             rowPtr=rowPtr, colPtr=colPtr)
-    if mode == 3:
+    if mode in (3, 4):
         s.enable_learning()
     if mode >= 0:
-        s.ctx.set_solver_mode(mode if mode != 3 else 2)
+        s.ctx.set_solver_mode(mode if mode not in (3, 4) else 2)
     return s, mode
 
 
@@ -302,10 +307,10 @@ def run_ours(args):
     warm_stats = []
     for k in range(args.warmup):
         warm_stats.append(dev_step())
-        if mode == 3:  # online training on the pairs of the warm-up steps, then learned mode
+        if mode in (3, 4):  # online training on the pairs of the warm-up steps, then learned mode
             s.ctx.gnn_train(50, 1e-3)
             if k == args.warmup - 1:
-                s.ctx.set_solver_mode(3)
+                s.ctx.set_solver_mode(mode)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -321,6 +326,7 @@ def run_ours(args):
         torch.cuda.synchronize()
     dev_ms = ev0.elapsed_time(ev1)
     launches = s.ctx.kernel_launches - launches0
+    rejects = s.ctx.learned_rejects
     if world > 1:
         t = torch.tensor([dev_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -378,6 +384,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (Val is 1.3-2.6 GB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "krylov_iters_per_step": [sum(q["itr"] for q in st) for st in stats], "krylov_iters": its,
         "newton_iters": newton, "newton_final_over_first": conv,
+        "learned_rejects_after_timed": rejects if mode in (3, 4) else None,
         "plain_gpu": plain,
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
@@ -404,8 +411,8 @@ def run_study(args):
     for path in args.study.split(","):
         s, mode = make_solver(api, mesh, rowPtr, colPtr, path)
         for k in range(args.steps):
-            if mode == 3 and k == 2:
-                s.ctx.set_solver_mode(3)
+            if mode in (3, 4) and k == 2:
+                s.ctx.set_solver_mode(mode)
             t = time.perf_counter()
             st = s.step(U_MEAN, U_AMP, U_FREQ)
             dt = time.perf_counter() - t
@@ -414,7 +421,7 @@ def run_study(args):
                               "rel": [float("%.2g" % (q["fNorm"] / max(q["iNorm"], 1e-300))) for q in st],
                               "iNorm": [float("%.3g" % q["iNorm"]) for q in st],
                               "rejects": s.ctx.learned_rejects}), flush=True)
-            if mode == 3 and k < 2:
+            if mode in (3, 4) and k < 2:
                 s.ctx.gnn_train(50, 1e-3)
         s.ctx.close()
 

@@ -201,8 +201,9 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
  * reference's method); 1 FGMRES with the network as right preconditioner and initial
  * guess; 2 FGMRES with an aggregation multilevel V-cycle (block-Jacobi smoothing) as
  * right preconditioner; 3 as 2 with the network as finest-level pre-smoother and
- * initial guess.  Learned initial guesses and learned cycles that do not lower the
- * FP64 residual are rejected (plain cycles finish the solve). */
+ * initial guess; 4 as 2 with the network as initial guess only.  Learned initial
+ * guesses and learned cycles that do not lower the FP64 residual are rejected (plain
+ * cycles finish the solve). */
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
 long long svgpu_learned_rejects(const svgpu_ctx* ctx);
 

@@ -129,7 +129,7 @@ struct CycleGraph {
 // Graphs of one context: the sD Arnoldi iterations of a restart cycle, one per kind
 // (0: FP64, 1: mixed precision).
 struct CtxGraphs {
-  std::unique_ptr<CycleGraph> g[5];  // 0: FP64, 1: mixed, 2..4: mixed flexible, by solver mode 1..3
+  std::unique_ptr<CycleGraph> g[5];  // 0: FP64, 1: mixed, 2..4: mixed flexible, by solver mode 1..3 (4 uses 3)
 };
 std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
   static std::map<const svgpu_ctx*, CtxGraphs> g;
@@ -421,8 +421,10 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   const int sD = kw.sD;
   int rc = SVGPU_OK;
   const int mode = ctx->learned_mode;
-  const bool use_gnn = (mode == 1 || mode == 3) && ctx->gnn != nullptr;
+  const bool use_gnn = (mode == 1 || mode == 3 || mode == 4) && ctx->gnn != nullptr;
   bool learned = mode != 0 && (use_gnn || mode == 2);  // flexible cycles
+  // mode 4 runs the cycles of mode 2 (multilevel V-cycle); only its initial guess is learned
+  const int cycle_kind = 1 + (mode == 4 ? 2 : mode);
   if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
   st->suc = 0;
   double nrm = device_norm(ctx, n, Rs, rc);
@@ -503,7 +505,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     launch_norm2(ctx->stream, n, kw.r64.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
     launch_start_vector32(ctx->stream, n, kw.r64.p, kw.scal.p + 2, kw.V32.p, kw.givens.p + 2 * sD, kw.flags.p);
     ctx->launches += 3;
-    if ((rc = run_cycle_kind(ctx, Val32, learned ? 1 + mode : 1))) return rc;
+    if ((rc = run_cycle_kind(ctx, Val32, learned ? cycle_kind : 1))) return rc;
     launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
     launch_xupdate32(ctx->stream, n, sD, learned ? kw.zbasis.p : kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
     ctx->launches += 2;

@@ -279,8 +279,8 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss) {
 
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode) {
   if (!ctx) return SVGPU_EINVAL;
-  if (mode < 0 || mode > 3) return set_err(ctx, SVGPU_EINVAL, "set_solver_mode: mode must be 0..3");
-  if ((mode == 1 || mode == 3) && !ctx->gnn)
+  if (mode < 0 || mode > 4) return set_err(ctx, SVGPU_EINVAL, "set_solver_mode: mode must be 0..4");
+  if ((mode == 1 || mode == 3 || mode == 4) && !ctx->gnn)
     return set_err(ctx, SVGPU_ESTATE, "set_solver_mode: the learned modes need a network (svgpu_gnn_create)");
   ctx->learned_mode = mode;
   return SVGPU_OK;
