@@ -187,6 +187,17 @@ def fsils_solve_gmres(rowPtr, colPtr, Val, R, dirMask, sD=50, mItr=100, relTol=1
     return R, Val, ls
 
 
+def fsils_solve_cg(rowPtr, colPtr, Val, R, dirMask, mItr=1000, relTol=1e-2, absTol=1e-10, dof=3):
+    """fsils_solve with LS_TYPE_CG; returns (increment, scaled Val, LS stats)."""
+    nNo = rowPtr.size - 1
+    Val = np.array(Val, dtype=np.float64, order="C", copy=True)
+    R = np.array(R, dtype=np.float64, order="C", copy=True)
+    ls = LS(0, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0)
+    mask = None if dirMask is None else _p(np.ascontiguousarray(dirMask, dtype=np.float64))
+    lib().or_fsils_solve_cg(nNo, dof, _p(rowPtr), _p(colPtr), _p(Val), _p(R), mask, C.byref(ls))
+    return R, Val, ls
+
+
 class FluidRun:
     """The reference's fluid time loop on one pipe mesh (oracle side)."""
 

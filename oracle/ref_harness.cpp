@@ -200,6 +200,34 @@ static int assemble_only(const std::string& dir, const std::string& out, std::ma
   write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
   write_raw(out + "/rowPtr.bin", com.rowPtr.data(), (size_t)com.rowPtr.size());
   write_raw(out + "/colPtr.bin", com.colPtr.data(), (size_t)com.colPtr.size());
+  if (P.count("solve_cg") && P.at("solve_cg") == "1") {
+    // fsils_solve with LS_TYPE_CG (cgrad_v, cgrad.cpp:166) + diagonal preconditioner on
+    // the assembled system, Dirichlet rows/cols (zero value) at the listed nodes
+    fsi_linear_solver::FSILS_commuType commu;
+    fsi_linear_solver::fsils_commu_create(commu, MPI_COMM_WORLD);
+    Vector<int> gNodes(nNo);
+    for (int a = 0; a < nNo; a++) gNodes(a) = a;
+    fsi_linear_solver::fsils_lhs_create(com.lhs, commu, nNo, nNo, nnz, gNodes, com.rowPtr, com.colPtr, 1);
+    auto dn = read_raw<int>(dir + "/dir_nodes.bin");
+    Vector<int> gN((int)dn.size());
+    for (size_t a = 0; a < dn.size(); a++) gN((int)a) = dn[a];
+    Array<double> sVl(3, (int)dn.size());
+    fsi_linear_solver::fsils_bc_create(com.lhs, 0, (int)dn.size(), 3, fsi_linear_solver::BcType::BC_TYPE_Dir, gN, sVl);
+    fsi_linear_solver::fsils_ls_create(eq.FSILS, fsi_linear_solver::LinearSolverType::LS_TYPE_CG,
+                                       getd("ls_rel_tol"), getd("ls_abs_tol"), std::stoi(P.at("ls_max_itr")));
+    Vector<int> incL(1);
+    incL = 1;
+    Vector<double> res(1);
+    res = 0.0;
+    fsi_linear_solver::fsils_solve(com.lhs, eq.FSILS, 3, com.R, com.Val, consts::PreconditionerType::PREC_FSILS, incL,
+                                   res);
+    write_raw(out + "/dX.bin", com.R.data(), (size_t)com.R.size());
+    auto& RI = eq.FSILS.RI;
+    std::ofstream log(out + "/log.txt");
+    log.precision(17);
+    log << "cg iNorm " << RI.iNorm << " fNorm " << RI.fNorm << " itr " << RI.itr << " suc " << RI.suc << " dB "
+        << RI.dB << "\n";
+  }
   return 0;
 }
 

@@ -473,12 +473,13 @@ void or_axpy(long n, double r, double* U, const double* V) {
   for (long k = 0; k < n; k++) U[k] = U[k] + r * V[k];
 }
 
-void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
-                          double* Val, double* R, const double* dirMask, or_ls* ls) {
+/* precond_diag (precond.cpp:122-257) with pre_mul / pos_mul: W = |diag|^-1/2 (0 -> 1)
+ * times the Dirichlet mask; Val <- diag(W) Val diag(W), R <- W R.  W is returned. */
+static double* precond_diag_apply(int nNo, int dof, const int* rowPtr, const int* colPtr, double* Val, double* R,
+                                  const double* dirMask) {
   const long n = (long)nNo * dof;
   const int d2 = dof * dof;
   double* W = (double*)malloc(sizeof(double) * (size_t)n);
-  /* precond_diag (precond.cpp:122-257) */
   for (int a = 0; a < nNo; a++) {
     int d = -1;
     for (int k = rowPtr[a]; k < rowPtr[a + 1]; k++)
@@ -499,6 +500,13 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
       for (int r = 0; r < dof; r++)
         for (int c = 0; c < dof; c++) Val[(long)d2 * k + r * dof + c] = Val[(long)d2 * k + r * dof + c] * W[dof * col + c];
     }
+  return W;
+}
+
+void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
+                          double* Val, double* R, const double* dirMask, or_ls* ls) {
+  const long n = (long)nNo * dof;
+  double* W = precond_diag_apply(nNo, dof, rowPtr, colPtr, Val, R, dirMask);
 
   /* gmres_v (gmres.cpp:450-629) */
   const int sD = ls->sD;
@@ -577,6 +585,48 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
   /* solve.cpp:184-186: R <- Wc * R */
   for (long i = 0; i < n; i++) R[i] = W[i] * R[i];
   free(W); free(h); free(X); free(u); free(y); free(c); free(s); free(err);
+}
+
+/* fsils_solve (solve.cpp:50-193) with LS_TYPE_CG: precond_diag, then cgrad_v
+ * (cgrad.cpp:166-246): X = 0, P = R, err = |R|^2, eps = max(absTol, relTol |R|)^2; per
+ * iteration KP = K P, alpha = errO / (P . KP), X += alpha P, R -= alpha KP,
+ * err = |R|^2, P = (P + (errO/err) R) * (err/errO) in that order; itr is the index of
+ * the last loop pass, fNorm = sqrt(err), dB = 5 log(err/errO).  R <- Wc X. */
+void or_fsils_solve_cg(int nNo, int dof, const int* rowPtr, const int* colPtr,
+                       double* Val, double* R, const double* dirMask, or_ls* ls) {
+  const long n = (long)nNo * dof;
+  double* W = precond_diag_apply(nNo, dof, rowPtr, colPtr, Val, R, dirMask);
+  double* P = (double*)malloc(sizeof(double) * (size_t)n);
+  double* KP = (double*)malloc(sizeof(double) * (size_t)n);
+  double* X = (double*)calloc((size_t)n, sizeof(double));
+  ls->suc = 0;
+  ls->iNorm = sqrt(dotv(n, R, R));
+  const double e0 = fmax(ls->absTol, ls->relTol * ls->iNorm);
+  const double eps = pow(e0, 2.0);
+  double errO = ls->iNorm * ls->iNorm;
+  double err = errO;
+  for (long k = 0; k < n; k++) P[k] = R[k];
+  int last_i = 0;
+  for (int i = 0; i < ls->mItr; i++) {
+    last_i = i;
+    if (err < eps) { ls->suc = 1; break; }
+    errO = err;
+    or_spar_mul(nNo, dof, rowPtr, colPtr, Val, P, KP);
+    const double alpha = errO / dotv(n, P, KP);
+    for (long k = 0; k < n; k++) X[k] = X[k] + alpha * P[k];
+    for (long k = 0; k < n; k++) R[k] = R[k] + (-alpha) * KP[k];
+    err = sqrt(dotv(n, R, R));
+    err = err * err;
+    const double c = errO / err, d = err / errO;
+    for (long k = 0; k < n; k++) P[k] = P[k] + c * R[k];
+    for (long k = 0; k < n; k++) P[k] = d * P[k];
+  }
+  for (long k = 0; k < n; k++) R[k] = X[k];
+  ls->itr = last_i;
+  ls->fNorm = sqrt(err);
+  ls->dB = errO < DBL_EPSILON ? 0.0 : 5.0 * log(err / errO);
+  for (long i = 0; i < n; i++) R[i] = W[i] * R[i];
+  free(W); free(P); free(KP); free(X);
 }
 
 /* ---------------------------------------------------------------- Newton loop */

@@ -110,6 +110,11 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
 
 /* fsils_nc_dot_v (dot.cpp:134-171) and omp_sum_v U += r V (omp_la.cpp:102-144) over n
  * entries, the Krylov vector kernels of gmres_v. */
+/* fsils_solve (solve.cpp:50-193) for CG (cgrad_v, cgrad.cpp:166-246) + FSILS diagonal
+ * preconditioning, any dof > 1; ls->sD unused, ls->mItr = CG iterations. */
+void or_fsils_solve_cg(int nNo, int dof, const int* rowPtr, const int* colPtr,
+                       double* Val, double* R, const double* dirMask, or_ls* ls);
+
 double or_dot(long n, const double* u, const double* v);
 void or_axpy(long n, double r, double* U, const double* V);
 

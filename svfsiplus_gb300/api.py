@@ -27,6 +27,7 @@ SVGPU_OK = 0
 SVGPU_FP64, SVGPU_MIXED = 0, 1
 BC_TYPE_Dir, BC_TYPE_Neu = 0, 1
 LS_TYPE_GMRES = 2
+LS_TYPE_CG = 3
 PREC_NONE, PREC_FSILS = 0, 1
 
 _lib = None

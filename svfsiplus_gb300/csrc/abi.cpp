@@ -603,8 +603,10 @@ int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, cons
     launch_fill(ctx->stream, n, 1.0, kw.Wc.p);
     ctx->launches++;
   }
-  if (ctx->lsType != SVGPU_LS_GMRES) return set_err(ctx, SVGPU_EINVAL, "only GMRES is available in fsils_solve");
-  rc = gmres_device(ctx, dof, Val, R, st);
+  if (ctx->lsType == SVGPU_LS_CG)
+    rc = cg_device(ctx, dof, Val, R, st);
+  else
+    rc = gmres_device(ctx, dof, Val, R, st);
   if (rc) return rc;
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches++;
@@ -707,6 +709,7 @@ int svgpu_destroy(svgpu_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   graphs().erase(ctx);
+  cg_release(ctx);
   cudaStream_t s = ctx->stream;
   cudaStream_t cs = ctx->capture_stream;
   bool own = ctx->own_stream;
@@ -727,6 +730,7 @@ int svgpu_set_stream(svgpu_ctx* ctx, void* stream) {
   ctx->stream = (cudaStream_t)stream;
   ctx->own_stream = false;
   graphs().erase(ctx);
+  cg_release(ctx);
   return SVGPU_OK;
 }
 
@@ -769,6 +773,7 @@ int svgpu_lhs_create(svgpu_ctx* ctx, int gnNo, int nNo, int nnz, const int* gNod
   if ((rc = to_device(ctx, ctx->blkRow, blkRow.data(), nnz))) return rc;
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   graphs().erase(ctx);
+  cg_release(ctx);
   return SVGPU_OK;
 }
 
@@ -803,13 +808,16 @@ int svgpu_bc_create(svgpu_ctx* ctx, int faIn, int nNo, int dof, int bcType, cons
 
 int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, int maxItr, int dimKry) {
   if (!ctx) return SVGPU_EINVAL;
-  if (lsType != SVGPU_LS_GMRES) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: only GMRES is supported");
-  // defaults of fsils_ls_create (liner_solver/ls.cpp:62-79)
+  if (lsType != SVGPU_LS_GMRES && lsType != SVGPU_LS_CG)
+    return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: GMRES or CG");
+  // defaults of fsils_ls_create (liner_solver/ls.cpp:62-79): GMRES relTol 0.1, 4 restarts
+  // of dimension 250; CG relTol 1e-2, 1000 iterations (the Krylov dimension is unused)
+  const bool cg = lsType == SVGPU_LS_CG;
   ctx->lsType = lsType;
-  ctx->relTol = relTol >= 0 ? relTol : 0.1;
+  ctx->relTol = relTol >= 0 ? relTol : (cg ? 1e-2 : 0.1);
   ctx->absTol = absTol >= 0 ? absTol : 1e-10;
-  ctx->mItr = maxItr > 0 ? maxItr : 4;
-  ctx->sD = dimKry > 0 ? dimKry : 250;
+  ctx->mItr = maxItr > 0 ? maxItr : (cg ? 1000 : 4);
+  ctx->sD = cg ? 1 : (dimKry > 0 ? dimKry : 250);
   if (ctx->sD > 250) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: Krylov dimension above 250");
   ctx->ls_created = true;
   return SVGPU_OK;

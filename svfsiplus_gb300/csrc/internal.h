@@ -160,6 +160,8 @@ struct svgpu_ctx {
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
+  svgpu::DevBuf<double> cg_part, cg_d;  // CG: per-CTA partial sums, device scalars
+  svgpu::DevBuf<int> cg_f;              // CG: stop, last_i, suc, next iteration
   std::unique_ptr<svgpu::GnnState> gnn;
   std::unique_ptr<struct svgpu::AmgState> amg;
   const float* amg_val0 = nullptr;  // level-0 matrix of the current numeric set-up
@@ -218,6 +220,12 @@ inline int grid_for(long n, int block, int cap = 152 * 16) {
 }
 
 // ---- k_krylov.cu -------------------------------------------------------------
+// k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
+int cg_parts(long n);
+void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
+                         double* P, double* KP, double* X, double* R, double* part, double* d, int* f, int mItr);
+int cg_device(svgpu_ctx* ctx, int dof, const double* K, double* R, svgpu_ls_stats* st);
+void cg_release(const svgpu_ctx* ctx);
 void launch_spmv4_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr,
                       const double* Val, const double* x, double* y);
 void launch_spmv_generic(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr,

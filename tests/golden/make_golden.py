@@ -51,13 +51,20 @@ SOLID["Kpen"] = SOLID["E"] / (3.0 * (1.0 - 2.0 * SOLID["nu"]))     # bulk modulu
 MESHMOTION = dict(rho=0.5, E=1.0, nu=0.3, dt=1e-3, rho_inf=0.5)
 
 
-def run_assembly(name, physics):
+def run_assembly(name, physics, solve=None):
+    """Assembly of one solid or mesh-motion system with seeded random state; with
+    `solve` = dict(ls_rel_tol, ls_abs_tol, ls_max_itr) also the reference's CG solve
+    (fsils_solve, LS_TYPE_CG, diagonal preconditioner) with zero Dirichlet values at
+    the inlet and outlet nodes."""
     mesh = named_pipe("small")
     rng = np.random.default_rng(17)
     nNo = mesh.nNo
     tDof = 3 if physics == "struct" else 7
     params = dict(SOLID if physics == "struct" else MESHMOTION)
     params["mode"] = "assemble_" + physics
+    if solve:
+        params.update(solve)
+        params["solve_cg"] = 1
     scale = 0.01 if physics == "struct" else 0.02
     A = rng.standard_normal((nNo, tDof))
     Y = rng.standard_normal((nNo, tDof))
@@ -74,9 +81,18 @@ def run_assembly(name, physics):
             Do = scale * rng.standard_normal((nNo, tDof))
             Do.tofile(os.path.join(cdir, "Do.bin"))
             out["Do"] = Do
+        if solve:
+            dirn = np.unique(np.concatenate([mesh.faces["inlet"].gN, mesh.faces["outlet"].gN])).astype(np.int32)
+            dirn.tofile(os.path.join(cdir, "dir_nodes.bin"))
+            out["dir_nodes"] = dirn
         os.makedirs(odir)
         subprocess.run([HARNESS, cdir, odir], check=True)
         rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
+        if solve:
+            out["dX"] = rd("dX.bin", np.float64).reshape(nNo, 3)
+            with open(os.path.join(odir, "log.txt")) as fh:
+                t = fh.read().split()
+            out["cg_stats"] = np.array([float(t[2]), float(t[4]), float(t[6]), float(t[8]), float(t[10])])
         out["rowPtr"] = rd("rowPtr.bin", np.int32)
         out["colPtr"] = rd("colPtr.bin", np.int32)
         out["R_asm"] = rd("R_asm.bin", np.float64).reshape(nNo, 3)
@@ -147,10 +163,14 @@ def run_case(name):
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small"]):
+    for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small", "mesh_cg_small", "mesh_cg7_small"]):
         if n == "struct_small":
             run_assembly(n, "struct")
         elif n == "mesh_small":
             run_assembly(n, "mesh")
+        elif n == "mesh_cg_small":  # CG to 1e-10 (stats: iNorm, fNorm, itr, suc, dB)
+            run_assembly(n, "mesh", dict(ls_rel_tol=1e-10, ls_abs_tol=1e-30, ls_max_itr=2000))
+        elif n == "mesh_cg7_small":  # exactly 7 CG iterations
+            run_assembly(n, "mesh", dict(ls_rel_tol=1e-30, ls_abs_tol=1e-300, ls_max_itr=7))
         else:
             run_case(n)
