@@ -350,6 +350,14 @@ def run_ours(args):
     breakdown = None
     if args.breakdown:
         breakdown = kernel_breakdown(dev_step, args.breakdown)
+    # phases of one more step (CUDA events at phase boundaries, outside the timed region)
+    s.ctx.phase_timing(True)
+    s.ctx.phase_times()
+    pst = dev_step()
+    phases = {k: {"ms": round(v[0], 3), "intervals": v[1]} for k, v in s.ctx.phase_times().items()}
+    s.ctx.phase_timing(False)
+    phases["krylov_iters"] = sum(q["itr"] for q in pst)
+    phases["newton_iters"] = len(pst)
 
     # the plain FP64 GPU path (the reference's method) from the same state, one step
     plain = None
@@ -393,6 +401,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "setup_s": setup_s,
     }
+    rec["phases_one_step"] = phases
     if breakdown:
         rec["kernel_breakdown"] = breakdown
     if rank == 0 and not args.no_cpu:
@@ -410,6 +419,7 @@ def run_study(args):
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
     for path in args.study.split(","):
         s, mode = make_solver(api, mesh, rowPtr, colPtr, path)
+        s.ctx.phase_timing(True)
         for k in range(args.steps):
             if mode in (3, 4) and k == 2:
                 s.ctx.set_solver_mode(mode)
@@ -420,7 +430,9 @@ def run_study(args):
                               "newton": len(st), "its": [q["itr"] for q in st],
                               "rel": [float("%.2g" % (q["fNorm"] / max(q["iNorm"], 1e-300))) for q in st],
                               "iNorm": [float("%.3g" % q["iNorm"]) for q in st],
-                              "rejects": s.ctx.learned_rejects}), flush=True)
+                              "rejects": s.ctx.learned_rejects,
+                              "phases_ms": {k: round(v[0], 2) for k, v in s.ctx.phase_times().items() if v[1]}}),
+                  flush=True)
             if mode in (3, 4) and k < 2:
                 s.ctx.gnn_train(50, 1e-3)
         s.ctx.close()

@@ -207,6 +207,20 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
 long long svgpu_learned_rejects(const svgpu_ctx* ctx);
 
+/* ---- phase timing (no reference counterpart: instrumentation of this library) --------
+ * With timing on, CUDA events on the library's stream bound the phases of every Newton
+ * iteration; svgpu_phase_times returns (and clears) the accumulated milliseconds and
+ * interval counts per phase: 0 assembly (+ backflow), 1 Dirichlet mask and diagonal
+ * scaling, 2 multilevel numeric set-up, 3 learned initial guess, 4 restart residuals,
+ * 5 Krylov cycles (+ back substitution and X update), 6 other (predictor, corrector,
+ * pair storage); with the cycles launched one kernel at a time (environment
+ * SVGPU_GRAPHS=0 at context creation) the flexible cycles are split further into
+ * 7 right preconditioner (network, or the V-cycle's finest level), 8 operator product,
+ * 9 Gram-Schmidt and Givens, 10 the V-cycle's coarse levels.
+ * n: entries of ms / intervals (11); intervals may be NULL. */
+int svgpu_phase_timing(svgpu_ctx* ctx, int on);
+int svgpu_phase_times(svgpu_ctx* ctx, double* ms, long long* intervals, int n);
+
 /* ---- Newton time step (solver/main.cpp:292-762 for one fluid equation) ----------- */
 typedef struct {
   int minItr, maxItr;        /* eqType minItr / maxItr */

@@ -262,6 +262,19 @@ class Context:
         lib().svgpu_learned_rejects.restype = C.c_longlong
         return int(lib().svgpu_learned_rejects(self._h))
 
+    PHASES = ("assembly", "precond", "amg_setup", "learned_guess", "restart", "cycles", "other",
+              "cycle_precond", "cycle_spmv", "cycle_ortho", "cycle_coarse")
+
+    def phase_timing(self, on=True):
+        self._check(lib().svgpu_phase_timing(self._h, int(bool(on))), "phase_timing")
+
+    def phase_times(self):
+        """Accumulated milliseconds and interval counts per phase since the last call."""
+        ms = (C.c_double * 11)()
+        cnt = (C.c_longlong * 11)()
+        self._check(lib().svgpu_phase_times(self._h, ms, cnt, 11), "phase_times")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PHASES)}
+
     def set_dirichlet(self, nodes):
         nodes = np.ascontiguousarray(nodes, dtype=np.int32)
         self._check(lib().svgpu_set_dirichlet(self._h, int(nodes.size), _ptr(nodes)), "set_dirichlet")

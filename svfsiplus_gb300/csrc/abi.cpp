@@ -239,6 +239,7 @@ int gmres_device(svgpu_ctx* ctx, int dof, const double* Val, double* R, svgpu_ls
   double dB = 0.0;
   const int sD = kw.sD;
   for (int l = 0; l < ctx->mItr; l++) {
+    phase_mark(ctx, PH_RESTART);
     dB = st->fNorm;
     st->itr++;
     // u0 = R - K X
@@ -253,6 +254,7 @@ int gmres_device(svgpu_ctx* ctx, int dof, const double* Val, double* R, svgpu_ls
     launch_norm2(ctx->stream, n, kw.V.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
     launch_scale_by_inv_norm(ctx->stream, n, kw.V.p, kw.scal.p + 2, kw.givens.p + 2 * sD, kw.flags.p);
     ctx->launches += 3;
+    phase_mark(ctx, PH_CYCLES);
     if ((rc = run_cycle(ctx, dof, Val))) return rc;
     launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
     launch_xupdate(ctx->stream, n, sD, kw.V.p, n, kw.givens.p, kw.flags.p, kw.X.p);
@@ -309,11 +311,14 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
     float* ui = kw.V32.p + (long)i * n;
     float* ui1 = kw.V32.p + (long)(i + 1) * n;
     float* zi = kw.zbasis.p + (long)i * n;
+    if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_PRECOND);
     if (ctx->learned_mode == 1)
       gnn_apply_device(ctx, ui, nullptr, ctx->gnn->scal.p + 4, zi, nullptr, kw.flags.p);
     else
       amg_vcycle(ctx, ui, zi, kw.flags.p);
+    if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_SPMV);
     launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
+    if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_ORTHO);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
                                        kw.flags.p);
     launch_reduce_partials_flag(ctx->stream, ctas, i + 2, kw.partial.p, hraw, kw.flags.p);
@@ -452,6 +457,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     const double sv = 1.0 / std::sqrt((double)n);  // scale of a unit-norm basis vector
     SVGPU_CUDA(ctx, cudaMemcpyAsync(g.scal.p + 4, &sv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     // learned initial guess X0 = M(Rs), kept only if it lowers the FP64 residual
+    phase_mark(ctx, PH_GUESS);
     launch_norm2(ctx->stream, n, Rs, g.nrmp.p, g.scal.p + 1, ctx->sm_count);
     gnn_scale(ctx->stream, g.scal.p + 1, n, g.scal.p);
     ctx->launches += 3;
@@ -473,6 +479,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   double dB = nrm;
   double before = nrm;  // FP64 residual norm when the current cycle started
   for (int l = 0; l < ctx->mItr; l++) {
+    phase_mark(ctx, PH_RESTART);
     if (l > 0) {
       launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
       launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
@@ -505,6 +512,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     launch_norm2(ctx->stream, n, kw.r64.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
     launch_start_vector32(ctx->stream, n, kw.r64.p, kw.scal.p + 2, kw.V32.p, kw.givens.p + 2 * sD, kw.flags.p);
     ctx->launches += 3;
+    phase_mark(ctx, PH_CYCLES);
     if ((rc = run_cycle_kind(ctx, Val32, learned ? cycle_kind : 1))) return rc;
     launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
     launch_xupdate32(ctx->stream, n, sD, learned ? kw.zbasis.p : kw.V32.p, n, kw.givens.p, kw.flags.p, kw.X.p);
@@ -538,6 +546,7 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   int rc = ensure_krylov(ctx, n, ctx->sD);
   if (rc) return rc;
   KrylovWork& kw = ctx->kw;
+  phase_mark(ctx, PH_PRECOND);
   launch_fill(ctx->stream, n, 1.0, kw.mask.p);
   ctx->launches++;
   for (int f = 0; f < ctx->nFaces; f++) {
@@ -555,12 +564,14 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
     if (!ctx->amg && (rc = amg_build(ctx))) return rc;
     ctx->amg->gnn_smoother = ctx->learned_mode == 3 && ctx->gnn;
     ctx->amg_val0 = Val32;
+    phase_mark(ctx, PH_AMG_SETUP);
     if ((rc = amg_numeric(ctx, Val32))) return rc;
   }
   const bool collect = ctx->gnn && ctx->gnn->collect;
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   rc = gmres_mixed(ctx, Val32, R, R, st);
   if (rc) return rc;
+  phase_mark(ctx, PH_OTHER);
   if (collect && st->iNorm > ctx->absTol) {
     // exact pair (K X, X) of the preconditioned system: K X = Rs - r, with r the final
     // FP64 residual the solve left in kw.r64 (valid whether or not it converged)
@@ -584,6 +595,7 @@ int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, cons
   int rc = ensure_krylov(ctx, n, ctx->sD);
   if (rc) return rc;
   KrylovWork& kw = ctx->kw;
+  phase_mark(ctx, PH_PRECOND);
   // Dirichlet mask from the included faces (precond.cpp:204-225)
   launch_fill(ctx->stream, n, 1.0, kw.mask.p);
   ctx->launches++;
@@ -1239,9 +1251,11 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
   int itr = 0;
   for (;;) {
     itr++;
+    phase_mark(ctx, PH_OTHER);
     launch_pic_initiate(ctx->stream, n4, props->am, props->af, ctx->Ao.p, ctx->An.p, ctx->Yo.p, ctx->Yn.p, ctx->Ag.p,
                         ctx->Yg.p);
     ctx->launches++;
+    phase_mark(ctx, PH_ASSEMBLY);
     if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr, opts->precision)))
       return rc;
     if (opts->outletFace >= 0) {
@@ -1257,6 +1271,7 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     else
       rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st);
     if (rc) return rc;
+    phase_mark(ctx, PH_OTHER);
     if (stats) stats[itr - 1] = st;
     // picc (pic.cpp:74-281)
     launch_pic_correct(ctx->stream, n4, props->gam * props->dt, props->beta * props->dt * props->dt, ctx->R.p,
@@ -1277,6 +1292,7 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, ctx->Yn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, ctx->Dn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  phase_mark(ctx, PH_COUNT);
   return itr;
 }
 

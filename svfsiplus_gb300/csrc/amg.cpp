@@ -69,7 +69,9 @@ int amg_numeric(svgpu_ctx* ctx, const float* Val0) {
   AmgState& st = *ctx->amg;
   const int L = (int)st.lv.size();
   amg_diag_inv(ctx->stream, st.lv[0].n, ctx->diagPtr.p, Val0, st.lv[0].dinv.p);
-  ctx->launches++;
+  SVGPU_CUDA(ctx, st.val0h.resize(16L * ctx->nnz));
+  amg_to_half(ctx->stream, 16L * ctx->nnz, Val0, st.val0h.p);
+  ctx->launches += 2;
   for (int l = 0; l + 1 < L; l++) {
     AmgLevel& F = st.lv[l];
     AmgLevel& C = st.lv[l + 1];
@@ -100,15 +102,28 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, 
   if (l == 0 && st.gnn_smoother && ctx->gnn)
     gnn_apply_device(ctx, b, nullptr, ctx->gnn->scal.p + 4, x, nullptr, fl);
   else
-    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, nullptr, x, true, fl);
-  amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
-  amg_residual(s, 4L * A.n, b, A.r.p, A.r.p, fl);
+    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, nullptr, x, 0, fl);
+  if (l == 0) {  // finest level: FP16 matrix, residual fused into the product
+    amg_spmv_res_h(s, A.n, rp, cp, st.val0h.p, x, b, A.r.p, fl);
+    ctx->launches += 2;
+  } else {
+    amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
+    amg_residual(s, 4L * A.n, b, A.r.p, A.r.p, fl);
+    ctx->launches += 3;
+  }
   amg_restrict(s, C.n, A.aggPtr.p, A.aggList.p, A.r.p, C.b.p, fl);
-  ctx->launches += 4;
+  ctx->launches += 1;
+  if (l == 0 && !ctx->use_graphs) phase_mark(ctx, PH_CYC_COARSE);
   vcycle(ctx, l + 1, Val0, C.b.p, C.x.p, fl);
+  if (l == 0 && !ctx->use_graphs) phase_mark(ctx, PH_CYC_PRECOND);
   amg_prolong_add(s, A.n, A.agg.p, C.x.p, x, fl);
-  amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
-  amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, false, fl);
+  if (l == 0) {
+    amg_spmv_res_h(s, A.n, rp, cp, st.val0h.p, x, b, A.r.p, fl);
+    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, 2, fl);
+  } else {
+    amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
+    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, 1, fl);
+  }
   ctx->launches += 3;
 }
 }  // namespace

@@ -22,6 +22,7 @@ struct AmgLevel {
 
 struct AmgState {
   std::vector<AmgLevel> lv;
+  DevBuf<uint16_t> val0h;       // FP16 copy of the finest level's (scaled) matrix
   float omega = 0.7f;           // damping of the block-Jacobi smoother
   int coarse_sweeps = 30;       // block-Jacobi sweeps on the coarsest level
   bool gnn_smoother = false;    // pre-smooth on level 0 with the learned network
@@ -37,8 +38,14 @@ void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx,
 void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, float* dinv);
 // the kernels below take the restart cycle's flag word (may be null) and return at
 // once when the cycle has stopped
+// mode 0: x = omega D^-1 b; 1: x += omega D^-1 (b - Ax); 2: x += omega D^-1 r, r passed as Ax
 void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
-                bool first, const int* flags);
+                int mode, const int* flags);
+// FP16 copy (bit patterns) of m floats, saturated to the finite half range
+void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h);
+// r = b - A x with an FP16 block matrix
+void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
+                    const float* b, float* r, const int* flags);
 void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags);
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags);

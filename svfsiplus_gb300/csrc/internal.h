@@ -100,6 +100,34 @@ struct KrylovWork {
 
 struct AmgState;
 
+// Phases of a Newton step timed with CUDA events on the library's stream when phase
+// timing is on (svgpu_phase_timing): consecutive marks bound contiguous intervals.
+enum Phase {
+  PH_ASSEMBLY = 0,   // element assembly and the outlet's backflow terms
+  PH_PRECOND = 1,    // Dirichlet mask, diagonal scaling of Val and R
+  PH_AMG_SETUP = 2,  // Galerkin coarse operators and diagonal-block inverses
+  PH_GUESS = 3,      // learned initial guess and its check
+  PH_RESTART = 4,    // restart residual R - K X, its norm, start vector
+  PH_CYCLES = 5,     // Arnoldi / flexible cycles, back substitution, X update
+  PH_OTHER = 6,      // predictor, corrector, pair storage, copies
+  // inside the cycles, marked only when the cycles run as individual launches
+  // (SVGPU_GRAPHS=0); with graphs the whole cycle counts as PH_CYCLES
+  PH_CYC_PRECOND = 7,  // right preconditioner of the flexible cycles (network, or the
+                       // finest level of the V-cycle)
+  PH_CYC_SPMV = 8,     // Krylov operator product
+  PH_CYC_ORTHO = 9,    // Gram-Schmidt dots, Givens, basis update
+  PH_CYC_COARSE = 10,  // coarse levels of the V-cycle and the coarsest solve
+  PH_COUNT = 11
+};
+
+struct PhaseTimer {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;                 // recycled events
+  std::vector<std::pair<int, cudaEvent_t>> marks;  // (phase starting here, event)
+  double ms[PH_COUNT] = {};
+  long long intervals[PH_COUNT] = {};
+};
+
 // Learned preconditioner state (k_gnn.cu kernels).
 struct GnnState {
   int nNo = 0;
@@ -160,6 +188,7 @@ struct svgpu_ctx {
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
+  svgpu::PhaseTimer phases;
   svgpu::DevBuf<double> cg_part, cg_d;  // CG: per-CTA partial sums, device scalars
   svgpu::DevBuf<int> cg_f;              // CG: stop, last_i, suc, next iteration
   std::unique_ptr<svgpu::GnnState> gnn;
@@ -220,6 +249,8 @@ inline int grid_for(long n, int block, int cap = 152 * 16) {
 }
 
 // ---- k_krylov.cu -------------------------------------------------------------
+// phase timing: start `phase` here (PH_COUNT: stop); no-op unless timing is on
+void phase_mark(svgpu_ctx* ctx, int phase);
 // k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
 int cg_parts(long n);
 void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,

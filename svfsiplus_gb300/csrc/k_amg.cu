@@ -2,6 +2,8 @@
 // summation of fine blocks, 4x4 diagonal-block inverses, damped block-Jacobi sweeps,
 // restriction (sum over an aggregate) and prolongation (injection), all FP32 on the
 // Jacobi-scaled system of the mixed path.
+#include <cuda_fp16.h>
+
 #include "amg.h"
 
 namespace svgpu {
@@ -67,9 +69,10 @@ __global__ void diag_inv_kernel(int n, const int* __restrict__ diagPtr, const fl
     for (int c = 0; c < 4; c++) dinv[16L * i + 4 * r + c] = (float)a[r][4 + c];
 }
 
-// x <- x + omega D^-1 (b - Ax)   (first: x <- omega D^-1 b)
+// mode 0: x <- omega D^-1 b;  mode 1: x <- x + omega D^-1 (b - Ax);
+// mode 2: x <- x + omega D^-1 r with the residual r given in place of Ax (b unused)
 __global__ void jacobi_kernel(int n, float omega, const float* __restrict__ dinv, const float* __restrict__ b,
-                              const float* __restrict__ Ax, float* __restrict__ x, int first,
+                              const float* __restrict__ Ax, float* __restrict__ x, int mode,
                               const int* flags) {
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,17 +80,63 @@ __global__ void jacobi_kernel(int n, float omega, const float* __restrict__ dinv
   const int r = (int)(t & 3);
   if (i >= n) return;
   const float4 rw = *reinterpret_cast<const float4*>(dinv + 16 * i + 4 * r);
-  const float4 bb = *reinterpret_cast<const float4*>(b + 4 * i);
-  float4 res = bb;
-  if (!first) {
-    const float4 ax = *reinterpret_cast<const float4*>(Ax + 4 * i);
-    res.x -= ax.x;
-    res.y -= ax.y;
-    res.z -= ax.z;
-    res.w -= ax.w;
+  float4 res;
+  if (mode == 2) {
+    res = *reinterpret_cast<const float4*>(Ax + 4 * i);
+  } else {
+    res = *reinterpret_cast<const float4*>(b + 4 * i);
+    if (mode == 1) {
+      const float4 ax = *reinterpret_cast<const float4*>(Ax + 4 * i);
+      res.x -= ax.x;
+      res.y -= ax.y;
+      res.z -= ax.z;
+      res.w -= ax.w;
+    }
   }
   const float d = rw.x * res.x + rw.y * res.y + rw.z * res.z + rw.w * res.w;
-  x[4 * i + r] = first ? omega * d : x[4 * i + r] + omega * d;
+  x[4 * i + r] = mode == 0 ? omega * d : x[4 * i + r] + omega * d;
+}
+
+// FP16 copy of the finest level's matrix for the V-cycle products, saturated at the
+// largest finite half value
+__global__ void to_half_kernel(long m, const float* __restrict__ v, __half* __restrict__ h) {
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (long)gridDim.x * blockDim.x)
+    h[k] = __float2half_rn(fminf(fmaxf(v[k], -65504.f), 65504.f));
+}
+
+// r = b - A x with the FP16 matrix: 2 threads per block row, each one 16-byte load of
+// two rows of the block (8 halves) and one 16-byte load of x per block, FP32
+// accumulation
+__global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __restrict__ rowPtr,
+                                                         const int* __restrict__ colPtr,
+                                                         const __half* __restrict__ val,
+                                                         const float* __restrict__ x, const float* __restrict__ b,
+                                                         float* __restrict__ r, const int* flags) {
+  if (stopped(flags)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 1;
+  const int q = (int)(t & 1);
+  if (row >= n) return;
+  float a0 = 0.f, a1 = 0.f;
+  for (int k = rowPtr[row]; k < rowPtr[row + 1]; k++) {
+    const int col = __ldg(colPtr + k);
+    const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(val + 16L * k + 8 * q));
+    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
+    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
+    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
+    a0 = fmaf(v0.x, xv.x, a0);
+    a0 = fmaf(v0.y, xv.y, a0);
+    a0 = fmaf(v1.x, xv.z, a0);
+    a0 = fmaf(v1.y, xv.w, a0);
+    a1 = fmaf(v2.x, xv.x, a1);
+    a1 = fmaf(v2.y, xv.y, a1);
+    a1 = fmaf(v3.x, xv.z, a1);
+    a1 = fmaf(v3.y, xv.w, a1);
+  }
+  const float2 bb = *reinterpret_cast<const float2*>(b + 4 * row + 2 * q);
+  *reinterpret_cast<float2*>(r + 4 * row + 2 * q) = make_float2(bb.x - a0, bb.y - a1);
 }
 
 // r = b - Ax; r may be the same array as Ax
@@ -152,8 +201,18 @@ void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, f
 }
 
 void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
-                bool first, const int* flags) {
-  jacobi_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, omega, dinv, b, Ax, x, first ? 1 : 0, flags);
+                int mode, const int* flags) {
+  jacobi_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, omega, dinv, b, Ax, x, mode, flags);
+}
+
+void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h) {
+  to_half_kernel<<<grid_for(m, 256), 256, 0, s>>>(m, v, reinterpret_cast<__half*>(h));
+}
+
+void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
+                    const float* b, float* r, const int* flags) {
+  spmv_res_h_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+      n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, b, r, flags);
 }
 
 void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags) {

@@ -571,6 +571,78 @@ __global__ void __launch_bounds__(256) multidot32_kernel(long n, int m, const fl
   }
 }
 
+// Partial <V_j, w> over FP32 vectors read as float4: every thread keeps JB FP32
+// accumulators (JB independent 16-byte loads in flight per step), FP64 across threads
+// and CTAs.  n4 = n / 4 float4 entries per vector, ldv4 = ldv / 4.
+template <int JB>
+__global__ void __launch_bounds__(256) multidot32v4_kernel(long n4, int m, const float4* __restrict__ V, long ldv4,
+                                                           const float4* __restrict__ w, double* __restrict__ partial,
+                                                           const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ double red[JB][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (int j0 = 0; j0 < m; j0 += JB) {
+    float acc[JB];
+#pragma unroll
+    for (int q = 0; q < JB; q++) acc[q] = 0.f;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += stride) {
+      const float4 wk = w[k];
+#pragma unroll
+      for (int q = 0; q < JB; q++) {
+        if (j0 + q < m) {
+          const float4 v = __ldcs(V + (long)(j0 + q) * ldv4 + k);
+          acc[q] = fmaf(v.x, wk.x, fmaf(v.y, wk.y, fmaf(v.z, wk.z, fmaf(v.w, wk.w, acc[q]))));
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < JB; q++) {
+      double v = (double)acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < JB && j0 + (int)threadIdx.x < m) {
+      double v = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += red[threadIdx.x][q];
+      partial[(long)blockIdx.x * m + j0 + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// u_{i+1} <- (u_{i+1} - sum_j h_j u_j) / h_{i+1}, float4 per thread, the j loop
+// unrolled so that several basis loads are in flight
+__global__ void __launch_bounds__(256) cgs_update32v4_kernel(long n4, int i, float4* __restrict__ V, long ldv4,
+                                                             const double* __restrict__ hcol, const int* flags) {
+  if (stopped(flags)) return;
+  __shared__ float hs[256];
+  __shared__ float rinv;
+  for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (float)hcol[j];
+  if (threadIdx.x == 0) rinv = (float)(1.0 / hcol[i + 1]);
+  __syncthreads();
+  float4* w = V + (long)(i + 1) * ldv4;
+  const float ri = rinv;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (long)gridDim.x * blockDim.x) {
+    float4 acc = w[k];
+#pragma unroll 8
+    for (int j = 0; j <= i; j++) {
+      const float4 v = __ldcs(V + (long)j * ldv4 + k);
+      const float h = hs[j];
+      acc.x = fmaf(-h, v.x, acc.x);
+      acc.y = fmaf(-h, v.y, acc.y);
+      acc.z = fmaf(-h, v.z, acc.z);
+      acc.w = fmaf(-h, v.w, acc.w);
+    }
+    acc.x *= ri;
+    acc.y *= ri;
+    acc.z *= ri;
+    acc.w *= ri;
+    w[k] = acc;
+  }
+}
+
 __global__ void __launch_bounds__(256) cgs_update32_kernel(long n, int i, float* __restrict__ V, long ldv,
                                                            const double* __restrict__ hcol, const int* flags) {
   if (stopped(flags)) return;
@@ -647,7 +719,11 @@ void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int*
 int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
                       int sm_count, const int* flags) {
   const int ctas = multidot_ctas(n, sm_count);
-  if (m <= 8 * MD_JMAX)
+  const bool v4 = (n % 4 == 0) && (ldv % 4 == 0) && ((reinterpret_cast<uintptr_t>(V) | reinterpret_cast<uintptr_t>(w)) % 16 == 0);
+  if (v4)
+    multidot32v4_kernel<16><<<ctas, 256, 0, s>>>(n / 4, m, reinterpret_cast<const float4*>(V), ldv / 4,
+                                                 reinterpret_cast<const float4*>(w), partial, flags);
+  else if (m <= 8 * MD_JMAX)
     multidot2_kernel<float, float><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
   else
     multidot32_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
@@ -655,7 +731,12 @@ int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, c
 }
 
 void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, const double* hcol, const int* flags) {
-  cgs_update32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, i, V, ldv, hcol, flags);
+  const bool v4 = (n % 4 == 0) && (ldv % 4 == 0) && (reinterpret_cast<uintptr_t>(V) % 16 == 0);
+  if (v4)
+    cgs_update32v4_kernel<<<grid_for(n / 4, 256, 152 * 8), 256, 0, s>>>(n / 4, i, reinterpret_cast<float4*>(V),
+                                                                        ldv / 4, hcol, flags);
+  else
+    cgs_update32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, i, V, ldv, hcol, flags);
 }
 
 void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, const double* g, const int* flags,
