@@ -417,8 +417,13 @@ def run_study(args):
     from svfsiplus_gb300.mesh import named_pipe
     mesh = named_pipe(args.workload)
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
-    for path in args.study.split(","):
+    combos = [None] if not args.ml_options else [tuple(float(v) for v in c.split(",")) for c in
+                                                  args.ml_options.split(";")]
+    runs = [(p, c) for p in args.study.split(",") for c in combos]
+    for path, combo in runs:
         s, mode = make_solver(api, mesh, rowPtr, colPtr, path)
+        if combo:
+            s.ctx.multilevel_options(combo[0], int(combo[1]), int(combo[2]), int(combo[3]) if len(combo) > 3 else 1)
         s.ctx.phase_timing(True)
         for k in range(args.steps):
             if mode in (3, 4) and k == 2:
@@ -426,11 +431,12 @@ def run_study(args):
             t = time.perf_counter()
             st = s.step(U_MEAN, U_AMP, U_FREQ)
             dt = time.perf_counter() - t
-            print(json.dumps({"workload": args.workload, "path": path, "mode": mode, "step": k + 1, "s": round(dt, 3),
+            print(json.dumps({"workload": args.workload, "path": path, "mode": mode, "ml_options": combo,
+                              "step": k + 1, "s": round(dt, 3),
                               "newton": len(st), "its": [q["itr"] for q in st],
                               "rel": [float("%.2g" % (q["fNorm"] / max(q["iNorm"], 1e-300))) for q in st],
                               "iNorm": [float("%.3g" % q["iNorm"]) for q in st],
-                              "rejects": s.ctx.learned_rejects,
+                              "rejects": s.ctx.learned_rejects, "levels": s.ctx.multilevel_info(),
                               "phases_ms": {k: round(v[0], 2) for k, v in s.ctx.phase_times().items() if v[1]}}),
                   flush=True)
             if mode in (3, 4) and k < 2:
@@ -490,6 +496,8 @@ def main():
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     ap.add_argument("--study", default=None, help="comma-separated paths: per-step solver statistics")
     ap.add_argument("--spmv-only", action="store_true", help="only the SpMV roofline measurement")
+    ap.add_argument("--ml-options", default=None,
+                    help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     args = ap.parse_args()
     if args.impl == "reference":

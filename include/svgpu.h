@@ -205,6 +205,16 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
  * guesses and learned cycles that do not lower the FP64 residual are rejected (plain
  * cycles finish the solve). */
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
+/* Options of the multilevel preconditioner (modes 2-4): damping of the block-Jacobi
+ * smoother (default 0.7), block-Jacobi sweeps on a coarsest level too large for the
+ * dense inverse (30), the node count at or below which coarsening stops (256), and the
+ * finest level's pre-smoothing sweeps (1; 0 leaves it out, post-smoothing stays).  A
+ * coarsest level of at most 256 nodes is solved with its dense inverse.  The hierarchy
+ * is rebuilt at the next solve. */
+int svgpu_multilevel_options(svgpu_ctx* ctx, double omega, int coarse_sweeps, int coarsest_nodes, int pre_sweeps);
+/* The multilevel hierarchy built by the last solve: number of levels (0 before the
+ * first), and per level (up to cap) its node and block counts. */
+int svgpu_multilevel_info(svgpu_ctx* ctx, int* nlevels, int* nodes, long long* blocks, int cap);
 long long svgpu_learned_rejects(const svgpu_ctx* ctx);
 
 /* ---- phase timing (no reference counterpart: instrumentation of this library) --------
@@ -216,8 +226,9 @@ long long svgpu_learned_rejects(const svgpu_ctx* ctx);
  * pair storage); with the cycles launched one kernel at a time (environment
  * SVGPU_GRAPHS=0 at context creation) the flexible cycles are split further into
  * 7 right preconditioner (network, or the V-cycle's finest level), 8 operator product,
- * 9 Gram-Schmidt and Givens, 10 the V-cycle's coarse levels.
- * n: entries of ms / intervals (11); intervals may be NULL. */
+ * 9 Gram-Schmidt and Givens, 10 the V-cycle's coarse levels, 11 its two finest-level
+ * products, 12 its finest-level restriction and prolongation (7 then keeps the
+ * finest-level smoothing).  n: entries of ms / intervals (13); intervals may be NULL. */
 int svgpu_phase_timing(svgpu_ctx* ctx, int on);
 int svgpu_phase_times(svgpu_ctx* ctx, double* ms, long long* intervals, int n);
 

@@ -257,22 +257,35 @@ class Context:
         with the learned smoother (modes 1-3 act on the mixed-precision path)."""
         self._check(lib().svgpu_set_solver_mode(self._h, int(mode)), "set_solver_mode")
 
+    def multilevel_options(self, omega=0.7, coarse_sweeps=30, coarsest_nodes=256, pre_sweeps=1):
+        self._check(lib().svgpu_multilevel_options(self._h, C.c_double(omega), int(coarse_sweeps),
+                                                   int(coarsest_nodes), int(pre_sweeps)), "multilevel_options")
+
+    def multilevel_info(self):
+        """[(nodes, blocks)] per level of the hierarchy of the last multilevel solve."""
+        nl = C.c_int(0)
+        nodes = (C.c_int * 16)()
+        blocks = (C.c_longlong * 16)()
+        self._check(lib().svgpu_multilevel_info(self._h, C.byref(nl), nodes, blocks, 16), "multilevel_info")
+        return [(nodes[i], blocks[i]) for i in range(min(nl.value, 16))]
+
     @property
     def learned_rejects(self):
         lib().svgpu_learned_rejects.restype = C.c_longlong
         return int(lib().svgpu_learned_rejects(self._h))
 
     PHASES = ("assembly", "precond", "amg_setup", "learned_guess", "restart", "cycles", "other",
-              "cycle_precond", "cycle_spmv", "cycle_ortho", "cycle_coarse")
+              "cycle_precond", "cycle_spmv", "cycle_ortho", "cycle_coarse", "vcycle_spmv", "vcycle_transfer")
 
     def phase_timing(self, on=True):
         self._check(lib().svgpu_phase_timing(self._h, int(bool(on))), "phase_timing")
 
     def phase_times(self):
         """Accumulated milliseconds and interval counts per phase since the last call."""
-        ms = (C.c_double * 11)()
-        cnt = (C.c_longlong * 11)()
-        self._check(lib().svgpu_phase_times(self._h, ms, cnt, 11), "phase_times")
+        n = len(self.PHASES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_longlong * n)()
+        self._check(lib().svgpu_phase_times(self._h, ms, cnt, n), "phase_times")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.PHASES)}
 
     def set_dirichlet(self, nodes):

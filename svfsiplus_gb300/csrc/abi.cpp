@@ -903,6 +903,33 @@ int svgpu_spar_mul(svgpu_ctx* ctx, int dof, const double* K, const double* U, do
   return SVGPU_OK;
 }
 
+int svgpu_multilevel_options(svgpu_ctx* ctx, double omega, int coarse_sweeps, int coarsest_nodes, int pre_sweeps) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (!(omega > 0.0 && omega <= 2.0) || coarse_sweeps < 1 || coarse_sweeps > 1000 || coarsest_nodes < 1 ||
+      coarsest_nodes > 100000 || pre_sweeps < 0 || pre_sweeps > 1)
+    return set_err(ctx, SVGPU_EINVAL,
+                   "multilevel_options: omega in (0,2], sweeps 1..1000, coarsest 1..100000, pre_sweeps 0 or 1");
+  ctx->ml_pre_sweeps = pre_sweeps;
+  cudaSetDevice(ctx->device);
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->ml_omega = (float)omega;
+  ctx->ml_coarse_sweeps = coarse_sweeps;
+  ctx->ml_coarsest = coarsest_nodes;
+  graphs().erase(ctx);  // the cycle graphs hold the old hierarchy's buffers
+  ctx->amg.reset();     // rebuilt at the next solve
+  return SVGPU_OK;
+}
+
+int svgpu_multilevel_info(svgpu_ctx* ctx, int* nlevels, int* nodes, long long* blocks, int cap) {
+  if (!ctx || !nlevels) return SVGPU_EINVAL;
+  *nlevels = ctx->amg ? (int)ctx->amg->lv.size() : 0;
+  for (int l = 0; l < *nlevels && l < cap; l++) {
+    if (nodes) nodes[l] = ctx->amg->lv[l].n;
+    if (blocks) blocks[l] = ctx->amg->lv[l].nnz;
+  }
+  return SVGPU_OK;
+}
+
 int svgpu_spar_mul_f32(svgpu_ctx* ctx, const float* K, const float* U, float* KU) {
   if (!ctx) return SVGPU_EINVAL;
   cudaSetDevice(ctx->device);

@@ -23,6 +23,20 @@ struct AmgLevel {
 struct AmgState {
   std::vector<AmgLevel> lv;
   DevBuf<uint16_t> val0h;       // FP16 copy of the finest level's (scaled) matrix
+  // A P on the finest level (fine rows x aggregates), FP16 values summed from A's blocks:
+  // the residual after the coarse correction is r - (A P) x_c
+  int ap_nnz = 0;
+  DevBuf<int> apRow, apCol, apSumPtr, apSumIdx;
+  DevBuf<uint16_t> apValh;
+  int pre_sweeps = 1;           // finest-level pre-smoothing sweeps (0 or 1)
+  // dense inverse of the coarsest level (dense_N = 4 n unknowns, 0: block-Jacobi sweeps)
+  int dense_N = 0;
+  DevBuf<float> dense, colk, rowk;
+  DevBuf<int> piv;
+  cudaGraphExec_t gj_graph = nullptr;  // the Gauss-Jordan launches, captured once
+  ~AmgState() {
+    if (gj_graph) cudaGraphExecDestroy(gj_graph);
+  }
   float omega = 0.7f;           // damping of the block-Jacobi smoother
   int coarse_sweeps = 30;       // block-Jacobi sweeps on the coarsest level
   bool gnn_smoother = false;    // pre-smooth on level 0 with the learned network
@@ -32,6 +46,16 @@ int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int
 void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::vector<int>& colPtr,
                     const std::vector<int>& agg, std::vector<int>& cRow, std::vector<int>& cCol,
                     std::vector<int>& sumPtr, std::vector<int>& sumIdx);
+void ap_pattern(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, const std::vector<int>& agg,
+                std::vector<int>& apRow, std::vector<int>& apCol, std::vector<int>& sumPtr, std::vector<int>& sumIdx);
+// FP16 sums of fine blocks into the blocks of A P (sumPtr / sumIdx as from ap_pattern)
+void amg_ap_values(cudaStream_t s, int nb, const int* sumPtr, const int* sumIdx, const float* fineVal, uint16_t* apValh);
+// x += P xc and r <- r - (A P) xc on the finest level (FP16 A P)
+void amg_correct(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh, const int* agg,
+                 const float* xc, float* x, float* r, const int* flags);
+// x = P xc (no pre-smoothing) and r = b - (A P) xc
+void amg_correct_from_zero(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
+                           const int* agg, const float* xc, const float* b, float* x, float* r, const int* flags);
 
 // k_amg.cu
 void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal, float* coarseVal);
@@ -52,6 +76,14 @@ void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList,
 void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x, const int* flags);
 void amg_coarse_solve(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* dinv,
                       const float* b, float* x, float* y, float omega, int sweeps, const int* flags);
+// dense coarsest solve: expand the block-CSR level into M (N x N, zeroed by the caller),
+// Gauss-Jordan steps k = 0..N-1 then unscramble (M becomes the inverse), apply x = M b
+void amg_dense_build(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, long nnz, int N,
+                     float* M);
+void amg_gj_step(cudaStream_t s, int N, int k, float* M, float* colk, float* rowk, int* piv);
+void amg_gj_unscramble(cudaStream_t s, int N, float* M, const int* piv);
+void amg_dense_apply(cudaStream_t s, int N, const float* Minv, const float* b, float* x, const int* flags);
+constexpr int kDenseMaxNodes = 256;  // coarsest levels up to this size are inverted densely
 // amg.cpp
 struct svgpu_ctx_fwd;
 int amg_build(svgpu_ctx* ctx);

@@ -70,4 +70,33 @@ void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::ve
   for (int c = 0; c < nc; c++) cRow[c + 1] += cRow[c];
 }
 
+// Pattern of A P (fine rows x coarse columns) for P the aggregate injection: row i
+// holds one block per distinct aggregate among its columns (ascending), and for every
+// such block the list of A's blocks of row i whose column lies in that aggregate.
+void ap_pattern(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, const std::vector<int>& agg,
+                std::vector<int>& apRow, std::vector<int>& apCol, std::vector<int>& sumPtr, std::vector<int>& sumIdx) {
+  apRow.assign(n + 1, 0);
+  apCol.clear();
+  sumPtr.clear();
+  sumIdx.clear();
+  sumIdx.reserve(rowPtr[n]);
+  std::vector<std::pair<int, int>> row;
+  for (int i = 0; i < n; i++) {
+    row.clear();
+    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++) row.emplace_back(agg[colPtr[k]], k);
+    std::sort(row.begin(), row.end());
+    int last = -1;
+    for (auto& e : row) {
+      if (e.first != last) {
+        apCol.push_back(e.first);
+        sumPtr.push_back((int)sumIdx.size());
+        last = e.first;
+      }
+      sumIdx.push_back(e.second);
+    }
+    apRow[i + 1] = (int)apCol.size();
+  }
+  sumPtr.push_back((int)sumIdx.size());
+}
+
 }  // namespace svgpu

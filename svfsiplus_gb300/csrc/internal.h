@@ -117,7 +117,9 @@ enum Phase {
   PH_CYC_SPMV = 8,     // Krylov operator product
   PH_CYC_ORTHO = 9,    // Gram-Schmidt dots, Givens, basis update
   PH_CYC_COARSE = 10,  // coarse levels of the V-cycle and the coarsest solve
-  PH_COUNT = 11
+  PH_VC_SPMV = 11,     // the V-cycle's two finest-level products (FP16 matrix)
+  PH_VC_TRANSFER = 12, // the V-cycle's finest-level restriction and prolongation
+  PH_COUNT = 13
 };
 
 struct PhaseTimer {
@@ -162,6 +164,11 @@ struct svgpu_ctx {
   // restart cycles as CUDA graphs (default) or as individual launches (environment
   // SVGPU_GRAPHS=0 at context creation: per-kernel profilers see plain launches)
   bool use_graphs = true;
+  // multilevel preconditioner options (svgpu_multilevel_options)
+  float ml_omega = 0.7f;
+  int ml_coarse_sweeps = 30;
+  int ml_coarsest = 256;
+  int ml_pre_sweeps = 1;
 
   // linear-system layout (fsils_lhs_create)
   int nNo = 0, nnz = 0, nFaces = 0;

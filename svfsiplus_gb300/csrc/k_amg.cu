@@ -118,14 +118,11 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   const int q = (int)(t & 1);
   if (row >= n) return;
   float a0 = 0.f, a1 = 0.f;
-  for (int k = rowPtr[row]; k < rowPtr[row + 1]; k++) {
-    const int col = __ldg(colPtr + k);
-    const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(val + 16L * k + 8 * q));
+  auto blk = [&](const uint4& raw, const float4& xv) {
     const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
     const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
     const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
     const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
-    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
     a0 = fmaf(v0.x, xv.x, a0);
     a0 = fmaf(v0.y, xv.y, a0);
     a0 = fmaf(v1.x, xv.z, a0);
@@ -134,6 +131,25 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
     a1 = fmaf(v2.y, xv.y, a1);
     a1 = fmaf(v3.x, xv.z, a1);
     a1 = fmaf(v3.y, xv.w, a1);
+  };
+  const int e = rowPtr[row + 1];
+  int k = rowPtr[row];
+  for (; k + 3 < e; k += 4) {  // four blocks per step: all loads issued before use
+    int c[4];
+    uint4 raw[4];
+    float4 xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) raw[u] = __ldcs(reinterpret_cast<const uint4*>(val + 16L * (k + u) + 8 * q));
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) blk(raw[u], xv[u]);
+  }
+  for (; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    blk(__ldcs(reinterpret_cast<const uint4*>(val + 16L * k + 8 * q)), *reinterpret_cast<const float4*>(x + 4L * col));
   }
   const float2 bb = *reinterpret_cast<const float2*>(b + 4 * row + 2 * q);
   *reinterpret_cast<float2*>(r + 4 * row + 2 * q) = make_float2(bb.x - a0, bb.y - a1);
@@ -177,7 +193,26 @@ __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict_
   const int r = (int)(t & 3);
   if (row >= n) return;
   float acc = 0.f;
-  for (int k = rowPtr[row]; k < rowPtr[row + 1]; k++) {
+  const int e = rowPtr[row + 1];
+  int k = rowPtr[row];
+  for (; k + 3 < e; k += 4) {  // four blocks per step: all loads issued before use
+    int c[4];
+    float4 v[4], xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) v[u] = *reinterpret_cast<const float4*>(val + 16L * (k + u) + 4 * r);
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      acc = fmaf(v[u].x, xv[u].x, acc);
+      acc = fmaf(v[u].y, xv[u].y, acc);
+      acc = fmaf(v[u].z, xv[u].z, acc);
+      acc = fmaf(v[u].w, xv[u].w, acc);
+    }
+  }
+  for (; k < e; k++) {
     const int col = __ldg(colPtr + k);
     const float4 v = *reinterpret_cast<const float4*>(val + 16L * k + 4 * r);
     const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
@@ -189,7 +224,84 @@ __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict_
   y[4 * row + r] = acc;
 }
 
+// A P block b, entry e: FP16 of the sum of entry e over the listed fine blocks
+__global__ void ap_values_kernel(int nb, const int* __restrict__ sumPtr, const int* __restrict__ sumIdx,
+                                 const float* __restrict__ fv, __half* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 16L * nb) return;
+  const long b = t >> 4;
+  const int e = (int)(t & 15);
+  float s = 0.f;
+  for (int p = sumPtr[b]; p < sumPtr[b + 1]; p++) s += fv[16L * sumIdx[p] + e];
+  out[t] = __float2half_rn(fminf(fmaxf(s, -65504.f), 65504.f));
+}
+
+// Coarse correction on the finest level, 2 threads per node (rows 2q, 2q+1 of its
+// blocks): x += P xc (or x = P xc) and r -= (A P) xc (or r = b - (A P) xc)
+__global__ void __launch_bounds__(256) correct_kernel(int n, const int* __restrict__ apRow,
+                                                      const int* __restrict__ apCol,
+                                                      const __half* __restrict__ apVal,
+                                                      const int* __restrict__ agg, const float* __restrict__ xc,
+                                                      const float* __restrict__ b, float* __restrict__ x,
+                                                      float* __restrict__ r, int from_zero, const int* flags) {
+  if (stopped(flags)) return;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 1;
+  const int q = (int)(t & 1);
+  if (row >= n) return;
+  float a0 = 0.f, a1 = 0.f;
+  for (int k = apRow[row]; k < apRow[row + 1]; k++) {
+    const int col = __ldg(apCol + k);
+    const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(apVal + 16L * k + 8 * q));
+    const float4 xv = *reinterpret_cast<const float4*>(xc + 4L * col);
+    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
+    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
+    a0 = fmaf(v0.x, xv.x, a0);
+    a0 = fmaf(v0.y, xv.y, a0);
+    a0 = fmaf(v1.x, xv.z, a0);
+    a0 = fmaf(v1.y, xv.w, a0);
+    a1 = fmaf(v2.x, xv.x, a1);
+    a1 = fmaf(v2.y, xv.y, a1);
+    a1 = fmaf(v3.x, xv.z, a1);
+    a1 = fmaf(v3.y, xv.w, a1);
+  }
+  const long o = 4 * row + 2 * q;
+  const float2 pc = *reinterpret_cast<const float2*>(xc + 4L * agg[row] + 2 * q);
+  float2 xr, rr;
+  if (from_zero) {
+    xr = pc;
+    const float2 bb = *reinterpret_cast<const float2*>(b + o);
+    rr = make_float2(bb.x - a0, bb.y - a1);
+  } else {
+    const float2 xo = *reinterpret_cast<const float2*>(x + o);
+    const float2 ro = *reinterpret_cast<const float2*>(r + o);
+    xr = make_float2(xo.x + pc.x, xo.y + pc.y);
+    rr = make_float2(ro.x - a0, ro.y - a1);
+  }
+  *reinterpret_cast<float2*>(x + o) = xr;
+  *reinterpret_cast<float2*>(r + o) = rr;
+}
+
 }  // namespace
+
+void amg_ap_values(cudaStream_t s, int nb, const int* sumPtr, const int* sumIdx, const float* fineVal, uint16_t* apValh) {
+  ap_values_kernel<<<(unsigned)((16L * nb + 255) / 256), 256, 0, s>>>(nb, sumPtr, sumIdx, fineVal,
+                                                                      reinterpret_cast<__half*>(apValh));
+}
+
+void amg_correct(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh, const int* agg,
+                 const float* xc, float* x, float* r, const int* flags) {
+  correct_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+      n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, nullptr, x, r, 0, flags);
+}
+
+void amg_correct_from_zero(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
+                           const int* agg, const float* xc, const float* b, float* x, float* r, const int* flags) {
+  correct_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+      n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, b, x, r, 1, flags);
+}
 
 void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal,
                   float* coarseVal) {
@@ -272,7 +384,164 @@ __global__ void __launch_bounds__(1024) coarse_solve_kernel(int n, const int* __
   }
 }
 
+// ---- dense direct solve of the coarsest level -------------------------------------
+// The coarsest operator (N = 4 n unknowns, N <= 1024) is expanded into a dense
+// row-major N x N matrix and inverted in place by Gauss-Jordan elimination with
+// partial pivoting (one pivot kernel and one elimination kernel per column, then the
+// column unscrambling in reverse pivot order); the V-cycle applies the inverse.
+
+// dense[(4i+r) N + 4j+c] = block (i,j) entry (r,c); the matrix was zeroed before
+__global__ void dense_fill_kernel(int n, const int* __restrict__ rowPtr, const int* __restrict__ colPtr,
+                                  const float* __restrict__ val, int N, float* __restrict__ M) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long k = t >> 4;
+  if (k >= rowPtr[n]) return;
+  const int e = (int)(t & 15), r = e >> 2, c = e & 3;
+  int lo = 0, hi = n;  // block row of k: rowPtr[row] <= k < rowPtr[row+1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (rowPtr[mid] <= k) lo = mid; else hi = mid;
+  }
+  M[(long)(4 * lo + r) * N + 4 * colPtr[k] + c] = val[16 * k + e];
+}
+
+// a row that is entirely zero (a Dirichlet dof removed on the whole aggregate) gets a
+// unit diagonal, as the diagonal-block inverses do
+__global__ void dense_fix_kernel(int N, float* __restrict__ M) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= N) return;
+  bool nz = false;
+  for (int j = lane; j < N; j += 32) nz = nz || M[(long)row * N + j] != 0.f;
+  nz = __any_sync(0xffffffffu, nz);
+  if (!nz && lane == 0) M[(long)row * N + row] = 1.f;
+}
+
+// step k: pivot row p = argmax_{i>=k} |M(i,k)| (smallest i on ties), swap rows k and p,
+// keep column k (colk) and the scaled pivot row (rowk) for the elimination kernel
+__global__ void __launch_bounds__(1024) gj_pivot_kernel(int N, int k, float* __restrict__ M, float* __restrict__ colk,
+                                                        float* __restrict__ rowk, int* __restrict__ piv) {
+  __shared__ float bv[32];
+  __shared__ int bi[32];
+  __shared__ int p_s;
+  __shared__ float pivot_s;
+  float best = -1.f;
+  int bidx = N;
+  for (int i = k + threadIdx.x; i < N; i += blockDim.x) {
+    const float a = fabsf(M[(long)i * N + k]);
+    if (a > best) {
+      best = a;
+      bidx = i;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ob = __shfl_down_sync(0xffffffffu, best, o);
+    const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
+    if (ob > best || (ob == best && oi < bidx)) {
+      best = ob;
+      bidx = oi;
+    }
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    bv[w] = best;
+    bi[w] = bidx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = -1.f;
+    int p = k;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++)
+      if (bv[q] > b || (bv[q] == b && bi[q] < p)) {
+        b = bv[q];
+        p = bi[q];
+      }
+    if (p >= N) p = k;
+    p_s = p;
+    piv[k] = p;
+  }
+  __syncthreads();
+  const int p = p_s;
+  if (p != k)
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const float a = M[(long)k * N + j];
+      M[(long)k * N + j] = M[(long)p * N + j];
+      M[(long)p * N + j] = a;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float pv = M[(long)k * N + k];
+    if (!(fabsf(pv) > 1e-30f)) pv = 1.f;  // singular column: leave the unknown unscaled
+    pivot_s = pv;
+  }
+  __syncthreads();
+  const float pv = pivot_s;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) colk[i] = M[(long)i * N + k];
+  __syncthreads();  // column k is read before row k is overwritten
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    const float v = (j == k) ? 1.f / pv : M[(long)k * N + j] / pv;
+    rowk[j] = v;
+    M[(long)k * N + j] = v;
+  }
+}
+
+__global__ void gj_elim_kernel(int N, int k, float* __restrict__ M, const float* __restrict__ colk,
+                               const float* __restrict__ rowk) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)N * N) return;
+  const int i = (int)(t / N), j = (int)(t - (long)i * N);
+  if (i == k) return;
+  const float f = colk[i];
+  M[t] = (j == k) ? -f * rowk[k] : M[t] - f * rowk[j];
+}
+
+// undo the row interchanges on the inverse: swap columns k and piv[k], k = N-1 .. 0
+__global__ void __launch_bounds__(1024) gj_unscramble_kernel(int N, float* __restrict__ M, const int* __restrict__ piv) {
+  for (int k = N - 1; k >= 0; k--) {
+    const int p = piv[k];
+    if (p != k)
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float a = M[(long)i * N + k];
+        M[(long)i * N + k] = M[(long)i * N + p];
+        M[(long)i * N + p] = a;
+      }
+    __syncthreads();
+  }
+}
+
+// x = Minv b, one warp per row
+__global__ void dense_apply_kernel(int N, const float* __restrict__ Minv, const float* __restrict__ b,
+                                   float* __restrict__ x, const int* flags) {
+  if (stopped(flags)) return;
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= N) return;
+  float acc = 0.f;
+  for (int j = lane; j < N; j += 32) acc = fmaf(Minv[(long)row * N + j], b[j], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[row] = acc;
+}
+
 }  // namespace
+
+void amg_dense_build(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, long nnz, int N,
+                     float* M) {
+  dense_fill_kernel<<<(unsigned)((16L * nnz + 255) / 256), 256, 0, s>>>(n, rowPtr, colPtr, val, N, M);
+  dense_fix_kernel<<<(N + 7) / 8, 256, 0, s>>>(N, M);
+}
+
+void amg_gj_step(cudaStream_t s, int N, int k, float* M, float* colk, float* rowk, int* piv) {
+  gj_pivot_kernel<<<1, 1024, 0, s>>>(N, k, M, colk, rowk, piv);
+  gj_elim_kernel<<<(unsigned)(((long)N * N + 255) / 256), 256, 0, s>>>(N, k, M, colk, rowk);
+}
+
+void amg_gj_unscramble(cudaStream_t s, int N, float* M, const int* piv) {
+  gj_unscramble_kernel<<<1, 1024, 0, s>>>(N, M, piv);
+}
+
+void amg_dense_apply(cudaStream_t s, int N, const float* Minv, const float* b, float* x, const int* flags) {
+  dense_apply_kernel<<<(N + 7) / 8, 256, 0, s>>>(N, Minv, b, x, flags);
+}
 
 void amg_coarse_solve(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* dinv,
                       const float* b, float* x, float* y, float omega, int sweeps, const int* flags) {

@@ -40,7 +40,29 @@ __global__ void __launch_bounds__(256) spmv4_f64_kernel(int nNo, const int* __re
   if (row >= nNo) return;
   const int s = rowPtr[row], e = rowPtr[row + 1];
   double acc = 0.0;
-  for (int k = s; k < e; k++) {
+  int k = s;
+  // four blocks per step: their column indices, values and x entries are loaded
+  // before any is used, so a thread waits for two memory latencies per four blocks
+  for (; k + 3 < e; k += 4) {
+    int c[4];
+    double2 v0[4], v1[4], x0[4], x1[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      v0[u] = ld_stream2(Val + 16L * (k + u) + 4 * r);
+      v1[u] = ld_stream2(Val + 16L * (k + u) + 4 * r + 2);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      x0[u] = *reinterpret_cast<const double2*>(x + 4L * c[u]);
+      x1[u] = *reinterpret_cast<const double2*>(x + 4L * c[u] + 2);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      acc = acc + v0[u].x * x0[u].x + v0[u].y * x0[u].y + v1[u].x * x1[u].x + v1[u].y * x1[u].y;
+  }
+  for (; k < e; k++) {
     const int col = __ldg(colPtr + k);
     const double2 v0 = ld_stream2(Val + 16L * k + 4 * r);
     const double2 v1 = ld_stream2(Val + 16L * k + 4 * r + 2);
@@ -500,7 +522,25 @@ __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __re
   if (row >= nNo) return;
   const int s = rowPtr[row], e = rowPtr[row + 1];
   float acc = 0.f;
-  for (int k = s; k < e; k++) {
+  int k = s;
+  for (; k + 3 < e; k += 4) {  // four blocks per step, loads first (see spmv4_f64_kernel)
+    int c[4];
+    float4 v[4], xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) v[u] = __ldcs(reinterpret_cast<const float4*>(Val + 16L * (k + u) + 4 * r));
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      acc = fmaf(v[u].x, xv[u].x, acc);
+      acc = fmaf(v[u].y, xv[u].y, acc);
+      acc = fmaf(v[u].z, xv[u].z, acc);
+      acc = fmaf(v[u].w, xv[u].w, acc);
+    }
+  }
+  for (; k < e; k++) {
     const int col = __ldg(colPtr + k);
     const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
     const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
