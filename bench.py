@@ -258,6 +258,39 @@ def run_spmv_only(args):
     print(json.dumps({"workload": args.workload, "path": args.path, "roofline": roof}), flush=True)
 
 
+def run_assembly_only(args):
+    """Only the fluid assembly (construct_fluid) of the workload, FP64 and mixed, timed
+    with CUDA events on the library's stream over `steps` calls (a small, graph-free
+    program for kernel profilers)."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(mesh.nNo, rowPtr, colPtr, 0)
+    ctx.mesh_create(mesh.x, mesh.ien)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    api.lib().svgpu_set_stream(ctx._h, api.C.c_void_p(stream.cuda_stream))
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    Ag = 0.1 * torch.randn((mesh.nNo, 4), dtype=torch.float64, device="cuda", generator=gen)
+    Yg = torch.randn((mesh.nNo, 4), dtype=torch.float64, device="cuda", generator=gen)
+    props = api.fluid_props()
+    out = {"workload": args.workload, "tets": int(mesh.nEl)}
+    for name, prec in (("fp64", api.SVGPU_FP64), ("mixed", api.SVGPU_MIXED)):
+        ctx.construct_fluid(props, Ag, Yg, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.construct_fluid(props, Ag, Yg, precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name + "_ms"] = e0.elapsed_time(e1) / args.steps
+    print(json.dumps(out), flush=True)
+
+
 def make_solver(api, mesh, rowPtr, colPtr, path, device=0):
     mode = PATH_MODES[path]
     precision = api.SVGPU_FP64 if mode < 0 else api.SVGPU_MIXED
@@ -496,6 +529,7 @@ def main():
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     ap.add_argument("--study", default=None, help="comma-separated paths: per-step solver statistics")
     ap.add_argument("--spmv-only", action="store_true", help="only the SpMV roofline measurement")
+    ap.add_argument("--assembly-only", action="store_true", help="only the fluid assembly, FP64 and mixed")
     ap.add_argument("--ml-options", default=None,
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
@@ -504,6 +538,8 @@ def main():
         run_reference(args)
     elif args.spmv_only:
         run_spmv_only(args)
+    elif args.assembly_only:
+        run_assembly_only(args)
     elif args.study:
         run_study(args)
     else:

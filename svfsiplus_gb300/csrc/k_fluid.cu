@@ -21,12 +21,12 @@ namespace svgpu {
 
 namespace {
 
-// utils::is_zero(v, 0) (utils.cpp:170-189)
+// utils::is_zero(v, 0) (utils.cpp:170-189): |v| / max(|v|, eps) < 10 eps.  With eps =
+// 2^-52 the division is an exact power-of-two scaling, so the test is exactly
+// |v| < 10 * 2^-104, which needs no FP64 division (and no FP64 at all for T = float).
 template <typename T>
 __device__ __forceinline__ bool is_zero_ref(T v) {
-  const double a = fabs((double)v);
-  const double eps = 2.220446049250313e-16;
-  return a / fmax(a, eps) < 10.0 * eps;
+  return fabs(v) < (T)4.930380657631324e-31;  // 10 * 2^-104, exact in float and double
 }
 
 template <typename T>
@@ -52,7 +52,7 @@ __device__ __forceinline__ void tet4_quad(Tet4Quad<T>& q) {
 }
 
 template <typename TV>
-__device__ __forceinline__ void add_block(TV* __restrict__ dst, const double (&blk)[16]);
+__device__ __forceinline__ void add_block(TV* __restrict__ dst, const TV (&blk)[16]);
 
 template <>
 __device__ __forceinline__ void add_block<double>(double* __restrict__ dst, const double (&blk)[16]) {
@@ -67,7 +67,7 @@ __device__ __forceinline__ void add_block<double>(double* __restrict__ dst, cons
 }
 
 template <>
-__device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const double (&blk)[16]) {
+__device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const float (&blk)[16]) {
   float4* d = reinterpret_cast<float4*>(dst);
 #pragma unroll
   for (int q = 0; q < 4; q++) {
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       const T NxNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
-      double blk[16];
+      TV blk[16];
 #pragma unroll
       for (int r = 0; r < 3; r++) {
 #pragma unroll
@@ -313,13 +313,13 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
             v = (c4mu + cTC) * Nx[r][a] * Nx[r][b] + c4mu * NxNx + wl * S[a][b];
           else
             v = c4mu * Nx[cc][a] * Nx[r][b] + cTC * Nx[r][a] * Nx[cc][b];
-          blk[4 * r + cc] = (double)v;
+          blk[4 * r + cc] = (TV)v;
         }
-        blk[4 * r + 3] = (double)(-(cSN * Nx[r][a] - wl * Nx[r][b] * Qv[a]));
+        blk[4 * r + 3] = (TV)(-(cSN * Nx[r][a] - wl * Nx[r][b] * Qv[a]));
       }
 #pragma unroll
-      for (int cc = 0; cc < 3; cc++) blk[12 + cc] = (double)(cSN * Nx[cc][b] - wl * Nx[cc][a] * Gv[b]);
-      blk[15] = (double)(cTM * NxNx);
+      for (int cc = 0; cc < 3; cc++) blk[12 + cc] = (TV)(cSN * Nx[cc][b] - wl * Nx[cc][a] * Gv[b]);
+      blk[15] = (TV)(cTM * NxNx);
       const long pos = rowbase + boff[16L * e + 4 * a + b];
       add_block<TV>(Val + 16 * pos, blk);
     }
@@ -378,8 +378,8 @@ __global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, con
     for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
     const int rowbase = rowPtr[nd[a]];
     for (int b = 0; b < 3; b++) {
-      double blk[16] = {0};
-      blk[0] = blk[5] = blk[10] = lk[a][b];
+      TV blk[16] = {0};
+      blk[0] = blk[5] = blk[10] = (TV)lk[a][b];
       const long pos = rowbase + boff[9L * e + 3 * a + b];
       add_block<TV>(Val + 16 * pos, blk);
     }
