@@ -31,7 +31,7 @@ enum svgpu_status {
 
 /* reference enums kept with their meaning (fils_struct.hpp:40-76, consts.h) */
 enum svgpu_bc_type { SVGPU_BC_DIR = 0, SVGPU_BC_NEU = 1 };            /* BcType */
-enum svgpu_ls_type { SVGPU_LS_GMRES = 2, SVGPU_LS_CG = 3, SVGPU_LS_FGMRES_LEARNED = 100 };
+enum svgpu_ls_type { SVGPU_LS_GMRES = 2, SVGPU_LS_CG = 3, SVGPU_LS_NS = 4, SVGPU_LS_FGMRES_LEARNED = 100 };
 enum svgpu_prec_type { SVGPU_PREC_NONE = 0, SVGPU_PREC_FSILS = 1 };  /* PreconditionerType */
 enum svgpu_precision { SVGPU_FP64 = 0, SVGPU_MIXED = 1 };
 

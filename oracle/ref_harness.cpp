@@ -344,7 +344,10 @@ int main(int argc, char** argv) {
     for (int a = 0; a < fa.nNo; a++) gN(a) = fa.gN(a);
     fsi_linear_solver::fsils_bc_create(com.lhs, f, fa.nNo, 3, fsi_linear_solver::BcType::BC_TYPE_Dir, gN, sVl);
   }
-  fsi_linear_solver::fsils_ls_create(eq.FSILS, fsi_linear_solver::LinearSolverType::LS_TYPE_GMRES,
+  // ls_type: "gmres" (default) or "ns" (ns_solver.cpp:167, with its GM/CG defaults)
+  const bool use_ns = P.count("ls_type") && P.at("ls_type") == "ns";
+  fsi_linear_solver::fsils_ls_create(eq.FSILS, use_ns ? fsi_linear_solver::LinearSolverType::LS_TYPE_NS
+                                                      : fsi_linear_solver::LinearSolverType::LS_TYPE_GMRES,
                                      getd("ls_rel_tol"), getd("ls_abs_tol"), geti("ls_max_itr"), geti("ls_krylov_dim"));
   FsilsLinearAlgebra fsils_la;
   eq.linear_algebra = &fsils_la;
@@ -412,7 +415,9 @@ int main(int argc, char** argv) {
       t_solve += std::chrono::duration<double>(t2 - t1).count();
       auto& RI = eq.FSILS.RI;
       log << "step " << cTS << " iter " << inner << " iNorm " << RI.iNorm << " fNorm " << RI.fNorm
-          << " itr " << RI.itr << " suc " << RI.suc << "\n";
+          << " itr " << RI.itr << " suc " << RI.suc;
+      if (use_ns) log << " gm_itr " << eq.FSILS.GM.itr << " cg_itr " << eq.FSILS.CG.itr << " dB " << RI.dB;
+      log << "\n";
       if (cTS == dump_step && inner == dump_iter) {
         write_raw(out + "/dX.bin", com.R.data(), (size_t)com.R.size());
         write_raw(out + "/Val_scaled.bin", com.Val.data(), (size_t)com.Val.size());

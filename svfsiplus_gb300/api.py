@@ -28,6 +28,7 @@ SVGPU_FP64, SVGPU_MIXED = 0, 1
 BC_TYPE_Dir, BC_TYPE_Neu = 0, 1
 LS_TYPE_GMRES = 2
 LS_TYPE_CG = 3
+LS_TYPE_NS = 4
 PREC_NONE, PREC_FSILS = 0, 1
 
 _lib = None
@@ -371,7 +372,8 @@ class PipeFluidSolver:
     time stepping through svgpu_fluid_step."""
 
     def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, sD=50, mItr=100, relTol=1e-8, absTol=1e-17,
-                 newton_min=3, newton_max=3, newton_tol=1e-11, precision=SVGPU_FP64, rowPtr=None, colPtr=None):
+                 newton_min=3, newton_max=3, newton_tol=1e-11, precision=SVGPU_FP64, rowPtr=None, colPtr=None,
+                 ls_type=LS_TYPE_GMRES):
         self.mesh = mesh
         self.props = props or fluid_props()
         self.ctx = Context(device)
@@ -382,7 +384,7 @@ class PipeFluidSolver:
         self.ctx.fsils_lhs_create(nNo, rowPtr, colPtr, 2)
         self.ctx.fsils_bc_create(0, mesh.faces["inlet"].gN, 3, BC_TYPE_Dir)
         self.ctx.fsils_bc_create(1, mesh.faces["wall"].gN, 3, BC_TYPE_Dir)
-        self.ctx.fsils_ls_create(LS_TYPE_GMRES, relTol, absTol, mItr, sD)
+        self.ctx.fsils_ls_create(ls_type, relTol, absTol, mItr, sD)
         self.ctx.mesh_create(mesh.x, mesh.ien)
         out = mesh.faces["outlet"]
         self.ctx.face_create(FACE_OUTLET, out.ien, out.gE)

@@ -118,6 +118,7 @@ int ensure_krylov(svgpu_ctx* ctx, long n, int sD) {
 struct CycleGraph {
   cudaGraphExec_t exec = nullptr;
   const void* val = nullptr;
+  const void* vbase = nullptr;  // the basis the graph was captured on
   long n = 0;
   int sD = 0, dof = 0;
   long long kernels = 0;  // kernel nodes in the graph (launches counted per graph launch)
@@ -129,7 +130,8 @@ struct CycleGraph {
 // Graphs of one context: the sD Arnoldi iterations of a restart cycle, one per kind
 // (0: FP64, 1: mixed precision).
 struct CtxGraphs {
-  std::unique_ptr<CycleGraph> g[5];  // 0: FP64, 1: mixed, 2..4: mixed flexible, by solver mode 1..3 (4 uses 3)
+  std::unique_ptr<CycleGraph> g[6];  // 0: FP64, 1: mixed, 2..4: mixed flexible, by solver mode 1..3 (4 uses 3),
+                                     // 5: the inner GMRES of the NS solver
 };
 std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
   static std::map<const svgpu_ctx*, CtxGraphs> g;
@@ -163,17 +165,17 @@ void enqueue_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
   }
 }
 
-int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
+int run_cycle(svgpu_ctx* ctx, int dof, const double* Val, int slot_index = 0) {
   if (!ctx->use_graphs) {
     enqueue_cycle(ctx, dof, Val);
     SVGPU_CUDA(ctx, cudaGetLastError());
     return SVGPU_OK;
   }
-  auto& slot = graphs()[ctx].g[0];
+  auto& slot = graphs()[ctx].g[slot_index];
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
-  if (!g.exec || g.val != Val || g.n != n || g.sD != ctx->kw.sD || g.dof != dof) {
+  if (!g.exec || g.val != Val || g.vbase != ctx->kw.V.p || g.n != n || g.sD != ctx->kw.sD || g.dof != dof) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -196,6 +198,7 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val) {
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
     cudaGraphDestroy(graph);
     g.val = Val;
+    g.vbase = ctx->kw.V.p;
     g.n = n;
     g.sD = ctx->kw.sD;
     g.dof = dof;
@@ -280,6 +283,77 @@ int gmres_device(svgpu_ctx* ctx, int dof, const double* Val, double* R, svgpu_ls
 }
 
 
+}  // namespace
+
+int svgpu::ensure_krylov_work(svgpu_ctx* ctx, long n, int sD) { return ensure_krylov(ctx, n, sD); }
+
+// gmres::gmres (gmres.cpp:91-280), the sub-solver of the NS solver: X = K^-1 R with R
+// kept, X0 = 0, the first restart from R itself, eps from the first residual norm;
+// iterations are added to *itr as the reference adds them to ls.itr.  ctx->kw must be
+// sized for n = nNo dof and the sub-solver's Krylov dimension.
+int svgpu::gmres_sub_device(svgpu_ctx* ctx, int dof, const double* K, const double* R, double* X, double relTol,
+                            double absTol, int mItr, int* itr, double* iNorm, double* fNorm) {
+  KrylovWork& kw = ctx->kw;
+  const long n = (long)ctx->nNo * dof;
+  const int sD = kw.sD;
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
+  double eps = 0.0, fN = 0.0;
+  for (int l = 0; l < mItr; l++) {
+    if (l == 0) {
+      launch_residual_init(ctx->stream, n, R, kw.V.p, kw.X.p, true, nullptr);
+      ctx->launches++;
+    } else {
+      spmv_any(ctx, dof, K, kw.X.p, kw.tmp.p, nullptr);
+      launch_residual_init(ctx->stream, n, R, kw.V.p, kw.X.p, false, kw.tmp.p);
+      ctx->launches++;
+      (*itr)++;
+    }
+    launch_norm2(ctx->stream, n, kw.V.p, kw.partial.p, kw.scal.p + 2, ctx->sm_count);
+    ctx->launches += 2;
+    if (l == 0) {
+      double nrm2 = 0.0;
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(&nrm2, kw.scal.p + 2, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      eps = std::sqrt(nrm2);
+      if (eps <= absTol) {  // X stays 0
+        SVGPU_CUDA(ctx, cudaMemsetAsync(X, 0, n * sizeof(double), ctx->stream));
+        if (iNorm) *iNorm = eps;
+        if (fNorm) *fNorm = eps;
+        return SVGPU_OK;
+      }
+      if (!std::isfinite(eps)) return set_err(ctx, SVGPU_ENAN, "non-finite residual");
+      if (iNorm) *iNorm = eps;
+      fN = eps;
+      eps = std::max(absTol, relTol * eps);
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    launch_scale_by_inv_norm(ctx->stream, n, kw.V.p, kw.scal.p + 2, kw.givens.p + 2 * sD, kw.flags.p);
+    ctx->launches++;
+    int rc;
+    if ((rc = run_cycle(ctx, dof, K, 5))) return rc;
+    launch_backsolve(ctx->stream, sD, kw.hess.p, kw.givens.p, kw.flags.p);
+    launch_xupdate(ctx->stream, n, sD, kw.V.p, n, kw.givens.p, kw.flags.p, kw.X.p);
+    ctx->launches += 2;
+    int flags[4];
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> err(sD + 1);
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(err.data(), kw.givens.p + 2 * sD, (sD + 1) * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int last = std::min(flags[1], sD - 1);
+    *itr += last + 1;
+    fN = std::fabs(err[last + 1]);
+    if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
+    if (flags[0]) break;
+  }
+  if (fNorm) *fNorm = fN;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(X, kw.X.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  return SVGPU_OK;
+}
+
+namespace {
+
 // FP32 Arnoldi cycle (mixed precision): same steps as enqueue_cycle on the FP32 basis.
 void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
   KrylovWork& kw = ctx->kw;
@@ -341,7 +415,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
-  if (!g.exec || g.val != Val32 || g.n != n || g.sD != ctx->kw.sD) {
+  if (!g.exec || g.val != Val32 || g.vbase != ctx->kw.V32.p || g.n != n || g.sD != ctx->kw.sD) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -365,6 +439,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
     cudaGraphDestroy(graph);
     g.val = Val32;
+    g.vbase = ctx->kw.V32.p;
     g.n = n;
     g.sD = ctx->kw.sD;
     g.dof = 4;
@@ -384,7 +459,7 @@ int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
-  if (!g.exec || g.val != Val32 || g.n != n || g.sD != ctx->kw.sD) {
+  if (!g.exec || g.val != Val32 || g.vbase != ctx->kw.V32.p || g.n != n || g.sD != ctx->kw.sD) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -407,6 +482,7 @@ int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
     SVGPU_CUDA(ctx, cudaGraphInstantiate(&g.exec, graph, 0));
     cudaGraphDestroy(graph);
     g.val = Val32;
+    g.vbase = ctx->kw.V32.p;
     g.n = n;
     g.sD = ctx->kw.sD;
     g.dof = 4;
@@ -617,6 +693,9 @@ int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, cons
   }
   if (ctx->lsType == SVGPU_LS_CG)
     rc = cg_device(ctx, dof, Val, R, st);
+  else if (ctx->lsType == SVGPU_LS_NS)
+    rc = dof == 4 ? ns_solve_device(ctx, Val, R, st)
+                  : set_err(ctx, SVGPU_EINVAL, "NS solver: dof must be 4 (3 velocity + pressure)");
   else
     rc = gmres_device(ctx, dof, Val, R, st);
   if (rc) return rc;
@@ -820,16 +899,21 @@ int svgpu_bc_create(svgpu_ctx* ctx, int faIn, int nNo, int dof, int bcType, cons
 
 int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, int maxItr, int dimKry) {
   if (!ctx) return SVGPU_EINVAL;
-  if (lsType != SVGPU_LS_GMRES && lsType != SVGPU_LS_CG)
-    return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: GMRES or CG");
-  // defaults of fsils_ls_create (liner_solver/ls.cpp:62-79): GMRES relTol 0.1, 4 restarts
-  // of dimension 250; CG relTol 1e-2, 1000 iterations (the Krylov dimension is unused)
-  const bool cg = lsType == SVGPU_LS_CG;
+  if (lsType != SVGPU_LS_GMRES && lsType != SVGPU_LS_CG && lsType != SVGPU_LS_NS)
+    return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: GMRES, CG or NS");
+  // defaults of fsils_ls_create (liner_solver/ls.cpp:50-79): GMRES relTol 0.1, 4 restarts
+  // of dimension 250; CG relTol 1e-2, 1000 iterations (the Krylov dimension is unused);
+  // NS relTol 0.4, 10 outer iterations, inner GMRES relTol 1e-2, 2 restarts of dimension
+  // dimKry (default 100), Schur CG relTol 0.2, 500 iterations
+  const bool cg = lsType == SVGPU_LS_CG, ns = lsType == SVGPU_LS_NS;
   ctx->lsType = lsType;
-  ctx->relTol = relTol >= 0 ? relTol : (cg ? 1e-2 : 0.1);
+  ctx->relTol = relTol >= 0 ? relTol : (cg ? 1e-2 : ns ? 0.4 : 0.1);
   ctx->absTol = absTol >= 0 ? absTol : 1e-10;
-  ctx->mItr = maxItr > 0 ? maxItr : (cg ? 1000 : 4);
-  ctx->sD = cg ? 1 : (dimKry > 0 ? dimKry : 250);
+  ctx->mItr = maxItr > 0 ? maxItr : (cg ? 1000 : ns ? 10 : 4);
+  ctx->sD = (cg || ns) ? 1 : (dimKry > 0 ? dimKry : 250);
+  ctx->ns_gm_sD = dimKry > 0 ? dimKry : 100;
+  if (ns && ctx->ns_gm_sD > 250) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: Krylov dimension above 250");
+  if (ns && ctx->mItr > 64) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: NS outer iterations above 64");
   if (ctx->sD > 250) return set_err(ctx, SVGPU_EINVAL, "fsils_ls_create: Krylov dimension above 250");
   ctx->ls_created = true;
   return SVGPU_OK;

@@ -100,6 +100,20 @@ struct KrylovWork {
 
 struct AmgState;
 
+// Work of the NS block solver (ns.cpp): the split operator blocks, the outer
+// iteration's vectors, and the inner GMRES work swapped into ctx->kw while it runs.
+struct NsWork {
+  int nNo = 0, nnz = 0, mItr = 0;
+  KrylovWork kw3;                        // inner GMRES (dof 3)
+  DevBuf<int> tmap;                      // block (i,j) -> position of block (j,i)
+  DevBuf<double> mK, mG, mD, mL, Gt;     // 9, 3, 3, 1, 3 doubles per block
+  DevBuf<double> W;                      // (2 mItr + 1) stacked [momentum (3 nNo); continuity (nNo)]
+  DevBuf<double> Rcur;                   // current [Rm; Rc]
+  DevBuf<double> U, P;                   // mItr x 3 nNo, mItr x nNo
+  DevBuf<double> sP, sGP, sSP, sX, sR;   // Schur CG scratch
+  DevBuf<double> coef, partial, dots;    // combination coefficients, multi-dot partials and results
+};
+
 // Phases of a Newton step timed with CUDA events on the library's stream when phase
 // timing is on (svgpu_phase_timing): consecutive marks bound contiguous intervals.
 enum Phase {
@@ -197,6 +211,9 @@ struct svgpu_ctx {
   svgpu::KrylovWork kw;
   svgpu::PhaseTimer phases;
   svgpu::DevBuf<double> cg_part, cg_d;  // CG: per-CTA partial sums, device scalars
+  std::unique_ptr<svgpu::NsWork> ns;    // NS block solver work
+  double ns_gm_relTol = 1e-2, ns_gm_absTol = 1e-10, ns_cg_relTol = 0.2, ns_cg_absTol = 1e-10;
+  int ns_gm_mItr = 2, ns_gm_sD = 100, ns_cg_mItr = 500;  // fsils_ls_create defaults (ls.cpp:50-58)
   svgpu::DevBuf<int> cg_f;              // CG: stop, last_i, suc, next iteration
   std::unique_ptr<svgpu::GnnState> gnn;
   std::unique_ptr<struct svgpu::AmgState> amg;
@@ -258,6 +275,34 @@ inline int grid_for(long n, int block, int cap = 152 * 16) {
 // ---- k_krylov.cu -------------------------------------------------------------
 // phase timing: start `phase` here (PH_COUNT: stop); no-op unless timing is on
 void phase_mark(svgpu_ctx* ctx, int phase);
+// gmres::gmres (the NS solver's sub-solver), abi.cpp
+int gmres_sub_device(svgpu_ctx* ctx, int dof, const double* K, const double* R, double* X, double relTol,
+                     double absTol, int mItr, int* itr, double* iNorm, double* fNorm);
+int ensure_krylov_work(svgpu_ctx* ctx, long n, int sD);
+// k_ns.cu / ns.cpp: the NS block solver (ns_solver)
+int ns_parts(int nNo);
+void launch_depart(cudaStream_t s, long nnz, const double* Val, const int* tmap, double* mK, double* mG, double* mD,
+                   double* mL, double* Gt);
+void launch_ns_split(cudaStream_t s, int nNo, const double* R, double* Rm, double* Rc);
+void launch_ns_merge(cudaStream_t s, int nNo, const double* Rm, const double* Rc, double* R);
+void launch_spmv_vs(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* K, const double* U,
+                    const double* base, double* y);
+void launch_spmv_sv(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* K, const double* U,
+                    const double* base, double* Y);
+void launch_spmv_ss(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* K, const double* U,
+                    double* y);
+void launch_schur_operator(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* G,
+                           const double* D, const double* L, const double* P, double* GP, double* SP, double* part,
+                           const int* f);
+void launch_combine(cudaStream_t s, long n, int m, const double* W, long ldw, const double* c, const double* base,
+                    double* out);
+void launch_gather_combine(cudaStream_t s, long n, int m, const double* V, long ldv, const double* c, double* out);
+void launch_schur_cg_iteration(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* G,
+                               const double* D, const double* L, double* P, double* GP, double* SP, double* X,
+                               double* R, double* part, double* d, int* f, int mItr);
+int schur_cg_device(svgpu_ctx* ctx, const double* G, const double* D, const double* L, double* R, double relTol,
+                    double absTol, int mItr, int* itr);
+int ns_solve_device(svgpu_ctx* ctx, const double* Val, double* R, svgpu_ls_stats* st);
 // k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
 int cg_parts(long n);
 void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
@@ -279,6 +324,7 @@ void launch_mask_face(cudaStream_t s, int nNo, int fdof, int dof, const int* glo
 int launch_multidot(cudaStream_t s, long n, int m, const double* V, long ldv, const double* w,
                     double* partial, int sm_count);
 void launch_reduce_partials(cudaStream_t s, int nparts, int m, const double* partial, double* out);
+int multidot_ctas(long n, int sm_count);
 void launch_residual_init(cudaStream_t s, long n, const double* R, double* u0, double* X, bool x_zero,
                           const double* AX);
 void launch_scale_by_inv_norm(cudaStream_t s, long n, double* u, const double* nrm2, double* err0,

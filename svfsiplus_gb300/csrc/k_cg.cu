@@ -150,4 +150,19 @@ void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, co
   cg_pupdate_kernel<<<g, kThreads, 0, s>>>(n, R, P, d, f);
 }
 
+// cgrad::schur (cgrad.cpp:50-160): the same recurrence on nNo scalars with the operator
+// S P = L P - D (G P) in place of the block SpMV
+void launch_schur_cg_iteration(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const double* G,
+                               const double* D, const double* L, double* P, double* GP, double* SP, double* X,
+                               double* R, double* part, double* d, int* f, int mItr) {
+  const long n = nNo;
+  const int g = cg_parts(n);
+  cg_check_kernel<<<1, 32, 0, s>>>(d, f, mItr);
+  launch_schur_operator(s, nNo, rowPtr, colPtr, G, D, L, P, GP, SP, part, f);
+  cg_alpha_kernel<<<1, 1024, 0, s>>>(part, g, d, f);
+  cg_update_kernel<<<g, kThreads, 0, s>>>(n, P, SP, X, R, part, d, f);
+  cg_err_kernel<<<1, 1024, 0, s>>>(part, g, d, f);
+  cg_pupdate_kernel<<<g, kThreads, 0, s>>>(n, R, P, d, f);
+}
+
 }  // namespace svgpu

@@ -40,6 +40,12 @@ CASES = {
     "small": dict(mesh="small", n_steps=3, dump_step=1, dump_iter=1, u_amp=5.0),
     # the CPU-runnable 50k-tet pipe, 10 time steps, fields after every step
     "pipe50k": dict(mesh="pipe50k", n_steps=10, dump_step=1, dump_iter=1),
+    # the NS block solver (ns_solver.cpp:167): 10 outer iterations or relative 1e-4,
+    # inner GMRES and Schur CG at the reference's NS defaults
+    "tiny_ns": dict(mesh="tiny", n_steps=2, dump_step=2, dump_iter=2, ls_type="ns", ls_rel_tol=1e-4,
+                    ls_max_itr=10),
+    "small_ns": dict(mesh="small", n_steps=3, dump_step=1, dump_iter=1, u_amp=5.0, ls_type="ns",
+                     ls_rel_tol=1e-4, ls_max_itr=10),
 }
 
 
@@ -137,7 +143,10 @@ def run_case(name):
         for line in log.splitlines():
             t = line.split()
             if t[0] == "step":
-                its.append([int(t[1]), int(t[3]), float(t[5]), float(t[7]), int(t[9]), int(t[11])])
+                row = [int(t[1]), int(t[3]), float(t[5]), float(t[7]), int(t[9]), int(t[11])]
+                if len(t) > 12:  # NS: inner GMRES and CG iteration totals, dB
+                    row += [int(t[13]), int(t[15]), float(t[17])]
+                its.append(row)
         out["newton_log"] = np.array(its, dtype=np.float64)
         rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
         out["rowPtr"] = rd("rowPtr.bin", np.int32)
