@@ -5,11 +5,10 @@ outer relative tolerance 1e-4, at most 10 outer iterations, inner GMRES and Schu
 the reference's NS defaults (GMRES relTol 1e-2, 2 restarts of 50; CG relTol 0.2, 500
 iterations).
 
-The GPU sums its dot products in another order, so the inexact inner solves end at
-slightly different iterates: the tests hold the GPU to the reference's own accuracy
-contract (the increment solves the preconditioned system to the outer tolerance; outer
-iteration counts within one) and to the reference's fields after the Newton steps
-(1e-6 relative)."""
+The GPU sums its dot products in another order, so the iterates differ by rounding
+only: equal outer iteration counts, increments within 1e-9 relative (measured 7e-15 on
+tiny, 2.5e-12 on small), the increment solving the preconditioned system to the outer
+tolerance, and the fields after three Newton steps within 1e-10 (measured 4e-15)."""
 import numpy as np
 import pytest
 
@@ -68,9 +67,9 @@ def test_gpu_ns_solve_matches_reference(golden, name):
     print(name, "GPU itr", st.itr, "ref itr", int(row[4]), "GPU fNorm", st.fNorm, "ref", row[3],
           "dX rel", rel(Ri, g["dX"]), "prec. residual", preconditioned_residual(g, Ri))
     assert abs(st.iNorm - row[2]) <= 1e-10 * row[2]
-    assert st.suc == 1 and abs(st.itr - int(row[4])) <= 1
+    assert st.suc == 1 and st.itr == int(row[4])
     assert preconditioned_residual(g, Ri) <= 1.5e-4
-    assert rel(Ri, g["dX"]) <= 1e-3
+    assert rel(Ri, g["dX"]) <= 1e-9
 
 
 @pytest.mark.gpu
@@ -90,4 +89,4 @@ def test_gpu_ns_time_steps_match_reference(golden):
         ref = g[f"Yn_{step}"]
         ev, ep = rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])
         print("step", step, "velocity", ev, "pressure", ep)
-        assert ev <= 1e-6 and ep <= 1e-6
+        assert ev <= 1e-10 and ep <= 1e-10
