@@ -153,6 +153,20 @@ typedef struct {
   double dt, am, af, gam, beta;
 } svgpu_solid_props;
 
+/* Element domains of the mesh for FSI (mshType eId, ComMod.h; all_fun::domain,
+ * all_fun.cpp:149-175): eId[e] bit 0 = fluid domain, bit 1 = solid domain, per element
+ * in the original numbering.  Elements with neither bit are skipped by
+ * svgpu_construct_fsi. */
+int svgpu_mesh_domains(svgpu_ctx* ctx, const int* eId);
+/* construct_fsi (fsi.cpp:48-332), one fluid domain and one neo-Hookean solid domain
+ * (struct_3d, sv_struct.cpp:851): fluid elements in the current configuration
+ * x + Dg(4..6) with the convection velocity relative to Yg(4..6) (fluid_3d_m/_c with
+ * mvMsh), solid elements as construct_dsolid with dof 4.  State arrays (tDof, nNo) with
+ * the FSI equation at rows 0..3 and the mesh equation at rows 4..6 (tDof >= 7); both
+ * property sets carry the FSI equation's generalised-alpha constants.  R (4, nNo) and
+ * Val (16, nnz) are added to. */
+int svgpu_construct_fsi(svgpu_ctx* ctx, const svgpu_fluid_props* fluid, const svgpu_solid_props* solid, int tDof,
+                        const double* Ag, const double* Yg, const double* Dg, double* R, double* Val);
 /* Replaces construct_dsolid (solver/sv_struct.cpp:213, struct_3d_carray :552) for
  * linear tets: adds into R (dof,nNo) and Val (dof*dof,nnz), dof = 3 (the struct
  * equation) or 4 (the solid blocks of the FSI equation, fsi.cpp:213-262).  State

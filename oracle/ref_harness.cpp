@@ -31,6 +31,7 @@
 #include "fsils_api.hpp"
 #include "commu.h"
 #include "lhs.h"
+#include "mat_fun.h"
 
 #include <cmath>
 #include <cstdio>
@@ -231,6 +232,122 @@ static int assemble_only(const std::string& dir, const std::string& out, std::ma
   return 0;
 }
 
+// FSI assembly (construct_fsi, fsi.cpp:48-332) on the case mesh: every element belongs
+// to the fluid domain (eId bit 0) or the solid domain (bit 1); tDof = 7 with the mesh
+// equation's displacement and velocity at rows 4..6 (fluid elements are integrated in
+// x + Dg(4..6) and convect with the velocity relative to Yg(4..6)).  Dumps R and Val.
+static int assemble_fsi(const std::string& dir, const std::string& out, std::map<std::string, std::string>& P) {
+  auto getd = [&](const char* k) { return std::stod(P.at(k)); };
+  Simulation sim;
+  auto& com = sim.com_mod;
+  auto xs = read_raw<double>(dir + "/x.bin");
+  auto iens = read_raw<int>(dir + "/ien.bin");
+  auto eid = read_raw<int>(dir + "/eid.bin");
+  const int nNo = (int)xs.size() / 3;
+  const int nEl = (int)iens.size() / 4;
+  const int tDof = 7;
+  com.nsd = 3;
+  com.nsymd = 6;
+  com.tnNo = nNo;
+  com.gtnNo = nNo;
+  com.nMsh = 1;
+  com.msh.resize(1);
+  com.nEq = 1;
+  com.eq.resize(1);
+  com.dt = getd("dt");
+  com.mvMsh = true;
+  com.dFlag = true;
+  auto& msh = com.msh[0];
+  msh.name = "pipe";
+  msh.eNoN = 4;
+  msh.nEl = nEl;
+  msh.gnEl = nEl;
+  msh.nNo = nNo;
+  msh.gnNo = nNo;
+  msh.IEN.resize(4, nEl);
+  msh.eId.resize(nEl);
+  for (int e = 0; e < nEl; e++) {
+    for (int a = 0; a < 4; a++) msh.IEN(a, e) = iens[4 * e + a];
+    msh.eId(e) = eid[e];
+  }
+  msh.gN.resize(nNo);
+  for (int a = 0; a < nNo; a++) msh.gN(a) = a;
+  nn::select_ele(com, msh);
+  msh.nFs = 1;
+  fs::init_fs_msh(com, msh);
+  com.x.resize(3, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < 3; i++) com.x(i, a) = xs[3 * a + i];
+  com.Bf.resize(3, nNo);
+  mat_fun::ten_init(3);  // the index table of the legacy tensor products (initialize.cpp)
+  auto& eq = com.eq[0];
+  eq.phys = consts::EquationType::phys_FSI;
+  eq.dof = 4;
+  eq.roInf = getd("rho_inf");
+  eq.am = 0.5 * (3.0 - eq.roInf) / (1.0 + eq.roInf);  // first-order equation (initialize.cpp:424-430)
+  eq.af = 1.0 / (1.0 + eq.roInf);
+  eq.beta = 0.25 * std::pow((1.0 + eq.am - eq.af), 2.0);
+  eq.gam = 0.5 + eq.am - eq.af;
+  eq.s = 0;
+  eq.e = 3;
+  eq.nDmn = 2;
+  eq.dmn.resize(2);
+  using PP = consts::PhysicalProperyType;
+  auto& fd = eq.dmn[0];
+  fd.Id = 0;
+  fd.phys = consts::EquationType::phys_fluid;
+  fd.prop[PP::fluid_density] = getd("rho_f");
+  fd.prop[PP::f_x] = 0.0;
+  fd.prop[PP::f_y] = 0.0;
+  fd.prop[PP::f_z] = 0.0;
+  fd.prop[PP::backflow_stab] = getd("backflow_beta");
+  fd.prop[PP::inverse_darcy_permeability] = 0.0;
+  fd.fluid_visc.viscType = consts::FluidViscosityModelType::viscType_Const;
+  fd.fluid_visc.mu_i = getd("mu");
+  auto& sd = eq.dmn[1];
+  sd.Id = 1;
+  sd.phys = consts::EquationType::phys_struct;
+  sd.prop[PP::solid_density] = getd("rho_s");
+  sd.prop[PP::elasticity_modulus] = getd("E");
+  sd.prop[PP::poisson_ratio] = getd("nu");
+  sd.prop[PP::damping] = 0.0;
+  sd.prop[PP::f_x] = 0.0;
+  sd.prop[PP::f_y] = 0.0;
+  sd.prop[PP::f_z] = 0.0;
+  sd.stM.isoType = consts::ConstitutiveModelType::stIso_nHook;
+  sd.stM.volType = consts::ConstitutiveModelType::stVol_ST91;
+  sd.stM.C10 = getd("C10");
+  sd.stM.Kpen = getd("Kpen");
+  com.tDof = tDof;
+  com.dof = 4;
+  int nnz = 0;
+  lhsa_ns::lhsa(&sim, nnz);
+  com.lhs.nnz = nnz;
+  FsilsLinearAlgebra fsils_la;
+  eq.linear_algebra = &fsils_la;
+  auto A = read_raw<double>(dir + "/A.bin");
+  auto Y = read_raw<double>(dir + "/Y.bin");
+  auto D = read_raw<double>(dir + "/D.bin");
+  Array<double> Ag(tDof, nNo), Yg(tDof, nNo), Dg(tDof, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < tDof; i++) {
+      Ag(i, a) = A[tDof * a + i];
+      Yg(i, a) = Y[tDof * a + i];
+      Dg(i, a) = D[tDof * a + i];
+    }
+  ls_ns::ls_alloc(com, eq);
+  com.R.resize(4, nNo);
+  com.R = 0.0;
+  com.Val = 0.0;
+  com.cEq = 0;
+  eq_assem::global_eq_assem(com, sim.get_cep_mod(), msh, Ag, Yg, Dg);
+  write_raw(out + "/R_asm.bin", com.R.data(), (size_t)com.R.size());
+  write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
+  write_raw(out + "/rowPtr.bin", com.rowPtr.data(), (size_t)com.rowPtr.size());
+  write_raw(out + "/colPtr.bin", com.colPtr.data(), (size_t)com.colPtr.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::fprintf(stderr, "usage: %s CASE_DIR OUT_DIR\n", argv[0]);
@@ -238,6 +355,7 @@ int main(int argc, char** argv) {
   }
   std::string dir = argv[1], out = argv[2];
   auto P = read_params(dir);
+  if (P.count("mode") && P.at("mode") == "assemble_fsi") return assemble_fsi(dir, out, P);
   if (P.count("mode") && P.at("mode").rfind("assemble_", 0) == 0) return assemble_only(dir, out, P);
   auto getd = [&](const char* k) { return std::stod(P.at(k)); };
   auto geti = [&](const char* k) { return std::stoi(P.at(k)); };

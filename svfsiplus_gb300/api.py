@@ -197,6 +197,14 @@ class Context:
         self._check(lib().svgpu_construct_fluid(self._h, C.byref(props), _ptr(Ag), _ptr(Yg), _ptr(Bf), _ptr(R),
                                                 _ptr(Val), int(precision)), "construct_fluid")
 
+    def mesh_domains(self, eId):
+        eId = np.ascontiguousarray(eId, dtype=np.int32)
+        self._check(lib().svgpu_mesh_domains(self._h, _ptr(eId)), "mesh_domains")
+
+    def construct_fsi(self, fluid, solid, tDof, Ag, Yg, Dg, R, Val):
+        self._check(lib().svgpu_construct_fsi(self._h, C.byref(fluid), C.byref(solid), int(tDof), _ptr(Ag), _ptr(Yg),
+                                              _ptr(Dg), _ptr(R), _ptr(Val)), "construct_fsi")
+
     def construct_dsolid(self, props, dof, tDof, s, Ag, Yg, Dg, R, Val):
         self._check(lib().svgpu_construct_dsolid(self._h, C.byref(props), int(dof), int(tDof), int(s), _ptr(Ag),
                                                  _ptr(Yg), _ptr(Dg), _ptr(R), _ptr(Val)), "construct_dsolid")

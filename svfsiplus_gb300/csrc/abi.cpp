@@ -1068,8 +1068,57 @@ int svgpu_mesh_create(svgpu_ctx* ctx, int nNo, int nEl, int eNoN, const int* IEN
   if ((rc = to_device(ctx, m->elem_id, perm.data(), perm.size()))) return rc;
   if ((rc = to_device(ctx, m->boff, boff.data(), boff.size()))) return rc;
   if ((rc = to_device(ctx, m->x4, x4.data(), x4.size()))) return rc;
+  m->split_fluid.assign(m->color_start.begin() + 1, m->color_start.end());
+  m->split_solid = m->split_fluid;
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->mesh = std::move(m);
+  return SVGPU_OK;
+}
+
+int svgpu_mesh_domains(svgpu_ctx* ctx, const int* eId) {
+  if (!ctx || !eId) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "mesh_domains before mesh_create");
+  MeshData& m = *ctx->mesh;
+  const int nEl = m.nEl;
+  int rc;
+  std::vector<int> eid, pien, perm;
+  std::vector<uint8_t> boff;
+  if ((rc = to_host(ctx, eid, eId, nEl))) return rc;
+  if ((rc = to_host(ctx, pien, m.ien.p, (size_t)4 * nEl))) return rc;
+  if ((rc = to_host(ctx, perm, m.elem_id.p, nEl))) return rc;
+  boff.resize((size_t)16 * nEl);
+  SVGPU_CUDA(ctx, cudaMemcpy(boff.data(), m.boff.p, boff.size(), cudaMemcpyDeviceToHost));
+  // within every colour: fluid elements (eId bit 0) first, then solid (bit 1), then the
+  // rest, each group in its previous order (all_fun::domain, all_fun.cpp:149-175, takes
+  // the first domain whose bit is set)
+  std::vector<int> order(nEl);
+  std::vector<int> sf(m.color_start.size() - 1), ss(m.color_start.size() - 1);
+  for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+    int o = m.color_start[k];
+    for (int g = 0; g < 3; g++) {
+      for (int q = m.color_start[k]; q < m.color_start[k + 1]; q++) {
+        const int bits = eid[perm[q]];
+        const int grp = (bits & 1) ? 0 : (bits & 2) ? 1 : 2;
+        if (grp == g) order[o++] = q;
+      }
+      if (g == 0) sf[k] = o;
+      if (g == 1) ss[k] = o;
+    }
+  }
+  std::vector<int> pien2((size_t)4 * nEl), perm2(nEl);
+  std::vector<uint8_t> boff2((size_t)16 * nEl);
+  for (int q = 0; q < nEl; q++) {
+    const int src = order[q];
+    perm2[q] = perm[src];
+    for (int a = 0; a < 4; a++) pien2[4 * (size_t)q + a] = pien[4 * (size_t)src + a];
+    for (int b = 0; b < 16; b++) boff2[16 * (size_t)q + b] = boff[16 * (size_t)src + b];
+  }
+  SVGPU_CUDA(ctx, cudaMemcpy(m.ien.p, pien2.data(), pien2.size() * sizeof(int), cudaMemcpyHostToDevice));
+  SVGPU_CUDA(ctx, cudaMemcpy(m.elem_id.p, perm2.data(), perm2.size() * sizeof(int), cudaMemcpyHostToDevice));
+  SVGPU_CUDA(ctx, cudaMemcpy(m.boff.p, boff2.data(), boff2.size(), cudaMemcpyHostToDevice));
+  m.split_fluid = sf;
+  m.split_solid = ss;
   return SVGPU_OK;
 }
 
@@ -1250,6 +1299,44 @@ static int assemble_generic(svgpu_ctx* ctx, int dof, int tDof, const double* con
   if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
+}
+
+int svgpu_construct_fsi(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp, int tDof,
+                        const double* Ag, const double* Yg, const double* Dg, double* R, double* Val) {
+  if (!ctx || !fp || !sp) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (tDof < 7) return set_err(ctx, SVGPU_EINVAL, "construct_fsi: tDof must hold the FSI (4) and mesh (3) rows");
+  const FluidConsts fc = fluid_consts(fp);
+  SolidConsts c;
+  c.rho = sp->rho;
+  c.damping = sp->damping;
+  c.f[0] = sp->f[0];
+  c.f[1] = sp->f[1];
+  c.f[2] = sp->f[2];
+  c.C10 = sp->C10;
+  c.Kpen = sp->Kpen;
+  c.volType = sp->volType;
+  c.dt = sp->dt;
+  c.am = sp->am;
+  c.af = sp->af;
+  c.gam = sp->gam;
+  c.beta = sp->beta;
+  const double* states[3] = {Ag, Yg, Dg};
+  MeshData& m = *ctx->mesh;
+  int k = 0;  // colour index of the next call
+  return assemble_generic(ctx, 4, tDof, states, 3, R, Val,
+                          [&](const double* const* st, double* Rd, double* Vd, int e0, int ne) {
+                            const int split_f = m.split_fluid[k], split_s = m.split_solid[k];
+                            k++;
+                            launch_fluid_ale_assembly(ctx->stream, fc, e0, split_f - e0, m.ien.p, m.boff.p,
+                                                      m.elem_id.p, m.x4.p, tDof, st[0], st[1], st[2], nullptr,
+                                                      ctx->rowPtr.p, Rd, Vd, ctx->errflag.p);
+                            launch_struct_assembly(ctx->stream, 4, c, split_f, split_s - split_f, m.ien.p, m.boff.p,
+                                                   m.elem_id.p, m.x4.p, tDof, 0, st[0], st[1], st[2],
+                                                   ctx->rowPtr.p, Rd, Vd, ctx->errflag.p);
+                            ctx->launches++;
+                            (void)ne;
+                          });
 }
 
 int svgpu_construct_dsolid(svgpu_ctx* ctx, const svgpu_solid_props* p, int dof, int tDof, int s, const double* Ag,

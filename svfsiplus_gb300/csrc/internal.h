@@ -82,6 +82,9 @@ struct MeshData {
   DevBuf<double> x4;     // (4, nNo): x, y, z, 0 -- 32-byte aligned node records
   DevBuf<uint8_t> boff;  // (nEl, 16) offset of block (a,b) within row ien[a]
   std::vector<int> color_start;  // nColors + 1
+  // per colour: fluid elements [color_start[k], split_fluid[k]), solid elements
+  // [split_fluid[k], split_solid[k]); the rest belong to no assembled domain
+  std::vector<int> split_fluid, split_solid;
 };
 
 struct KrylovWork {
@@ -358,6 +361,11 @@ void launch_start_vector32(cudaStream_t s, long n, const double* r, const double
 struct FluidConsts {
   double rho, mu, f0, f1, f2, kd, beta_bf, dt, am, af, gam;
 };
+// FP64 fluid elements of the FSI equation (ALE: state arrays with ld rows per node)
+void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
+                               const uint8_t* boff, const int* elem_id, const double* x4, int ld, const double* Ag,
+                               const double* Yg, const double* Dg, const double* Bf, const int* rowPtr, double* R,
+                               double* Val64, int* errflag);
 void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, int e0, int ne,
                            const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
                            const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,

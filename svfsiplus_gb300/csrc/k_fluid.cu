@@ -83,7 +83,11 @@ __device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const 
 // T: arithmetic type of the element integrals; TV: storage type of Val.  WR / WK
 // select writing the residual rows / the tangent blocks (the mixed-precision path
 // runs the residual in FP64 and the tangent in FP32 as two launches).
-template <typename T, typename TV, bool WR, bool WK>
+// ALE (construct_fsi, fsi.cpp:158-164 and fluid.cpp:1508-1516/1835-1843): the state
+// arrays have ld rows per node (the FSI equation's 4, then the mesh equation's 3); the
+// element is integrated in the current configuration x + Dg(4..6) and convects with
+// the velocity relative to the mesh velocity Yg(4..6).
+template <typename T, typename TV, bool WR, bool WK, bool ALE>
 __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, int ne,
                                                        const int* __restrict__ ien,
                                                        const uint8_t* __restrict__ boff,
@@ -94,7 +98,8 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
                                                        const double* __restrict__ Bf,
                                                        const int* __restrict__ rowPtr,
                                                        double* __restrict__ R, TV* __restrict__ Val,
-                                                       int* __restrict__ errflag) {
+                                                       int* __restrict__ errflag, int ld,
+                                                       const double* __restrict__ Dg) {
   const int le = blockIdx.x * blockDim.x + threadIdx.x;
   if (le >= ne) return;
   const int e = e0 + le;
@@ -104,19 +109,30 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 
   // gather: coordinates, acceleration, velocity/pressure, body force
   T xl[4][3], al[4][3], yl[4][4];
+  T ym[ALE ? 4 : 1][3];  // mesh velocity
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     const double2 x01 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a]);
     const double2 x23 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a] + 2);
-    const double2 a01 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a]);
-    const double2 a23 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a] + 2);
-    const double2 y01 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a]);
-    const double2 y23 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a] + 2);
-    xl[a][0] = (T)x01.x; xl[a][1] = (T)x01.y; xl[a][2] = (T)x23.x;
     double b0 = 0.0, b1 = 0.0, b2 = 0.0;
     if (Bf) { b0 = Bf[3L * nd[a]]; b1 = Bf[3L * nd[a] + 1]; b2 = Bf[3L * nd[a] + 2]; }
-    al[a][0] = (T)(a01.x - b0); al[a][1] = (T)(a01.y - b1); al[a][2] = (T)(a23.x - b2);
-    yl[a][0] = (T)y01.x; yl[a][1] = (T)y01.y; yl[a][2] = (T)y23.x; yl[a][3] = (T)y23.y;
+    if (!ALE) {
+      const double2 a01 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a]);
+      const double2 a23 = *reinterpret_cast<const double2*>(Ag + 4L * nd[a] + 2);
+      const double2 y01 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a]);
+      const double2 y23 = *reinterpret_cast<const double2*>(Yg + 4L * nd[a] + 2);
+      xl[a][0] = (T)x01.x; xl[a][1] = (T)x01.y; xl[a][2] = (T)x23.x;
+      al[a][0] = (T)(a01.x - b0); al[a][1] = (T)(a01.y - b1); al[a][2] = (T)(a23.x - b2);
+      yl[a][0] = (T)y01.x; yl[a][1] = (T)y01.y; yl[a][2] = (T)y23.x; yl[a][3] = (T)y23.y;
+    } else {
+      const double* A = Ag + (long)ld * nd[a];
+      const double* Y = Yg + (long)ld * nd[a];
+      const double* D = Dg + (long)ld * nd[a];
+      xl[a][0] = (T)(x01.x + D[4]); xl[a][1] = (T)(x01.y + D[5]); xl[a][2] = (T)(x23.x + D[6]);
+      al[a][0] = (T)(A[0] - b0); al[a][1] = (T)(A[1] - b1); al[a][2] = (T)(A[2] - b2);
+      yl[a][0] = (T)Y[0]; yl[a][1] = (T)Y[1]; yl[a][2] = (T)Y[2]; yl[a][3] = (T)Y[3];
+      ym[ALE ? a : 0][0] = (T)Y[4]; ym[ALE ? a : 0][1] = (T)Y[5]; ym[ALE ? a : 0][2] = (T)Y[6];
+    }
   }
 
   // gnn (nn.cpp:489-545): xXi(i,j) = sum_a x(i,a) dN_a/dxi_j with dN/dxi = (I; -1 -1 -1)
@@ -208,6 +224,12 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
       p += N[a] * yl[a][3];
 #pragma unroll
       for (int k = 0; k < 3; k++) px[k] += Nx[k][a] * yl[a][3];
+    }
+    if (ALE) {  // convection relative to the mesh (fluid.cpp:1837-1843)
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) u[i] = u[i] - N[a] * ym[ALE ? a : 0][i];
     }
     const T divU = ux[0][0] + ux[1][1] + ux[2][2];
     // stabilisation (fluid.cpp:1922-1995)
@@ -446,15 +468,24 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
   const int block = 128;
   const int grid = (ne + block - 1) / block;
   if (precision == SVGPU_FP64) {
-    fluid_p1_kernel<double, double, true, true><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg,
-                                                                        Bf, rowPtr, R, Val64, errflag);
+    fluid_p1_kernel<double, double, true, true, false><<<grid, block, 0, s>>>(
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr);
   } else {
     // residual rows in FP64, tangent blocks in FP32
-    fluid_p1_kernel<double, double, true, false><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg,
-                                                                         Bf, rowPtr, R, nullptr, errflag);
-    fluid_p1_kernel<float, float, false, true><<<grid, block, 0, s>>>(c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf,
-                                                                       rowPtr, R, Val32, errflag);
+    fluid_p1_kernel<double, double, true, false, false><<<grid, block, 0, s>>>(
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
+    fluid_p1_kernel<float, float, false, true, false><<<grid, block, 0, s>>>(
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr);
   }
+}
+
+void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
+                               const uint8_t* boff, const int* elem_id, const double* x4, int ld, const double* Ag,
+                               const double* Yg, const double* Dg, const double* Bf, const int* rowPtr, double* R,
+                               double* Val64, int* errflag) {
+  if (ne <= 0) return;
+  fluid_p1_kernel<double, double, true, true, true><<<(ne + 127) / 128, 128, 0, s>>>(
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, ld, Dg);
 }
 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,

@@ -109,6 +109,52 @@ def run_assembly(name, physics, solve=None):
         shutil.rmtree(tmp)
 
 
+# FSI assembly on the small pipe: elements whose centroid lies outside 0.35 (of the
+# radius 0.5) form the solid domain, the rest the fluid; seeded random state with the
+# mesh displacement/velocity at rows 4..6 (tDof 7).
+FSI = dict(rho_f=1.06, mu=0.04, backflow_beta=0.2, rho_s=1.2, E=1.0e6, nu=0.45, dt=1e-3, rho_inf=0.5)
+FSI["C10"] = FSI["E"] / (4.0 * (1.0 + FSI["nu"]))
+FSI["Kpen"] = FSI["E"] / (3.0 * (1.0 - 2.0 * FSI["nu"]))
+
+
+def fsi_domains(mesh):
+    """eId per element: bit 0 fluid, bit 1 solid (solid where the centroid radius > 0.35)."""
+    cen = mesh.x[mesh.ien].mean(axis=1)
+    r = np.hypot(cen[:, 0], cen[:, 1])
+    return np.where(r > 0.35, 2, 1).astype(np.int32)
+
+
+def run_fsi(name):
+    mesh = named_pipe("small")
+    rng = np.random.default_rng(23)
+    nNo, tDof = mesh.nNo, 7
+    params = dict(FSI)
+    params["mode"] = "assemble_fsi"
+    A = rng.standard_normal((nNo, tDof))
+    Y = rng.standard_normal((nNo, tDof))
+    D = 0.01 * rng.standard_normal((nNo, tDof))
+    eid = fsi_domains(mesh)
+    tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        cdir, odir = os.path.join(tmp, "case"), os.path.join(tmp, "out")
+        write_case(mesh, cdir, params)
+        for k, v in (("A", A), ("Y", Y), ("D", D)):
+            v.tofile(os.path.join(cdir, f"{k}.bin"))
+        eid.tofile(os.path.join(cdir, "eid.bin"))
+        os.makedirs(odir)
+        subprocess.run([HARNESS, cdir, odir], check=True)
+        rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
+        out = {"params": np.array(repr(params)), "A": A, "Y": Y, "D": D, "eid": eid,
+               "rowPtr": rd("rowPtr.bin", np.int32), "colPtr": rd("colPtr.bin", np.int32),
+               "R_asm": rd("R_asm.bin", np.float64).reshape(nNo, 4),
+               "Val_asm": rd("Val_asm.bin", np.float64).reshape(-1, 16)}
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+        print(name, "nNo", nNo, "solid elements", int((eid == 2).sum()), "of", eid.size,
+              "|R|", np.linalg.norm(out["R_asm"]), "|Val|", np.linalg.norm(out["Val_asm"]))
+    finally:
+        shutil.rmtree(tmp)
+
+
 def write_case(mesh, d, params):
     os.makedirs(d, exist_ok=True)
     mesh.x.astype(np.float64).tofile(os.path.join(d, "x.bin"))
@@ -172,8 +218,11 @@ def run_case(name):
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small", "mesh_cg_small", "mesh_cg7_small"]):
-        if n == "struct_small":
+    for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small", "mesh_cg_small", "mesh_cg7_small",
+                                             "fsi_small"]):
+        if n == "fsi_small":
+            run_fsi(n)
+        elif n == "struct_small":
             run_assembly(n, "struct")
         elif n == "mesh_small":
             run_assembly(n, "mesh")
