@@ -192,6 +192,13 @@ int svgpu_get_system(svgpu_ctx* ctx, double* R, double* Val);
 int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h,
                        const double* Yg, double* R, double* Val);
 
+/* The same on a moving mesh (b_assem_neu_bc with com_mod.mvMsh): state arrays
+ * (tDof, nNo) with the mesh equation at rows 4..6; the face is placed at x + Do(4..6)
+ * (gnnb, nn.cpp:627-640) and the backflow term convects with Yg(0..2) - Yg(4..6)
+ * (b_fluid, fluid.cpp:79-84).  R (4, nNo) and Val (16, nnz) are added to. */
+int svgpu_neu_bc_fluid_ale(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h, int tDof,
+                           const double* Yg, const double* Do, double* R, double* Val);
+
 /* ---- learned preconditioner (no counterpart in the reference) ------------------------
  * A 3-layer message-passing network on the CSR graph (hidden width 64, BF16 weights,
  * FP32 accumulation) trained online on (residual, increment) pairs of the
@@ -269,6 +276,65 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                      const double* Ao, const double* Yo, const double* Do,
                      double* An, double* Yn, double* Dn,
                      double* iNorm, double* pNorm, svgpu_ls_stats* stats);
+
+/* ---- coupled ALE FSI time step (solver/main.cpp:292-762 with the FSI and mesh
+ * equations coupled, as in the reference's fsi/pipe_3d case) ----------------------- */
+/* Physical properties and generalised-alpha constants of the two equations: the FSI
+ * equation (first order; fluid domain = eId bit 0, neo-Hookean solid domain = eId bit 1,
+ * both with the FSI equation's constants) and the mesh-motion equation (second order,
+ * linear elastic over every element, l_elas_3d l_elas.cpp:274). */
+typedef struct {
+  svgpu_fluid_props fluid;
+  svgpu_solid_props solid;
+  double mesh_E, mesh_nu, mesh_rho;
+  double mesh_am, mesh_af, mesh_gam, mesh_beta;
+} svgpu_fsi_props;
+
+/* Newton and linear-solver settings per equation (index 0 FSI, 1 mesh): eqType
+ * minItr/maxItr/tol, and the fsils_ls_create arguments of each equation's FSILS
+ * handle (lsType SVGPU_LS_GMRES or SVGPU_LS_CG; negative values keep the reference
+ * defaults).  incL[q] (nFaces flags, as main.cpp:559-575 builds them) selects the
+ * Dirichlet faces of svgpu_bc_create that equation q's solves apply. */
+typedef struct {
+  int minItr[2], maxItr[2];
+  double tol[2];
+  int lsType[2];
+  double relTol[2], absTol[2];
+  int lsMaxItr[2], dimKry[2];
+  const int* incL[2];
+  int outletFace;   /* mesh face (svgpu_face_create) of the lumen outlet, -1 for none */
+  double outletH;   /* Neumann value on it; backflow stabilisation in the moving configuration */
+  /* FSI equation's solve: SVGPU_FP64 (fsils_solve as the reference) or SVGPU_MIXED (an
+   * FP32 copy of the FP64-assembled tangent in the FP64 defect-correction loop, with
+   * the context's solver mode, svgpu_set_solver_mode, as preconditioner; GMRES only) */
+  int precision;
+} svgpu_fsi_opts;
+
+/* Strong Dirichlet values of one equation: n nodes, Y and A values (3, n) for the
+ * equation's rows 0..2 (FSI: velocity; mesh: mesh velocity/acceleration at rows 4..6). */
+typedef struct {
+  int n;
+  const int* nodes;
+  const double* Y;
+  const double* A;
+} svgpu_dirichlet_set;
+
+/* One time step of the coupled FSI problem on the mesh given to svgpu_mesh_create and
+ * svgpu_mesh_domains: picp (pic.cpp:591) + the strong Dirichlet values of both
+ * equations, then Newton iterations that alternate between the equations
+ * (picc's coupled cycling, pic.cpp:283-327) until both have converged:
+ *   pici for all rows -> assemble (FSI: construct_fsi, fsi.cpp:48, plus the outlet's
+ *   b_assem_neu_bc in the moving configuration; mesh: construct_mesh, mesh.cpp:49) ->
+ *   fsils_solve (FP64, diagonal preconditioner) -> picc (FSI: rows 0..3, then solid
+ *   nodes copy rows 0..2 into 4..6; mesh: rows 4..6).
+ * State arrays (7, nNo): Ao/Yo/Do in, An/Yn/Dn out.  iNorm[2]/pNorm[2] carry the
+ * equations' eqType iNorm/pNorm across steps (in/out).  stats receives one entry per
+ * Newton iteration (room for maxItr[0] + maxItr[1]) and stat_eq its equation index;
+ * either may be NULL.  Returns the number of Newton iterations or a negative status. */
+int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, const svgpu_fsi_opts* opts,
+                   const svgpu_dirichlet_set* dir_fsi, const svgpu_dirichlet_set* dir_mesh,
+                   const double* Ao, const double* Yo, const double* Do, double* An, double* Yn, double* Dn,
+                   double* iNorm, double* pNorm, svgpu_ls_stats* stats, int* stat_eq);
 
 #ifdef __cplusplus
 }

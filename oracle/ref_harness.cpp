@@ -32,6 +32,7 @@
 #include "commu.h"
 #include "lhs.h"
 #include "mat_fun.h"
+#include "all_fun.h"
 
 #include <cmath>
 #include <cstdio>
@@ -348,6 +349,281 @@ static int assemble_fsi(const std::string& dir, const std::string& out, std::map
   return 0;
 }
 
+// Coupled ALE FSI time steps (iterate_solution, main.cpp:292-762, with two coupled
+// equations): the FSI equation (dof 4, rows 0..3 of a 7-row state, fluid domain Id 0
+// and legacy struct_3d solid domain Id 1, GMRES) and the mesh equation (dof 3, rows
+// 4..6, linear elastic over every element, CG).  Per Newton iteration: pici (all
+// equations) -> ls_alloc -> global_eq_assem (construct_fsi / construct_mesh) ->
+// outlet b_assem_neu_bc (FSI only; gnnb moves the face by Do(4..6), b_fluid convects
+// with the velocity relative to the mesh) -> ls_solve -> picc, which copies the solid
+// nodes' An/Yn/Dn(0..2) into rows 4..6 after an FSI solve and alternates the
+// equations until both converge.  Linear-solver faces follow baf_ini (fsi_ls_ini,
+// baf_ini.cpp:690-790, and the structure-node face, :197-227): 0 lumen inlet, 1 wall
+// inlet ring, 2 wall outlet ring (FSI, Dirichlet), 3 (the outlet Neumann BC: no face),
+// 4 lumen inlet, 5 lumen outlet (mesh, Dirichlet), 6 every solid-domain node (mesh).
+// Dirichlet values are written directly (the role of set_bc_dir, set_bc.cpp:794):
+// inlet velocity u_z = u_c(t) * profile and acceleration du_c/dt * profile, zero on
+// the wall rings (rows 0..2) and zero mesh motion at the lumen ends (rows 4..6).
+static int run_fsi(const std::string& dir, const std::string& out, std::map<std::string, std::string>& P) {
+  auto getd = [&](const char* k) { return std::stod(P.at(k)); };
+  auto geti = [&](const char* k) { return std::stoi(P.at(k)); };
+  Simulation sim;
+  auto& com = sim.com_mod;
+  auto xs = read_raw<double>(dir + "/x.bin");
+  auto iens = read_raw<int>(dir + "/ien.bin");
+  auto eid = read_raw<int>(dir + "/eid.bin");
+  const int nNo = (int)xs.size() / 3;
+  const int nEl = (int)iens.size() / 4;
+  const int tDof = 7;
+  com.nsd = 3;
+  com.nsymd = 6;
+  com.tnNo = nNo;
+  com.gtnNo = nNo;
+  com.nMsh = 1;
+  com.msh.resize(1);
+  com.nEq = 2;
+  com.eq.resize(2);
+  com.dt = getd("dt");
+  com.mvMsh = true;
+  com.dFlag = true;
+  com.sstEq = false;
+  com.pstEq = false;
+  auto& msh = com.msh[0];
+  msh.name = "pipe";
+  msh.eNoN = 4;
+  msh.nEl = nEl;
+  msh.gnEl = nEl;
+  msh.nNo = nNo;
+  msh.gnNo = nNo;
+  msh.IEN.resize(4, nEl);
+  msh.eId.resize(nEl);
+  com.dmnId.resize(nNo);
+  for (int a = 0; a < nNo; a++) com.dmnId(a) = 0;
+  for (int e = 0; e < nEl; e++) {
+    for (int a = 0; a < 4; a++) msh.IEN(a, e) = iens[4 * e + a];
+    msh.eId(e) = eid[e];
+    for (int a = 0; a < 4; a++) com.dmnId(iens[4 * e + a]) |= eid[e];  // read_msh.cpp:1519-1533
+  }
+  msh.gN.resize(nNo);
+  for (int a = 0; a < nNo; a++) msh.gN(a) = a;
+  nn::select_ele(com, msh);
+  msh.nFs = 1;
+  fs::init_fs_msh(com, msh);
+  const char* fnames[4] = {"inlet", "outlet", "wall_inlet", "wall_outlet"};
+  msh.fa.resize(4);
+  msh.nFa = 4;
+  for (int f = 0; f < 4; f++) setup_face(msh.fa[f], dir, fnames[f]);
+  com.x.resize(3, nNo);
+  for (int a = 0; a < nNo; a++)
+    for (int i = 0; i < 3; i++) com.x(i, a) = xs[3 * a + i];
+  com.Bf.resize(3, nNo);
+  mat_fun::ten_init(3);
+  using PP = consts::PhysicalProperyType;
+  // equation 0: FSI (first order), initialize.cpp:424-465
+  auto& eq = com.eq[0];
+  eq.phys = consts::EquationType::phys_FSI;
+  eq.sym = "FS";
+  eq.dof = 4;
+  eq.coupled = true;
+  eq.roInf = getd("rho_inf");
+  eq.am = 0.5 * (3.0 - eq.roInf) / (1.0 + eq.roInf);
+  eq.af = 1.0 / (1.0 + eq.roInf);
+  eq.beta = 0.25 * std::pow((1.0 + eq.am - eq.af), 2.0);
+  eq.gam = 0.5 + eq.am - eq.af;
+  eq.pNorm = std::numeric_limits<double>::max();
+  eq.s = 0;
+  eq.e = 3;
+  eq.minItr = geti("newton_min");
+  eq.maxItr = geti("newton_max");
+  eq.tol = getd("newton_tol");
+  eq.nDmn = 2;
+  eq.dmn.resize(2);
+  auto& fd = eq.dmn[0];
+  fd.Id = 0;
+  fd.phys = consts::EquationType::phys_fluid;
+  fd.prop[PP::fluid_density] = getd("rho_f");
+  fd.prop[PP::f_x] = 0.0;
+  fd.prop[PP::f_y] = 0.0;
+  fd.prop[PP::f_z] = 0.0;
+  fd.prop[PP::backflow_stab] = getd("backflow_beta");
+  fd.prop[PP::inverse_darcy_permeability] = 0.0;
+  fd.fluid_visc.viscType = consts::FluidViscosityModelType::viscType_Const;
+  fd.fluid_visc.mu_i = getd("mu");
+  auto& sd = eq.dmn[1];
+  sd.Id = 1;
+  sd.phys = consts::EquationType::phys_struct;
+  sd.prop[PP::solid_density] = getd("rho_s");
+  sd.prop[PP::elasticity_modulus] = getd("E");
+  sd.prop[PP::poisson_ratio] = getd("nu");
+  sd.prop[PP::damping] = 0.0;
+  sd.prop[PP::f_x] = 0.0;
+  sd.prop[PP::f_y] = 0.0;
+  sd.prop[PP::f_z] = 0.0;
+  sd.stM.isoType = consts::ConstitutiveModelType::stIso_nHook;
+  sd.stM.volType = consts::ConstitutiveModelType::stVol_ST91;
+  sd.stM.C10 = getd("C10");
+  sd.stM.Kpen = getd("Kpen");
+  // equation 1: mesh motion (second order), one domain over every element
+  auto& meq = com.eq[1];
+  meq.phys = consts::EquationType::phys_mesh;
+  meq.sym = "MS";
+  meq.dof = 3;
+  meq.coupled = true;
+  meq.roInf = getd("rho_inf");
+  meq.am = (2.0 - meq.roInf) / (1.0 + meq.roInf);
+  meq.af = 1.0 / (1.0 + meq.roInf);
+  meq.beta = 0.25 * std::pow((1.0 + meq.am - meq.af), 2.0);
+  meq.gam = 0.5 + meq.am - meq.af;
+  meq.pNorm = std::numeric_limits<double>::max();
+  meq.s = 4;
+  meq.e = 6;
+  meq.minItr = geti("mesh_newton_min");
+  meq.maxItr = geti("mesh_newton_max");
+  meq.tol = getd("mesh_newton_tol");
+  meq.nDmn = 1;
+  meq.dmn.resize(1);
+  auto& md = meq.dmn[0];
+  md.Id = -1;
+  md.phys = consts::EquationType::phys_mesh;
+  md.prop[PP::solid_density] = getd("mesh_rho");
+  md.prop[PP::elasticity_modulus] = getd("mesh_E");
+  md.prop[PP::poisson_ratio] = getd("mesh_nu");
+  md.prop[PP::damping] = 0.0;
+  md.prop[PP::f_x] = 0.0;
+  md.prop[PP::f_y] = 0.0;
+  md.prop[PP::f_z] = 0.0;
+  com.tDof = tDof;
+  com.dof = 4;
+  com.Ao.resize(tDof, nNo); com.An.resize(tDof, nNo);
+  com.Yo.resize(tDof, nNo); com.Yn.resize(tDof, nNo);
+  com.Do.resize(tDof, nNo); com.Dn.resize(tDof, nNo);
+  Array<double> Ag(tDof, nNo), Yg(tDof, nNo), Dg(tDof, nNo);
+
+  int nnz = 0;
+  lhsa_ns::lhsa(&sim, nnz);
+  com.lhs.nnz = nnz;
+  fsi_linear_solver::FSILS_commuType commu;
+  fsi_linear_solver::fsils_commu_create(commu, MPI_COMM_WORLD);
+  Vector<int> gNodes(nNo);
+  for (int a = 0; a < nNo; a++) gNodes(a) = a;
+  const int nFacesLS = 7;
+  fsi_linear_solver::fsils_lhs_create(com.lhs, commu, nNo, nNo, nnz, gNodes, com.rowPtr, com.colPtr, nFacesLS);
+  auto dir_face = [&](int lsPtr, const faceType& fa) {
+    Array<double> sVl(3, fa.nNo);
+    Vector<int> gN(fa.nNo);
+    for (int a = 0; a < fa.nNo; a++) gN(a) = fa.gN(a);
+    fsi_linear_solver::fsils_bc_create(com.lhs, lsPtr, fa.nNo, 3, fsi_linear_solver::BcType::BC_TYPE_Dir, gN, sVl);
+  };
+  dir_face(0, msh.fa[0]);
+  dir_face(1, msh.fa[2]);
+  dir_face(2, msh.fa[3]);
+  dir_face(4, msh.fa[0]);
+  dir_face(5, msh.fa[1]);
+  {  // baf_ini.cpp:197-227: every node of a solid domain
+    std::vector<int> sn;
+    for (int a = 0; a < nNo; a++)
+      if (all_fun::is_domain(com, eq, a, consts::EquationType::phys_struct)) sn.push_back(a);
+    Vector<int> gN((int)sn.size());
+    for (size_t k = 0; k < sn.size(); k++) gN((int)k) = sn[k];
+    fsi_linear_solver::fsils_bc_create(com.lhs, nFacesLS - 1, (int)sn.size(), 3, fsi_linear_solver::BcType::BC_TYPE_Dir,
+                                       gN);
+  }
+  fsi_linear_solver::fsils_ls_create(eq.FSILS, fsi_linear_solver::LinearSolverType::LS_TYPE_GMRES, getd("ls_rel_tol"),
+                                     getd("ls_abs_tol"), geti("ls_max_itr"), geti("ls_krylov_dim"));
+  fsi_linear_solver::fsils_ls_create(meq.FSILS, fsi_linear_solver::LinearSolverType::LS_TYPE_CG,
+                                     getd("mesh_ls_rel_tol"), getd("mesh_ls_abs_tol"), geti("mesh_ls_max_itr"), 1);
+  FsilsLinearAlgebra la0, la1;
+  eq.linear_algebra = &la0;
+  meq.linear_algebra = &la1;
+  eq.linear_algebra_preconditioner = consts::PreconditionerType::PREC_FSILS;
+  meq.linear_algebra_preconditioner = consts::PreconditionerType::PREC_FSILS;
+
+  auto prof = read_raw<double>(dir + "/inlet_prof.bin");
+  const double u_mean = getd("u_mean"), u_amp = getd("u_amp"), freq = getd("u_freq");
+  const int nSteps = geti("n_steps");
+  Vector<int> incL(nFacesLS);
+  Vector<double> res(nFacesLS);
+  Vector<double> hg(nNo);
+  std::ofstream log(out + "/log.txt");
+  log.precision(17);
+  double time = 0.0;
+  for (int cTS = 1; cTS <= nSteps; cTS++) {
+    time += com.dt;
+    com.cTS = cTS;
+    com.time = time;
+    com.cEq = 0;
+    for (auto& e : com.eq) {
+      e.itr = 0;
+      e.ok = false;
+    }
+    pic::picp(&sim);
+    const double w = 2.0 * M_PI * freq;
+    const double uc = u_mean + u_amp * std::sin(w * time);
+    const double duc = u_amp * w * std::cos(w * time);
+    for (int f : {2, 3, 0}) {  // FSI equation: wall rings, then the lumen inlet (its profile is 0 on the ring)
+      auto& fa = msh.fa[f];
+      for (int a = 0; a < fa.nNo; a++) {
+        int Ac = fa.gN(a);
+        for (int i = 0; i < 3; i++) { com.An(i, Ac) = 0.0; com.Yn(i, Ac) = 0.0; }
+        if (f == 0) {
+          com.An(2, Ac) = duc * prof[a];
+          com.Yn(2, Ac) = uc * prof[a];
+        }
+      }
+    }
+    for (int f : {0, 1}) {  // mesh equation: no mesh motion at the lumen ends
+      auto& fa = msh.fa[f];
+      for (int a = 0; a < fa.nNo; a++)
+        for (int i = 4; i < 7; i++) { com.An(i, fa.gN(a)) = 0.0; com.Yn(i, fa.gN(a)) = 0.0; }
+    }
+    int inner = 1;
+    while (true) {
+      const int iEq = com.cEq;
+      auto& ceq = com.eq[iEq];
+      pic::pici(&sim, Ag, Yg, Dg);
+      ls_ns::ls_alloc(com, ceq);
+      com.R = 0.0;
+      com.Val = 0.0;
+      eq_assem::global_eq_assem(com, sim.get_cep_mod(), msh, Ag, Yg, Dg);
+      incL = 0;
+      res = 0.0;
+      if (iEq == 0) {
+        hg = 0.0;
+        eq_assem::b_assem_neu_bc(com, msh.fa[1], hg, Yg);
+        incL(0) = incL(1) = incL(2) = 1;
+      } else {
+        incL(4) = incL(5) = incL(nFacesLS - 1) = 1;
+      }
+      if (P.count("dump_step") && cTS == geti("dump_step") && inner == geti("dump_iter")) {
+        write_raw(out + "/R_asm.bin", com.R.data(), (size_t)com.R.size());
+        write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
+        write_raw(out + "/Ag.bin", Ag.data(), (size_t)Ag.size());
+        write_raw(out + "/Yg.bin", Yg.data(), (size_t)Yg.size());
+        write_raw(out + "/Dg.bin", Dg.data(), (size_t)Dg.size());
+        write_raw(out + "/Do.bin", com.Do.data(), (size_t)com.Do.size());
+        write_raw(out + "/rowPtr.bin", com.rowPtr.data(), (size_t)com.rowPtr.size());
+        write_raw(out + "/colPtr.bin", com.colPtr.data(), (size_t)com.colPtr.size());
+      }
+      ls_ns::ls_solve(com, ceq, incL, res);
+      auto& RI = ceq.FSILS.RI;
+      log << "step " << cTS << " eq " << iEq << " iter " << ceq.itr << " iNorm " << RI.iNorm << " fNorm " << RI.fNorm
+          << " itr " << RI.itr << " suc " << RI.suc << "\n";
+      pic::picc(&sim);
+      bool all_ok = true;
+      for (auto& e : com.eq) all_ok = all_ok && e.ok;
+      if (all_ok) break;
+      inner++;
+    }
+    write_raw(out + "/An_" + std::to_string(cTS) + ".bin", com.An.data(), (size_t)com.An.size());
+    write_raw(out + "/Yn_" + std::to_string(cTS) + ".bin", com.Yn.data(), (size_t)com.Yn.size());
+    write_raw(out + "/Dn_" + std::to_string(cTS) + ".bin", com.Dn.data(), (size_t)com.Dn.size());
+    com.Ao = com.An;
+    com.Yo = com.Yn;
+    com.Do = com.Dn;
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::fprintf(stderr, "usage: %s CASE_DIR OUT_DIR\n", argv[0]);
@@ -356,6 +632,7 @@ int main(int argc, char** argv) {
   std::string dir = argv[1], out = argv[2];
   auto P = read_params(dir);
   if (P.count("mode") && P.at("mode") == "assemble_fsi") return assemble_fsi(dir, out, P);
+  if (P.count("mode") && P.at("mode") == "fsi_run") return run_fsi(dir, out, P);
   if (P.count("mode") && P.at("mode").rfind("assemble_", 0) == 0) return assemble_only(dir, out, P);
   auto getd = [&](const char* k) { return std::stod(P.at(k)); };
   auto geti = [&](const char* k) { return std::stoi(P.at(k)); };

@@ -83,6 +83,23 @@ def solid_props(rho=1.2, E=1.0e6, nu=0.45, dt=1e-3, rho_inf=0.5, volType=1, damp
     return SolidProps(rho, damping, (C.c_double * 3)(0.0, 0.0, 0.0), C10, Kpen, volType, dt, am, af, gam, beta)
 
 
+class FsiProps(C.Structure):
+    _fields_ = [("fluid", FluidProps), ("solid", SolidProps), ("mesh_E", C.c_double), ("mesh_nu", C.c_double),
+                ("mesh_rho", C.c_double), ("mesh_am", C.c_double), ("mesh_af", C.c_double),
+                ("mesh_gam", C.c_double), ("mesh_beta", C.c_double)]
+
+
+class FsiOpts(C.Structure):
+    _fields_ = [("minItr", C.c_int * 2), ("maxItr", C.c_int * 2), ("tol", C.c_double * 2), ("lsType", C.c_int * 2),
+                ("relTol", C.c_double * 2), ("absTol", C.c_double * 2), ("lsMaxItr", C.c_int * 2),
+                ("dimKry", C.c_int * 2), ("incL", C.c_void_p * 2), ("outletFace", C.c_int), ("outletH", C.c_double),
+                ("precision", C.c_int)]
+
+
+class DirichletSet(C.Structure):
+    _fields_ = [("n", C.c_int), ("nodes", C.c_void_p), ("Y", C.c_void_p), ("A", C.c_void_p)]
+
+
 class NewtonOpts(C.Structure):
     _fields_ = [("minItr", C.c_int), ("maxItr", C.c_int), ("tol", C.c_double), ("precision", C.c_int),
                 ("outletFace", C.c_int), ("outletH", C.c_double)]
@@ -223,6 +240,11 @@ class Context:
         self._check(lib().svgpu_neu_bc_fluid(self._h, int(face_id), C.byref(props), C.c_double(h), _ptr(Yg),
                                              _ptr(R), _ptr(Val)), "b_assem_neu_bc")
 
+    def b_assem_neu_bc_ale(self, face_id, props, h, tDof, Yg, Do, R, Val):
+        """b_assem_neu_bc on the moving mesh: face at x + Do(4..6), backflow relative to Yg(4..6)."""
+        self._check(lib().svgpu_neu_bc_fluid_ale(self._h, int(face_id), C.byref(props), C.c_double(h), int(tDof),
+                                                 _ptr(Yg), _ptr(Do), _ptr(R), _ptr(Val)), "b_assem_neu_bc_ale")
+
     # ---- learned preconditioner
     def gnn_create(self, node_features, seed=1):
         f = np.ascontiguousarray(node_features, dtype=np.float32)
@@ -310,6 +332,33 @@ class Context:
                                                 C.byref(iN), C.byref(pN), stats), "fluid_step")
         norms[0], norms[1] = iN.value, pN.value
         return [stats[i].as_dict() for i in range(it)]
+
+
+    def fsi_step(self, props, opts, dir_fsi, dir_mesh, Ao, Yo, Do, An, Yn, Dn, iNorm, pNorm):
+        """svgpu_fsi_step: one coupled FSI + mesh-motion time step.  dir_* are
+        (nodes, Y, A) triples; iNorm/pNorm are 2-element lists carried across steps.
+        Returns [(equation, stats dict)] per Newton iteration."""
+        cap = opts.maxItr[0] + opts.maxItr[1]
+        stats = (LsStats * cap)()
+        eqs = (C.c_int * cap)()
+        keep = []
+
+        def dset(d):
+            nodes = np.ascontiguousarray(d[0], dtype=np.int32)
+            Y = np.ascontiguousarray(d[1], dtype=np.float64)
+            A = np.ascontiguousarray(d[2], dtype=np.float64)
+            keep.extend((nodes, Y, A))
+            return DirichletSet(int(nodes.size), _ptr(nodes), _ptr(Y), _ptr(A))
+
+        dF, dM = dset(dir_fsi), dset(dir_mesh)
+        iN = (C.c_double * 2)(*iNorm)
+        pN = (C.c_double * 2)(*pNorm)
+        n = self._check(lib().svgpu_fsi_step(self._h, C.byref(props), C.byref(opts), C.byref(dF), C.byref(dM),
+                                             _ptr(Ao), _ptr(Yo), _ptr(Do), _ptr(An), _ptr(Yn), _ptr(Dn), iN, pN,
+                                             stats, eqs), "fsi_step")
+        iNorm[:] = list(iN)
+        pNorm[:] = list(pN)
+        return [(int(eqs[i]), stats[i].as_dict()) for i in range(n)]
 
 
 # ------------------------------------------------------------------ host driver
@@ -417,4 +466,91 @@ class PipeFluidSolver:
                                     self.An, self.Yn, self.Dn, self.norms)
         self.Ao[:] = self.An
         self.Yo[:] = self.Yn
+        return stats
+
+
+# Linear-solver faces of the FSI pipe, numbered as the reference's fsi_ls_ini numbers
+# them (baf_ini.cpp:190-227 over the FSI equation's BCs, then the mesh equation's, then
+# the structure-node face): 0 lumen inlet, 1 wall inlet ring, 2 wall outlet ring (FSI
+# Dirichlet), 3 unused (the outlet's plain Neumann BC has no face), 4 lumen inlet,
+# 5 lumen outlet (mesh Dirichlet), 6 every node of the solid domain (mesh).
+FSI_LS_FACES = 7
+FSI_INCL = (np.array([1, 1, 1, 0, 0, 0, 0], np.int32), np.array([0, 0, 0, 0, 1, 1, 1], np.int32))
+
+
+def fsi_props(rho_f=1.06, mu=0.04, backflow_beta=0.2, rho_s=1.2, E=1.0e6, nu=0.45, dt=1e-3, rho_inf=0.5,
+              mesh_E=1.0, mesh_nu=0.3, mesh_rho=0.0, volType=1):
+    """Both domains of the FSI equation carry its first-order constants
+    (initialize.cpp:424-430); the mesh equation is second order."""
+    fp = fluid_props(rho=rho_f, mu=mu, dt=dt, rho_inf=rho_inf, backflow_beta=backflow_beta)
+    sp = solid_props(rho_s, E, nu, dt, rho_inf, volType)
+    sp.am, sp.af, sp.gam, sp.beta = fp.am, fp.af, fp.gam, fp.beta
+    mam, maf, mgam, mbeta = genalpha_second_order(rho_inf)
+    return FsiProps(fp, sp, mesh_E, mesh_nu, mesh_rho, mam, maf, mgam, mbeta)
+
+
+class PipeFsiSolver:
+    """The FSI pipe case on the GPU (lumen plus a neo-Hookean wall annulus, linear-elastic
+    mesh motion): CSR set-up, the element domains, the linear-solver faces of both
+    equations (FSI_LS_FACES), the outlet face, and time stepping through svgpu_fsi_step
+    with parabolic pulsatile inflow, fixed wall rings and no mesh motion at the lumen
+    ends."""
+
+    def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, newton=(3, 3, 1e-11), mesh_newton=(3, 3, 1e-11),
+                 gmres=(1e-10, 1e-17, 100, 50), cg=(1e-10, 1e-17, 2000), rowPtr=None, colPtr=None,
+                 precision=SVGPU_FP64):
+        if mesh.eid is None:
+            raise ValueError("PipeFsiSolver needs an FSI pipe (mesh.make_pipe with nrs > 0)")
+        self.mesh = mesh
+        self.props = props or fsi_props()
+        self.ctx = Context(device)
+        nNo = mesh.nNo
+        if rowPtr is None:
+            rowPtr, colPtr = csr_pattern(nNo, mesh.ien)
+        self.rowPtr, self.colPtr = rowPtr, colPtr
+        F = mesh.faces
+        self.ctx.fsils_lhs_create(nNo, rowPtr, colPtr, FSI_LS_FACES)
+        solid = np.zeros(nNo, bool)
+        solid[mesh.ien[mesh.eid == 2].ravel()] = True
+        self.solid_nodes = np.nonzero(solid)[0].astype(np.int32)
+        for fa, name in ((0, "inlet"), (1, "wall_inlet"), (2, "wall_outlet"), (4, "inlet"), (5, "outlet")):
+            self.ctx.fsils_bc_create(fa, F[name].gN, 3, BC_TYPE_Dir)
+        self.ctx.fsils_bc_create(6, self.solid_nodes, 3, BC_TYPE_Dir)
+        self.ctx.fsils_ls_create(LS_TYPE_GMRES, *gmres)
+        self.ctx.mesh_create(mesh.x, mesh.ien)
+        self.ctx.mesh_domains(mesh.eid)
+        self.ctx.face_create(FACE_OUTLET, F["outlet"].ien, F["outlet"].gE)
+        self.opts = FsiOpts()
+        for q, (mn, mx, tol) in enumerate((newton, mesh_newton)):
+            self.opts.minItr[q], self.opts.maxItr[q], self.opts.tol[q] = mn, mx, tol
+        self.opts.lsType[0], self.opts.lsType[1] = LS_TYPE_GMRES, LS_TYPE_CG
+        self.opts.relTol[0], self.opts.absTol[0], self.opts.lsMaxItr[0], self.opts.dimKry[0] = gmres
+        self.opts.relTol[1], self.opts.absTol[1], self.opts.lsMaxItr[1] = cg
+        self.opts.dimKry[1] = -1
+        self._incl = FSI_INCL
+        self.opts.incL[0] = self._incl[0].ctypes.data
+        self.opts.incL[1] = self._incl[1].ctypes.data
+        self.opts.outletFace, self.opts.outletH = FACE_OUTLET, 0.0
+        self.opts.precision = precision
+        # FSI Dirichlet nodes: wall rings (zero) and the lumen inlet (profile, 0 on the ring)
+        rings = np.union1d(F["wall_inlet"].gN, F["wall_outlet"].gN)
+        self.dirF = np.union1d(rings, F["inlet"].gN).astype(np.int32)
+        self.profF = np.zeros(self.dirF.size)
+        inl = np.searchsorted(self.dirF, F["inlet"].gN)
+        self.profF[inl] = mesh.inlet_profile
+        self.dirM = np.union1d(F["inlet"].gN, F["outlet"].gN).astype(np.int32)
+        z = lambda: np.zeros((nNo, 7))  # noqa: E731
+        self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
+        self.iNorm, self.pNorm = [0.0, 0.0], [0.0, 0.0]
+        self.time = 0.0
+
+    def step(self, u_mean=15.0, u_amp=5.0, freq=1.0):
+        self.time += self.props.fluid.dt
+        dY, dA = inflow(self.profF, self.time, u_mean, u_amp, freq)
+        zm = np.zeros((self.dirM.size, 3))
+        stats = self.ctx.fsi_step(self.props, self.opts, (self.dirF, dY, dA), (self.dirM, zm, zm), self.Ao, self.Yo,
+                                  self.Do, self.An, self.Yn, self.Dn, self.iNorm, self.pNorm)
+        self.Ao[:] = self.An
+        self.Yo[:] = self.Yn
+        self.Do[:] = self.Dn
         return stats

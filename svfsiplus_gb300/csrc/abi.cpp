@@ -762,6 +762,16 @@ int backflow_device(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, 
 
 }  // namespace
 
+int svgpu::solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st) {
+  return solve_device(ctx, dof, R, Val, SVGPU_PREC_FSILS, incL, st);
+}
+
+int svgpu::solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st) {
+  return solve_device_mixed(ctx, R, Val32, incL, st);
+}
+
+svgpu::FluidConsts svgpu::fluid_consts_of(const svgpu_fluid_props* p) { return fluid_consts(p); }
+
 // =============================================================================== ABI
 extern "C" {
 
@@ -1119,6 +1129,15 @@ int svgpu_mesh_domains(svgpu_ctx* ctx, const int* eId) {
   SVGPU_CUDA(ctx, cudaMemcpy(m.boff.p, boff2.data(), boff2.size(), cudaMemcpyHostToDevice));
   m.split_fluid = sf;
   m.split_solid = ss;
+  // solid-domain nodes: dmnId(node) = OR of the eId of its elements (read_msh.cpp:1519-1533)
+  std::vector<uint8_t> solid(m.nNo, 0);
+  for (int q = 0; q < nEl; q++)
+    if (eid[perm2[q]] & 2)
+      for (int a = 0; a < 4; a++) solid[pien2[4 * (size_t)q + a]] = 1;
+  m.n_solid_nodes = 0;
+  for (int a = 0; a < m.nNo; a++) m.n_solid_nodes += solid[a];
+  if ((rc = to_device(ctx, m.solid_node, solid.data(), solid.size()))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
 }
 
@@ -1256,6 +1275,42 @@ int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* prop
   if (!dR) { if ((rc = to_device(ctx, ctx->stage1, (const double*)R, n4))) return rc; Rd = ctx->stage1.p; }
   if (!dV) { if ((rc = to_device(ctx, ctx->stage2, (const double*)Val, nv))) return rc; Vd = ctx->stage2.p; }
   if ((rc = backflow_device(ctx, faceId, props, h, Ygd, Rd, Vd, nullptr))) return rc;
+  if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, n4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_neu_bc_fluid_ale(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h, int tDof,
+                           const double* Yg, const double* Do, double* R, double* Val) {
+  if (!ctx || !props || !Yg || !Do || !R || !Val) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "neu_bc before mesh_create");
+  if (tDof < 7) return set_err(ctx, SVGPU_EINVAL, "neu_bc_ale: tDof must hold the mesh rows 4..6");
+  if (misaligned_device(Yg) || misaligned_device(Do) || misaligned_device(R) || misaligned_device(Val))
+    return set_err(ctx, SVGPU_EINVAL, "neu_bc_ale: device arrays must be 16-byte aligned");
+  auto it = ctx->mfaces.find(faceId);
+  if (it == ctx->mfaces.end()) return set_err(ctx, SVGPU_EINVAL, "unknown face id");
+  MeshFace& f = *it->second;
+  const long n4 = 4L * ctx->nNo, nt = (long)tDof * ctx->nNo;
+  const size_t nv = (size_t)ctx->nnz * 16;
+  int rc;
+  DevBuf<double> y, d;
+  const double* Ygd = Yg;
+  const double* Dod = Do;
+  if (!is_device_ptr(Yg)) { if ((rc = to_device(ctx, y, Yg, nt))) return rc; Ygd = y.p; }
+  if (!is_device_ptr(Do)) { if ((rc = to_device(ctx, d, Do, nt))) return rc; Dod = d.p; }
+  const bool dR = is_device_ptr(R), dV = is_device_ptr(Val);
+  double* Rd = R;
+  double* Vd = Val;
+  if (!dR) { if ((rc = to_device(ctx, ctx->stage1, (const double*)R, n4))) return rc; Rd = ctx->stage1.p; }
+  if (!dV) { if ((rc = to_device(ctx, ctx->stage2, (const double*)Val, nv))) return rc; Vd = ctx->stage2.p; }
+  const FluidConsts c = fluid_consts(props);
+  for (size_t k = 0; k + 1 < f.color_start.size(); k++) {
+    launch_neu_backflow_ale(ctx->stream, c, h, f.color_start[k], f.color_start[k + 1] - f.color_start[k], f.fien.p,
+                            f.inner.p, f.boff.p, ctx->mesh->x4.p, tDof, Ygd, Dod, ctx->rowPtr.p, Rd, Vd);
+    ctx->launches++;
+  }
   if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(R, Rd, n4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

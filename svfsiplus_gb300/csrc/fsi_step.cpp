@@ -1,0 +1,236 @@
+// The coupled ALE FSI time step (svgpu_fsi_step): iterate_solution (main.cpp:292-762)
+// with two coupled equations, the FSI equation (dof 4, state rows 0..3) and the
+// mesh-motion equation (dof 3, rows 4..6).  Every operation runs on the device; the
+// host keeps the reference's control flow: which equation is current, the Newton
+// counters and the picc convergence test (pic.cpp:235-327).
+//
+// The two equations keep their own linear-solver settings (each equation has its own
+// FSILS handle in the reference, ls.cpp:40).  While the mesh equation solves, its
+// settings and its own Krylov work are swapped into the context, so the FSI solver's
+// captured restart-cycle graph and the mesh solver's CG graphs both stay valid across
+// the alternation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <utility>
+
+#include "internal.h"
+
+using namespace svgpu;
+
+namespace {
+
+struct LsSettings {
+  int lsType;
+  double relTol, absTol;
+  int mItr, sD;
+};
+
+// fsils_ls_create defaults (ls.cpp:50-79) for the arguments left negative
+LsSettings ls_settings(int lsType, double relTol, double absTol, int maxItr, int dimKry) {
+  const bool cg = lsType == SVGPU_LS_CG;
+  LsSettings s;
+  s.lsType = lsType;
+  s.relTol = relTol >= 0 ? relTol : (cg ? 1e-2 : 0.1);
+  s.absTol = absTol >= 0 ? absTol : 1e-10;
+  s.mItr = maxItr > 0 ? maxItr : (cg ? 1000 : 4);
+  s.sD = cg ? 1 : (dimKry > 0 ? dimKry : 250);
+  return s;
+}
+
+void swap_in(svgpu_ctx* ctx, LsSettings& s, KrylovWork& kw) {
+  std::swap(ctx->lsType, s.lsType);
+  std::swap(ctx->relTol, s.relTol);
+  std::swap(ctx->absTol, s.absTol);
+  std::swap(ctx->mItr, s.mItr);
+  std::swap(ctx->sD, s.sD);
+  std::swap(ctx->kw, kw);
+}
+
+bool is_zero_ref(double v) {  // utils::is_zero (utils.cpp:170-189)
+  const double eps = 2.220446049250313e-16;
+  const double a = std::fabs(v);
+  return a / std::fmax(a, eps) < 10.0 * eps;
+}
+
+int upload_dir(svgpu_ctx* ctx, const svgpu_dirichlet_set* d, DevBuf<int>& nodes, DevBuf<double>& Y,
+               DevBuf<double>& A) {
+  if (!d || d->n == 0) return SVGPU_OK;
+  if (d->n < 0 || !d->nodes || !d->Y || !d->A) return set_err(ctx, SVGPU_EINVAL, "fsi_step: bad Dirichlet set");
+  std::vector<int> h;
+  int rc = to_host(ctx, h, d->nodes, d->n);
+  if (rc) return rc;
+  for (int k = 0; k < d->n; k++)
+    if (h[k] < 0 || h[k] >= ctx->nNo) return set_err(ctx, SVGPU_EINVAL, "fsi_step: Dirichlet node out of range");
+  if ((rc = to_device(ctx, nodes, h.data(), h.size()))) return rc;
+  if ((rc = to_device(ctx, Y, d->Y, 3L * d->n))) return rc;
+  return to_device(ctx, A, d->A, 3L * d->n);
+}
+
+}  // namespace
+
+extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, const svgpu_fsi_opts* opts,
+                              const svgpu_dirichlet_set* dir_fsi, const svgpu_dirichlet_set* dir_mesh,
+                              const double* Ao, const double* Yo, const double* Do, double* An, double* Yn,
+                              double* Dn, double* iNorm, double* pNorm, svgpu_ls_stats* stats, int* stat_eq) {
+  if (!ctx || !props || !opts || !Ao || !Yo || !Do || !An || !Yn || !Dn || !iNorm || !pNorm) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (!ctx->mesh || !ctx->mesh->solid_node.p)
+    return set_err(ctx, SVGPU_ESTATE, "fsi_step before mesh_create / mesh_domains");
+  if (ctx->nFaces > 0 && (!opts->incL[0] || !opts->incL[1]))
+    return set_err(ctx, SVGPU_EINVAL, "fsi_step: incL of both equations required");
+  for (int q = 0; q < 2; q++) {
+    if (opts->maxItr[q] < 1) return set_err(ctx, SVGPU_EINVAL, "fsi_step: maxItr < 1");
+    if (opts->lsType[q] != SVGPU_LS_GMRES && opts->lsType[q] != SVGPU_LS_CG)
+      return set_err(ctx, SVGPU_EINVAL, "fsi_step: GMRES or CG per equation");
+    if (opts->lsType[q] == SVGPU_LS_GMRES && opts->dimKry[q] > 250)
+      return set_err(ctx, SVGPU_EINVAL, "fsi_step: Krylov dimension above 250");
+  }
+  if (opts->precision != SVGPU_FP64 && opts->precision != SVGPU_MIXED)
+    return set_err(ctx, SVGPU_EINVAL, "fsi_step: bad precision");
+  const bool mixed = opts->precision == SVGPU_MIXED;
+  if (mixed && opts->lsType[0] != SVGPU_LS_GMRES)
+    return set_err(ctx, SVGPU_EINVAL, "fsi_step: the mixed-precision FSI solve is (F)GMRES");
+  if (opts->outletFace >= 0 && !ctx->mfaces.count(opts->outletFace))
+    return set_err(ctx, SVGPU_EINVAL, "fsi_step: unknown outlet face");
+  if (!ctx->fsi) ctx->fsi = std::make_unique<FsiWork>();
+  FsiWork& w = *ctx->fsi;
+  MeshData& m = *ctx->mesh;
+  const int nNo = ctx->nNo;
+  const long n7 = 7L * nNo;
+  int rc;
+  if ((rc = to_device(ctx, w.Ao, Ao, n7))) return rc;
+  if ((rc = to_device(ctx, w.Yo, Yo, n7))) return rc;
+  if ((rc = to_device(ctx, w.Do, Do, n7))) return rc;
+  SVGPU_CUDA(ctx, w.An.resize(n7));
+  SVGPU_CUDA(ctx, w.Yn.resize(n7));
+  SVGPU_CUDA(ctx, w.Dn.resize(n7));
+  SVGPU_CUDA(ctx, w.Ag.resize(n7));
+  SVGPU_CUDA(ctx, w.Yg.resize(n7));
+  SVGPU_CUDA(ctx, w.Dg.resize(n7));
+  SVGPU_CUDA(ctx, w.R3.resize(3L * nNo));
+  SVGPU_CUDA(ctx, w.Val9.resize((size_t)9 * ctx->nnz));
+  SVGPU_CUDA(ctx, ctx->R.resize(4L * nNo));
+  SVGPU_CUDA(ctx, ctx->Val.resize((size_t)16 * ctx->nnz));
+  if (mixed) SVGPU_CUDA(ctx, ctx->Val32.resize((size_t)16 * ctx->nnz));
+  if ((rc = upload_dir(ctx, dir_fsi, w.dirF, w.dirYF, w.dirAF))) return rc;
+  if ((rc = upload_dir(ctx, dir_mesh, w.dirM, w.dirYM, w.dirAM))) return rc;
+
+  const svgpu_fluid_props& fp = props->fluid;
+  const double dt = fp.dt;
+  const double gam[2] = {fp.gam, props->mesh_gam}, beta[2] = {fp.beta, props->mesh_beta};
+  const double am[2] = {fp.am, props->mesh_am}, af[2] = {fp.af, props->mesh_af};
+  FsiCoefs c;
+  c.dt = dt;
+  for (int q = 0; q < 2; q++) {
+    c.pred_a[q] = (gam[q] - 1.0) / gam[q];
+    c.pred_d[q] = dt * dt * (0.5 * gam[q] - beta[q]) / (gam[q] - 1.0);
+    c.ini[q][0] = 1.0 - am[q];
+    c.ini[q][1] = am[q];
+    c.ini[q][2] = 1.0 - af[q];
+    c.ini[q][3] = af[q];
+  }
+  // picp and the strong Dirichlet values (set_bc_dir, set_bc.cpp:794-1004)
+  phase_mark(ctx, PH_OTHER);
+  launch_fsi_predict(ctx->stream, nNo, c, w.Ao.p, w.Yo.p, w.Do.p, w.An.p, w.Yn.p, w.Dn.p);
+  launch_fsi_dirichlet(ctx->stream, dir_fsi ? dir_fsi->n : 0, 0, w.dirF.p, w.dirYF.p, w.dirAF.p, w.An.p, w.Yn.p);
+  launch_fsi_dirichlet(ctx->stream, dir_mesh ? dir_mesh->n : 0, 4, w.dirM.p, w.dirYM.p, w.dirAM.p, w.An.p, w.Yn.p);
+  ctx->launches += 3;
+
+  LsSettings ls_fsi = ls_settings(opts->lsType[0], opts->relTol[0], opts->absTol[0], opts->lsMaxItr[0],
+                                  opts->dimKry[0]);
+  LsSettings ls_mesh = ls_settings(opts->lsType[1], opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
+                                   opts->dimKry[1]);
+  const LsSettings saved{ctx->lsType, ctx->relTol, ctx->absTol, ctx->mItr, ctx->sD};
+  ctx->lsType = ls_fsi.lsType;
+  ctx->relTol = ls_fsi.relTol;
+  ctx->absTol = ls_fsi.absTol;
+  ctx->mItr = ls_fsi.mItr;
+  ctx->sD = ls_fsi.sD;
+  ctx->resident_mixed = false;
+
+  svgpu_solid_props sp = props->solid;
+  int itr[2] = {0, 0};
+  bool ok[2] = {false, false};
+  int cEq = 0, total = 0;
+  const int cap = opts->maxItr[0] + opts->maxItr[1];
+  rc = SVGPU_OK;
+  for (;;) {
+    itr[cEq]++;
+    phase_mark(ctx, PH_OTHER);
+    launch_fsi_initiate(ctx->stream, nNo, c, w.Ao.p, w.An.p, w.Yo.p, w.Yn.p, w.Do.p, w.Dn.p, w.Ag.p, w.Yg.p, w.Dg.p);
+    ctx->launches++;
+    svgpu_ls_stats st;
+    std::memset(&st, 0, sizeof(st));
+    phase_mark(ctx, PH_ASSEMBLY);
+    if (cEq == 0) {
+      // ls_alloc zeroes R and Val (ls.cpp:51-61); construct_fsi + the outlet's Neumann term
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, 4L * nNo * sizeof(double), ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val.p, 0, (size_t)16 * ctx->nnz * sizeof(double), ctx->stream));
+      if ((rc = svgpu_construct_fsi(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, ctx->Val.p))) break;
+      if (opts->outletFace >= 0) {
+        MeshFace& f = *ctx->mfaces[opts->outletFace];
+        const FluidConsts fc = fluid_consts_of(&fp);
+        for (size_t k = 0; k + 1 < f.color_start.size(); k++) {
+          launch_neu_backflow_ale(ctx->stream, fc, opts->outletH, f.color_start[k],
+                                  f.color_start[k + 1] - f.color_start[k], f.fien.p, f.inner.p, f.boff.p, m.x4.p, 7,
+                                  w.Yg.p, w.Do.p, ctx->rowPtr.p, ctx->R.p, ctx->Val.p);
+          ctx->launches++;
+        }
+      }
+      if (mixed) {
+        launch_f64_to_f32(ctx->stream, (long)16 * ctx->nnz, ctx->Val.p, ctx->Val32.p);
+        ctx->launches++;
+        rc = solve_mixed(ctx, ctx->R.p, ctx->Val32.p, opts->incL[0], &st);
+      } else {
+        rc = solve_fp64(ctx, 4, ctx->R.p, ctx->Val.p, opts->incL[0], &st);
+      }
+      if (rc) break;
+      phase_mark(ctx, PH_OTHER);
+      launch_fsi_correct(ctx->stream, nNo, gam[0] * dt, beta[0] * dt * dt, ctx->R.p, m.solid_node.p, w.An.p, w.Yn.p,
+                         w.Dn.p);
+      ctx->launches++;
+    } else {
+      SVGPU_CUDA(ctx, cudaMemsetAsync(w.R3.p, 0, 3L * nNo * sizeof(double), ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemsetAsync(w.Val9.p, 0, (size_t)9 * ctx->nnz * sizeof(double), ctx->stream));
+      rc = svgpu_construct_mesh(ctx, props->mesh_E, props->mesh_nu, props->mesh_rho, dt, am[1], af[1], beta[1], 7, 4,
+                                w.Ag.p, w.Dg.p, w.Do.p, w.R3.p, w.Val9.p);
+      if (rc) break;
+      swap_in(ctx, ls_mesh, w.kw_mesh);
+      rc = solve_fp64(ctx, 3, w.R3.p, w.Val9.p, opts->incL[1], &st);
+      swap_in(ctx, ls_mesh, w.kw_mesh);
+      if (rc) break;
+      phase_mark(ctx, PH_OTHER);
+      launch_mesh_correct(ctx->stream, nNo, gam[1] * dt, beta[1] * dt * dt, w.R3.p, w.An.p, w.Yn.p, w.Dn.p);
+      ctx->launches++;
+    }
+    if (stats && total < cap) stats[total] = st;
+    if (stat_eq && total < cap) stat_eq[total] = cEq;
+    total++;
+    // picc convergence test (pic.cpp:235-281)
+    const double eps = 2.220446049250313e-16;
+    double iN = st.iNorm;
+    if (is_zero_ref(iN)) iN = eps;
+    if (is_zero_ref(iNorm[cEq])) iNorm[cEq] = iN;
+    if (itr[cEq] == 1) pNorm[cEq] = iN / iNorm[cEq];
+    const double r1 = iN / iNorm[cEq];
+    const bool l1 = itr[cEq] >= opts->maxItr[cEq], l2 = r1 <= opts->tol[cEq], l3 = r1 <= opts->tol[cEq] * pNorm[cEq],
+               l4 = itr[cEq] >= opts->minItr[cEq];
+    if (l1 || ((l2 || l3) && l4)) ok[cEq] = true;
+    if (ok[0] && ok[1]) break;
+    // both equations are coupled: the next one in turn (pic.cpp:292-318)
+    cEq = (cEq + 1) % 2;
+  }
+  ctx->lsType = saved.lsType;
+  ctx->relTol = saved.relTol;
+  ctx->absTol = saved.absTol;
+  ctx->mItr = saved.mItr;
+  ctx->sD = saved.sD;
+  if (rc) return rc;
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(An, w.An.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, w.Yn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, w.Dn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  phase_mark(ctx, PH_COUNT);
+  return total;
+}

@@ -85,6 +85,10 @@ struct MeshData {
   // per colour: fluid elements [color_start[k], split_fluid[k]), solid elements
   // [split_fluid[k], split_solid[k]); the rest belong to no assembled domain
   std::vector<int> split_fluid, split_solid;
+  // per node: 1 if an element of the solid domain holds it (all_fun::is_domain with
+  // dmnId, all_fun.cpp:931-961; read_msh.cpp:1519-1533); set by svgpu_mesh_domains
+  DevBuf<uint8_t> solid_node;
+  int n_solid_nodes = 0;
 };
 
 struct KrylovWork {
@@ -102,6 +106,27 @@ struct KrylovWork {
 };
 
 struct AmgState;
+
+// Work of the coupled FSI time step (fsi_step.cpp): the 7-row state arrays, the mesh
+// equation's system and its own Krylov work (swapped into ctx->kw while it solves, so
+// that the captured FSI and mesh solver graphs both stay valid).
+struct FsiWork {
+  DevBuf<double> Ao, Yo, Do, An, Yn, Dn, Ag, Yg, Dg;  // (7, nNo)
+  DevBuf<double> R3, Val9;                             // mesh equation: (3, nNo), (9, nnz)
+  DevBuf<int> dirF, dirM;                              // Dirichlet node lists (FSI rows 0..2, mesh rows 4..6)
+  DevBuf<double> dirYF, dirAF, dirYM, dirAM;           // their values (3, n)
+  KrylovWork kw_mesh;
+  int lsType = SVGPU_LS_CG, mItr = 1000, sD = 1;
+  double relTol = 1e-2, absTol = 1e-10;
+};
+
+// Generalised-alpha coefficients of the two equations of the FSI time step
+// (0: FSI, rows 0..3; 1: mesh, rows 4..6).
+struct FsiCoefs {
+  double dt;
+  double pred_a[2], pred_d[2];  // picp: (gam-1)/gam and dt^2 (gam/2 - beta)/(gam-1)
+  double ini[2][4];             // pici: 1-am, am, 1-af, af
+};
 
 // Work of the NS block solver (ns.cpp): the split operator blocks, the outer
 // iteration's vectors, and the inner GMRES work swapped into ctx->kw while it runs.
@@ -219,6 +244,7 @@ struct svgpu_ctx {
   int ns_gm_mItr = 2, ns_gm_sD = 100, ns_cg_mItr = 500;  // fsils_ls_create defaults (ls.cpp:50-58)
   svgpu::DevBuf<int> cg_f;              // CG: stop, last_i, suc, next iteration
   std::unique_ptr<svgpu::GnnState> gnn;
+  std::unique_ptr<svgpu::FsiWork> fsi;  // coupled FSI time step
   std::unique_ptr<struct svgpu::AmgState> amg;
   const float* amg_val0 = nullptr;  // level-0 matrix of the current numeric set-up
   // 0: GMRES + diagonal preconditioner (the reference's method)
@@ -306,6 +332,12 @@ void launch_schur_cg_iteration(cudaStream_t s, int nNo, const int* rowPtr, const
 int schur_cg_device(svgpu_ctx* ctx, const double* G, const double* D, const double* L, double* R, double relTol,
                     double absTol, int mItr, int* itr);
 int ns_solve_device(svgpu_ctx* ctx, const double* Val, double* R, svgpu_ls_stats* st);
+// fsils_solve with the diagonal preconditioner on device arrays (abi.cpp), with the
+// context's current linear-solver settings
+int solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st);
+// the mixed-precision solve of a dof-4 system with an FP32 tangent (abi.cpp), with the
+// context's solver mode
+int solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st);
 // k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
 int cg_parts(long n);
 void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
@@ -373,6 +405,7 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
                          const int* fien, const int* inner, const uint8_t* boff, const double* x4,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32);
+FluidConsts fluid_consts_of(const svgpu_fluid_props* p);
 struct SolidConsts {
   double rho, damping, f[3], C10, Kpen;
   int volType;
@@ -388,6 +421,21 @@ void launch_struct_assembly(cudaStream_t st, int dof, const SolidConsts& c, int 
 void launch_mesh_assembly(cudaStream_t st, const MeshConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
                           const int* elem_id, const double* x4, int tDof, int s, const double* Ag, const double* Dg,
                           const double* Do, const int* rowPtr, double* R, double* Val, int* errflag);
+void launch_neu_backflow_ale(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne, const int* fien,
+                             const int* inner, const uint8_t* boff, const double* x4, int ld, const double* Yg,
+                             const double* Do, const int* rowPtr, double* R, double* Val64);
+// ---- k_fsi.cu: generalised-alpha updates of the 7-row FSI state ------------------
+void launch_fsi_predict(cudaStream_t s, int nNo, const FsiCoefs& c, const double* Ao, const double* Yo,
+                        const double* Do, double* An, double* Yn, double* Dn);
+void launch_fsi_dirichlet(cudaStream_t s, int n, int row0, const int* nodes, const double* dirY, const double* dirA,
+                          double* An, double* Yn);
+void launch_fsi_initiate(cudaStream_t s, int nNo, const FsiCoefs& c, const double* Ao, const double* An,
+                         const double* Yo, const double* Yn, const double* Do, const double* Dn, double* Ag,
+                         double* Yg, double* Dg);
+void launch_fsi_correct(cudaStream_t s, int nNo, double c0, double c1, const double* R, const uint8_t* solid,
+                        double* An, double* Yn, double* Dn);
+void launch_mesh_correct(cudaStream_t s, int nNo, double c0, double c1, const double* R, double* An, double* Yn,
+                         double* Dn);
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn);
 void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,

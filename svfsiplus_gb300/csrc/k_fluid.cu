@@ -351,10 +351,15 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 // Outlet faces: Neumann value h plus backflow stabilisation (b_fluid), one thread
 // per face triangle, faces grouped by colour.
 template <typename TV>
+// With Do != nullptr (moving mesh, com_mod.mvMsh): state arrays have ld rows per node,
+// the face is placed at x + Do(4..6) (gnnb, nn.cpp:627-640) and the backflow term
+// convects with the velocity relative to the mesh, Yg(0..2) - Yg(4..6) (b_fluid,
+// fluid.cpp:79-84).
 __global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, const int* __restrict__ fien,
                                     const int* __restrict__ inner, const uint8_t* __restrict__ boff,
-                                    const double* __restrict__ x4, const double* __restrict__ Yg,
-                                    const int* __restrict__ rowPtr, double* __restrict__ R, TV* __restrict__ Val) {
+                                    const double* __restrict__ x4, int ld, const double* __restrict__ Yg,
+                                    const double* __restrict__ Do, const int* __restrict__ rowPtr,
+                                    double* __restrict__ R, TV* __restrict__ Val) {
   const int le = blockIdx.x * blockDim.x + threadIdx.x;
   if (le >= ne) return;
   const int e = e0 + le;
@@ -366,13 +371,14 @@ __global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, con
   // normal (gnnb, nn.cpp:727-760): d x/d xi_1 = x0 - x2, d x/d xi_2 = x1 - x2
   double xa[3][3];
   for (int a = 0; a < 3; a++)
-    for (int i = 0; i < 3; i++) xa[a][i] = x4[4L * nd[a] + i];
+    for (int i = 0; i < 3; i++) xa[a][i] = x4[4L * nd[a] + i] + (Do ? Do[(long)ld * nd[a] + 4 + i] : 0.0);
   double g1[3], g2[3];
   for (int i = 0; i < 3; i++) { g1[i] = xa[0][i] - xa[2][i]; g2[i] = xa[1][i] - xa[2][i]; }
   double n[3] = {g1[1] * g2[2] - g1[2] * g2[1], g1[2] * g2[0] - g1[0] * g2[2], g1[0] * g2[1] - g1[1] * g2[0]};
   const int in = inner[e];
   double nv = 0.0;
-  for (int i = 0; i < 3; i++) nv += n[i] * (xa[0][i] - x4[4L * in + i]);
+  for (int i = 0; i < 3; i++)
+    nv += n[i] * (xa[0][i] - (x4[4L * in + i] + (Do ? Do[(long)ld * in + 4 + i] : 0.0)));
   if (nv < 0.0) for (int i = 0; i < 3; i++) n[i] = -n[i];
   const double Jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
   for (int i = 0; i < 3; i++) n[i] /= Jac;
@@ -380,13 +386,22 @@ __global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, con
   const double wl = w * c.af * c.gam * c.dt;
   double yl[3][3];
   for (int a = 0; a < 3; a++)
-    for (int i = 0; i < 3; i++) yl[a][i] = Yg[4L * nd[a] + i];
+    for (int i = 0; i < 3; i++) yl[a][i] = Yg[(long)ld * nd[a] + i];
+  double ml[3][3] = {{0}};  // mesh velocity at the face nodes (moving mesh only)
+  if (Do)
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 3; i++) ml[a][i] = Yg[(long)ld * nd[a] + 4 + i];
   double lR[3][3] = {{0}}, lk[3][3] = {{0}};
   for (int g = 0; g < 3; g++) {
     const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
-    double y[3] = {0, 0, 0};
+    double y[3] = {0, 0, 0}, ym[3] = {0, 0, 0};
     for (int a = 0; a < 3; a++)
-      for (int i = 0; i < 3; i++) y[i] += N[a] * yl[a][i];
+      for (int i = 0; i < 3; i++) {
+        y[i] += N[a] * yl[a][i];
+        ym[i] += N[a] * ml[a][i];
+      }
+    if (Do)
+      for (int i = 0; i < 3; i++) y[i] = y[i] - ym[i];
     double udn = y[0] * n[0] + y[1] * n[1] + y[2] * n[2];
     udn = 0.5 * c.beta_bf * c.rho * (udn - fabs(udn));
     const double hh = h * (N[0] + N[1] + N[2]);
@@ -494,9 +509,19 @@ void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0,
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
   if (Val64)
-    neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, Yg, rowPtr, R, Val64);
+    neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, 4, Yg, nullptr, rowPtr, R,
+                                                     Val64);
   else
-    neu_backflow_kernel<float><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, Yg, rowPtr, R, Val32);
+    neu_backflow_kernel<float><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, 4, Yg, nullptr, rowPtr, R,
+                                                    Val32);
+}
+
+void launch_neu_backflow_ale(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne, const int* fien,
+                             const int* inner, const uint8_t* boff, const double* x4, int ld, const double* Yg,
+                             const double* Do, const int* rowPtr, double* R, double* Val64) {
+  if (ne <= 0) return;
+  const int grid = (ne + 127) / 128;
+  neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, ld, Yg, Do, rowPtr, R, Val64);
 }
 
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,

@@ -43,6 +43,8 @@ class PipeMesh:
     length: float
     inlet_profile: np.ndarray  # (nNo_inlet,) parabolic profile 1 - r^2/Rwall^2 at inlet.gN
     params: dict
+    # FSI pipes only: element domains (mshType eId: bit 0 fluid, bit 1 solid)
+    eid: np.ndarray | None = None
 
     @property
     def nNo(self) -> int:
@@ -53,11 +55,13 @@ class PipeMesh:
         return int(self.ien.shape[0])
 
 
-def _cross_section(nc: int, nr: int, radius: float, core_frac: float = 0.55):
-    """O-grid quads of the unit-radius disc scaled by ``radius``.
+def _cross_section(nc: int, nr: int, radius: float, core_frac: float = 0.55, nrs: int = 0,
+                   thickness: float = 0.0):
+    """O-grid quads of the unit-radius disc scaled by ``radius``, optionally followed by
+    ``nrs`` rings of quads of a wall annulus from ``radius`` to ``radius + thickness``.
 
-    Returns node xy (nN, 2), quads (nQ, 4) counter-clockwise, and the ids of the
-    nodes on the outer circle (in angular order)."""
+    Returns node xy (nN, 2), quads (nQ, 4) counter-clockwise, the ids of the nodes on
+    the circle of radius ``radius`` (in angular order) and on the outermost circle."""
     a = core_frac * radius / np.sqrt(2.0)
     # core square nodes (nc+1)^2
     t = np.linspace(-a, a, nc + 1)
@@ -99,13 +103,18 @@ def _cross_section(nc: int, nr: int, radius: float, core_frac: float = 0.55):
         nodes.append(ps + s * (pc - ps))
         ring_ids.append(base + np.arange(nloop))
         base += nloop
+    unit = np.stack([np.cos(ang), np.sin(ang)], axis=1)
+    for j in range(1, nrs + 1):
+        nodes.append((radius + thickness * j / nrs) * unit)
+        ring_ids.append(base + np.arange(nloop))
+        base += nloop
     xy = np.concatenate(nodes, axis=0)
-    for j in range(nr):
+    for j in range(nr + nrs):
         inner, outer = ring_ids[j], ring_ids[j + 1]
         for k in range(nloop):
             k1 = (k + 1) % nloop
             quads.append((inner[k], inner[k1], outer[k1], outer[k]))
-    return xy, np.asarray(quads, dtype=np.int64), ring_ids[-1]
+    return xy, np.asarray(quads, dtype=np.int64), ring_ids[nr], ring_ids[-1]
 
 
 def _split_prisms(bot: np.ndarray, top: np.ndarray) -> np.ndarray:
@@ -167,10 +176,18 @@ def _match_faces(tri: np.ndarray, ien: np.ndarray, cand: np.ndarray, nNo: int) -
 
 
 def make_pipe(nc: int, nr: int, nz: int, radius: float = 0.5, length: float = 5.0,
-              perturb_modes: int = 0, seed: int = 20261203, max_amp: float = 0.1) -> PipeMesh:
+              perturb_modes: int = 0, seed: int = 20261203, max_amp: float = 0.1,
+              nrs: int = 0, thickness: float = 0.1) -> PipeMesh:
     """Build the tet pipe.  Nodes are numbered layer by layer (z outer), which keeps
-    the CSR bandwidth of the block matrix near one cross-section."""
-    xy, quads, wall_loop = _cross_section(nc, nr, radius)
+    the CSR bandwidth of the block matrix near one cross-section.
+
+    With ``nrs > 0`` the pipe gets a solid wall annulus of ``nrs`` element rings from
+    ``radius`` to ``radius + thickness`` that shares its inner surface nodes with the
+    lumen (the monolithic FSI set-up of the reference's fsi/pipe_3d case):
+    ``eid`` marks fluid (1) and solid (2) elements, the faces 'inlet'/'outlet' are the
+    lumen's, 'wall' is the fluid-solid interface (owner: the fluid tet), and
+    'wall_inlet', 'wall_outlet', 'wall_outer' bound the solid."""
+    xy, quads, wall_loop, outer_loop = _cross_section(nc, nr, radius, nrs=nrs, thickness=thickness)
     nxy = xy.shape[0]
     z = np.linspace(0.0, length, nz + 1)
     x = np.empty(((nz + 1) * nxy, 3))
@@ -203,6 +220,8 @@ def make_pipe(nc: int, nr: int, nz: int, radius: float = 0.5, length: float = 5.
     tB = np.where(alt[:, None], q[:, [0, 2, 3]], q[:, [1, 2, 3]])
     tri2d = np.concatenate([tA, tB], axis=0)
     ntri = tri2d.shape[0]
+    nq_fluid = nc * nc + nr * 4 * nc
+    tri_solid = (np.arange(ntri) % q.shape[0]) >= nq_fluid
 
     tets = []
     for k in range(nz):
@@ -214,15 +233,43 @@ def make_pipe(nc: int, nr: int, nz: int, radius: float = 0.5, length: float = 5.
 
     # faces
     per_layer = 3 * ntri
-    inlet_tri = tri2d.copy()
-    outlet_tri = tri2d + nz * nxy
+    elem_solid = np.tile(np.repeat(tri_solid, 3), nz)
+    inlet_tri = tri2d[~tri_solid].copy()
+    outlet_tri = tri2d[~tri_solid] + nz * nxy
     cand_in = np.arange(0, per_layer)
     cand_out = np.arange((nz - 1) * per_layer, nz * per_layer)
     gE_in = _match_faces(inlet_tri, ien, cand_in, nNo)
     gE_out = _match_faces(outlet_tri, ien, cand_out, nNo)
 
-    # wall quads between consecutive wall-loop nodes, cut through their smallest node
-    L = wall_loop
+    wall_tri, gE_w = _loop_face(wall_loop, nz, nxy, ien, nNo, ~elem_solid)
+
+    def face(name, tri, gE):
+        return Face(name, tri.astype(np.int32), gE, np.unique(tri).astype(np.int32))
+
+    faces = {"inlet": face("inlet", inlet_tri, gE_in), "outlet": face("outlet", outlet_tri, gE_out),
+             "wall": face("wall", wall_tri, gE_w)}
+    eid = None
+    if nrs > 0:
+        sin_tri = tri2d[tri_solid]
+        sout_tri = tri2d[tri_solid] + nz * nxy
+        faces["wall_inlet"] = face("wall_inlet", sin_tri, _match_faces(sin_tri, ien, cand_in, nNo))
+        faces["wall_outlet"] = face("wall_outlet", sout_tri, _match_faces(sout_tri, ien, cand_out, nNo))
+        otri, gE_o = _loop_face(outer_loop, nz, nxy, ien, nNo, elem_solid)
+        faces["wall_outer"] = face("wall_outer", otri, gE_o)
+        eid = np.where(elem_solid, 2, 1).astype(np.int32)
+        params.update(nrs=nrs, thickness=thickness)
+    gi = faces["inlet"].gN
+    rr = np.hypot(x[gi, 0], x[gi, 1])
+    rw = radius * rwall_ratio[gi]
+    prof = np.clip(1.0 - (rr / rw) ** 2, 0.0, None)
+    return PipeMesh(x=x, ien=ien, faces=faces, radius=radius, length=length,
+                    inlet_profile=prof, params=params, eid=eid)
+
+
+def _loop_face(L: np.ndarray, nz: int, nxy: int, ien: np.ndarray, nNo: int, elem_ok: np.ndarray):
+    """Triangles of the cylindrical surface through the node loop ``L`` (quads between
+    consecutive loop nodes of neighbouring layers, cut through their smallest node) and
+    their owner tets among the elements flagged in ``elem_ok``."""
     nl = L.size
     wtris = []
     for k in range(nz):
@@ -238,25 +285,14 @@ def make_pipe(nc: int, nr: int, nz: int, radius: float = 0.5, length: float = 5.
         t2 = np.where(d02[:, None], np.stack([a, b1, a1], 1), np.stack([b, b1, a1], 1))
         wtris.append(t1)
         wtris.append(t2)
-    wall_tri = np.concatenate(wtris, axis=0)
-    # candidate tets: those with at least 3 wall nodes
-    is_wall = np.zeros(nNo, dtype=bool)
+    tri = np.concatenate(wtris, axis=0)
+    assert tri.shape[0] == 2 * nl * nz
+    # candidate tets: those with at least 3 loop nodes
+    on = np.zeros(nNo, dtype=bool)
     for k in range(nz + 1):
-        is_wall[L + k * nxy] = True
-    cand_w = np.nonzero(is_wall[ien].sum(axis=1) >= 3)[0]
-    gE_w = _match_faces(wall_tri, ien, cand_w, nNo)
-
-    faces = {
-        "inlet": Face("inlet", inlet_tri.astype(np.int32), gE_in, np.unique(inlet_tri).astype(np.int32)),
-        "outlet": Face("outlet", outlet_tri.astype(np.int32), gE_out, np.unique(outlet_tri).astype(np.int32)),
-        "wall": Face("wall", wall_tri.astype(np.int32), gE_w, np.unique(wall_tri).astype(np.int32)),
-    }
-    gi = faces["inlet"].gN
-    rr = np.hypot(x[gi, 0], x[gi, 1])
-    rw = radius * rwall_ratio[gi]
-    prof = np.clip(1.0 - (rr / rw) ** 2, 0.0, None)
-    return PipeMesh(x=x, ien=ien, faces=faces, radius=radius, length=length,
-                    inlet_profile=prof, params=params)
+        on[L + k * nxy] = True
+    cand = np.nonzero((on[ien].sum(axis=1) >= 3) & elem_ok)[0]
+    return tri, _match_faces(tri, ien, cand, nNo)
 
 
 # Named sizes.  'pipe50k' is the CPU-runnable case (~50k tets); 'pipe8m' the 8M-tet pipe
@@ -268,6 +304,11 @@ SIZES = {
     "pipe1m": dict(nc=20, nr=12, nz=120, perturb_modes=8),
     "pipe4m": dict(nc=32, nr=20, nz=180, perturb_modes=8),
     "pipe8m": dict(nc=40, nr=25, nz=240, perturb_modes=8),
+    # FSI pipes: lumen plus a 1 mm solid wall annulus (radius 0.5 -> 0.6)
+    "fsi_tiny": dict(nc=2, nr=1, nz=3, nrs=1),
+    "fsi_small": dict(nc=4, nr=2, nz=6, nrs=2),
+    # 4.15M fluid + 0.97M solid tets: the 4M + 1M-tet FSI pipe
+    "fsi5m": dict(nc=32, nr=20, nz=180, nrs=7, perturb_modes=8),
 }
 
 

@@ -155,6 +155,56 @@ def run_fsi(name):
         shutil.rmtree(tmp)
 
 
+# Coupled ALE FSI time steps on the FSI pipe (lumen + 1 mm neo-Hookean/ST91 wall
+# annulus, E=1e6, nu=0.45, rho=1.2) with linear-elastic mesh motion (E=1, nu=0.3, no
+# mass): FSI equation by GMRES(50) + diagonal preconditioner, mesh equation by CG; three
+# Newton iterations per equation per step (tolerance below reach), pulsatile inflow
+# 15 + 5 sin(2 pi t) cm/s.
+FSI_RUN = dict(FSI)
+FSI_RUN.update(mode="fsi_run", mesh_E=1.0, mesh_nu=0.3, mesh_rho=0.0,
+               ls_rel_tol=1e-10, ls_abs_tol=1e-17, ls_max_itr=100, ls_krylov_dim=50,
+               mesh_ls_rel_tol=1e-10, mesh_ls_abs_tol=1e-17, mesh_ls_max_itr=2000,
+               newton_min=3, newton_max=3, newton_tol=1e-11,
+               mesh_newton_min=3, mesh_newton_max=3, mesh_newton_tol=1e-11,
+               u_mean=15.0, u_amp=5.0, u_freq=1.0, n_steps=3, dump_step=2, dump_iter=3)
+
+
+def run_fsi_steps(name, mesh_name):
+    mesh = named_pipe(mesh_name)
+    nNo, tDof = mesh.nNo, 7
+    params = dict(FSI_RUN)
+    tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        cdir, odir = os.path.join(tmp, "case"), os.path.join(tmp, "out")
+        write_case(mesh, cdir, params)
+        mesh.eid.tofile(os.path.join(cdir, "eid.bin"))
+        os.makedirs(odir)
+        subprocess.run([HARNESS, cdir, odir], check=True)
+        rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
+        with open(os.path.join(odir, "log.txt")) as fh:
+            log = fh.read()
+        rows = []
+        for line in log.splitlines():
+            t = line.split()
+            if t and t[0] == "step":  # step S eq E iter I iNorm X fNorm Y itr N suc K
+                rows.append([int(t[1]), int(t[3]), int(t[5]), float(t[7]), float(t[9]), int(t[11]), int(t[13])])
+        out = {"params": np.array(repr(params)), "log": np.array(log), "newton_log": np.array(rows, dtype=np.float64),
+               "rowPtr": rd("rowPtr.bin", np.int32), "colPtr": rd("colPtr.bin", np.int32)}
+        # the mesh equation's system at the dump point (dof 3)
+        out["R_asm"] = rd("R_asm.bin", np.float64).reshape(nNo, -1)
+        out["Val_asm"] = rd("Val_asm.bin", np.float64).reshape(out["colPtr"].size, -1)
+        for k in ("Ag", "Yg", "Dg", "Do"):
+            out[k] = rd(f"{k}.bin", np.float64).reshape(nNo, tDof)
+        for s in range(1, params["n_steps"] + 1):
+            for k in ("An", "Yn", "Dn"):
+                out[f"{k}_{s}"] = rd(f"{k}_{s}.bin", np.float64).reshape(nNo, tDof)
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+        print(name, "nNo", nNo, "nEl", mesh.nEl, "solid", int((mesh.eid == 2).sum()))
+        print(log)
+    finally:
+        shutil.rmtree(tmp)
+
+
 def write_case(mesh, d, params):
     os.makedirs(d, exist_ok=True)
     mesh.x.astype(np.float64).tofile(os.path.join(d, "x.bin"))
@@ -219,9 +269,11 @@ if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
     for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small", "mesh_cg_small", "mesh_cg7_small",
-                                             "fsi_small"]):
+                                             "fsi_small", "fsi_run_small"]):
         if n == "fsi_small":
             run_fsi(n)
+        elif n == "fsi_run_small":
+            run_fsi_steps(n, "fsi_small")
         elif n == "struct_small":
             run_assembly(n, "struct")
         elif n == "mesh_small":

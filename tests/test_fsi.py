@@ -44,3 +44,104 @@ def test_gpu_fsi_assembly_matches_reference(golden):
     er, ev = rel(R, g["R_asm"]), rel(V, g["Val_asm"])
     print("FSI assembly rel err: R", er, "Val", ev)
     assert er <= 1e-12 and ev <= 1e-12
+
+
+# ---- coupled FSI time steps (iterate_solution with the FSI and mesh equations) -------
+# Golden: tests/golden/ref_fsi_run_small.npz, made by make_golden.py from the compiled
+# reference (main.cpp's loop with construct_fsi, construct_mesh, b_assem_neu_bc on the
+# moving mesh, fsils_solve GMRES/CG and picp/pici/picc) on the FSI pipe 'fsi_small'
+# (lumen + 2-ring wall annulus, 2880 tets of which 1152 solid), three time steps of
+# three Newton iterations per equation.
+
+def _run_params(g):
+    return eval(str(g["params"]))
+
+
+def test_fsi_run_golden_is_consistent(golden):
+    """The reference's run: the equations alternate FSI, mesh, FSI, ... within a step,
+    every solve converged, and after a step the solid nodes' mesh rows equal their
+    displacement rows (picc, pic.cpp:181-201)."""
+    from svfsiplus_gb300.mesh import named_pipe
+    g = golden("fsi_run_small")
+    log = g["newton_log"]
+    assert log.shape[0] == 3 * 6
+    assert list(log[:6, 1]) == [0, 1, 0, 1, 0, 1]
+    assert np.all(log[:, 6] == 1)
+    m = named_pipe("fsi_small")
+    solid = np.zeros(m.nNo, bool)
+    solid[m.ien[m.eid == 2].ravel()] = True
+    for s in (1, 2, 3):
+        D = g[f"Dn_{s}"]
+        assert np.array_equal(D[solid, 4:7], D[solid, 0:3])
+        assert np.abs(D[solid, 0:3]).max() > 0
+    assert m.nNo == g["Yn_1"].shape[0] and g["colPtr"].size == g["Val_asm"].shape[0]
+
+
+@pytest.mark.gpu
+def test_gpu_fsi_ale_system_matches_reference(golden):
+    """The FSI system of step 2, Newton iteration 3 (the reference dumped it after
+    construct_fsi and the outlet's b_assem_neu_bc on the moving mesh): construct_fsi
+    + svgpu_neu_bc_fluid_ale from the same Ag/Yg/Dg/Do.  Tolerance 1e-12 relative."""
+    from svfsiplus_gb300 import api
+    g = golden("fsi_run_small")
+    ps = _run_params(g)
+    m = named_pipe("fsi_small")
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(m.nNo, g["rowPtr"], g["colPtr"], 0)
+    ctx.mesh_create(m.x, m.ien)
+    ctx.mesh_domains(m.eid)
+    out = m.faces["outlet"]
+    ctx.face_create(api.FACE_OUTLET, out.ien, out.gE)
+    p = api.fsi_props(ps["rho_f"], ps["mu"], ps["backflow_beta"], ps["rho_s"], ps["E"], ps["nu"], ps["dt"],
+                      ps["rho_inf"], ps["mesh_E"], ps["mesh_nu"], ps["mesh_rho"])
+    R = np.zeros((m.nNo, 4))
+    V = np.zeros((g["colPtr"].size, 16))
+    ctx.construct_fsi(p.fluid, p.solid, 7, g["Ag"], g["Yg"], g["Dg"], R, V)
+    ctx.b_assem_neu_bc_ale(api.FACE_OUTLET, p.fluid, 0.0, 7, g["Yg"], g["Do"], R, V)
+    er, ev = rel(R, g["R_asm"]), rel(V, g["Val_asm"])
+    print("FSI ALE system rel err: R", er, "Val", ev)
+    assert er <= 1e-12 and ev <= 1e-12
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fsi_steps_match_reference(golden):
+    """Three coupled time steps through svgpu_fsi_step (C ABI) against the reference's
+    fields after every step.  Per-field relative L2 tolerance 1e-8 (both sides solve
+    each linear system to relative 1e-10): fluid velocity, pressure, solid displacement
+    and mesh displacement.  Every Newton iteration's preconditioned initial residual
+    norm within 1e-6 relative, the equation order identical."""
+    from svfsiplus_gb300 import api
+    g = golden("fsi_run_small")
+    ps = _run_params(g)
+    m = named_pipe("fsi_small")
+    p = api.fsi_props(ps["rho_f"], ps["mu"], ps["backflow_beta"], ps["rho_s"], ps["E"], ps["nu"], ps["dt"],
+                      ps["rho_inf"], ps["mesh_E"], ps["mesh_nu"], ps["mesh_rho"])
+    s = api.PipeFsiSolver(m, p, newton=(ps["newton_min"], ps["newton_max"], ps["newton_tol"]),
+                          mesh_newton=(ps["mesh_newton_min"], ps["mesh_newton_max"], ps["mesh_newton_tol"]),
+                          gmres=(ps["ls_rel_tol"], ps["ls_abs_tol"], ps["ls_max_itr"], ps["ls_krylov_dim"]),
+                          cg=(ps["mesh_ls_rel_tol"], ps["mesh_ls_abs_tol"], ps["mesh_ls_max_itr"]))
+    assert np.array_equal(s.rowPtr, g["rowPtr"]) and np.array_equal(s.colPtr, g["colPtr"])
+    solid = np.zeros(m.nNo, bool)
+    solid[s.solid_nodes] = True
+    fluid = ~solid
+    log = g["newton_log"]
+    k = 0
+    for step in (1, 2, 3):
+        st = s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"])
+        assert [q for q, _ in st] == [int(v) for v in log[k:k + len(st), 1]]
+        for q, d in st:
+            ref = log[k]
+            assert abs(d["iNorm"] - ref[3]) <= 1e-6 * ref[3], (step, q, d["iNorm"], ref[3])
+            assert d["suc"] == 1
+            k += 1
+        Yr, Dr = g[f"Yn_{step}"], g[f"Dn_{step}"]
+        errs = {"velocity": rel(s.Yn[fluid, 0:3], Yr[fluid, 0:3]),
+                "pressure": rel(s.Yn[:, 3], Yr[:, 3]),
+                "solid displacement": rel(s.Dn[solid, 0:3], Dr[solid, 0:3]),
+                "mesh displacement": rel(s.Dn[:, 4:7], Dr[:, 4:7]),
+                "acceleration": rel(s.An[:, 0:4], g[f"An_{step}"][:, 0:4])}
+        print("step", step, {k2: f"{v:.2e}" for k2, v in errs.items()})
+        assert max(errs.values()) <= 1e-8, errs
+        assert np.array_equal(s.Dn[solid, 4:7], s.Dn[solid, 0:3])
+    s.ctx.close()
