@@ -477,6 +477,59 @@ def run_study(args):
         s.ctx.close()
 
 
+def run_fsi(args):
+    """The coupled ALE FSI pipe (lumen + 1 mm neo-Hookean wall, linear-elastic mesh
+    motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s): s per time step through the C ABI
+    (svgpu_fsi_step, host state copied in and out every step) for the multilevel
+    mixed-precision FSI solve and for the plain FP64 GMRES + diagonal solve, both from
+    rest over the same steps, and the per-field relative L2 difference of the two."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+
+    name = args.workload if args.workload != WORKLOAD else "fsi5m"
+    mesh = named_pipe(name)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    out = {"workload": name, "tets": mesh.nEl, "solid_tets": int((mesh.eid == 2).sum()), "nodes": mesh.nNo,
+           "blocks": int(colPtr.size)}
+    fields = {}
+    for path in ("multilevel", "plain"):
+        mixed = path == "multilevel"
+        s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=(1, NEWTON_MAX, NEWTON_TOL),
+                              mesh_newton=(1, NEWTON_MAX, NEWTON_TOL),
+                              gmres=(LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM), cg=(1e-6, 1e-17, 5000),
+                              rowPtr=rowPtr, colPtr=colPtr, precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64)
+        if mixed:
+            s.ctx.set_solver_mode(2)
+        steps = []
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            st = s.step(15.0, 5.0, 1.0)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            rec = {"s": round(dt, 4), "fsi_its": [d["itr"] for q, d in st if q == 0],
+                   "mesh_its": [d["itr"] for q, d in st if q == 1],
+                   "fsi_final_over_first": [d["iNorm"] for q, d in st if q == 0][-1] /
+                                           [d["iNorm"] for q, d in st if q == 0][0],
+                   "timed": k >= args.warmup}
+            steps.append(rec)
+        timed = [r["s"] for r in steps if r["timed"]]
+        out[path] = {"s_per_step": float(np.mean(timed)), "steps": steps}
+        fields[path] = (s.Yn.copy(), s.Dn.copy())
+        solid = np.zeros(mesh.nNo, bool)
+        solid[s.solid_nodes] = True
+        s.ctx.close()
+        torch.cuda.empty_cache()
+    (Ym, Dm), (Yp, Dp) = fields["multilevel"], fields["plain"]
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+    out["mixed_vs_fp64_rel_l2"] = {"velocity": rel(Ym[~solid, :3], Yp[~solid, :3]), "pressure": rel(Ym[:, 3], Yp[:, 3]),
+                                   "solid_displacement": rel(Dm[solid, :3], Dp[solid, :3]),
+                                   "mesh_displacement": rel(Dm[:, 4:7], Dp[:, 4:7])}
+    out["speedup_plain_over_multilevel"] = out["plain"]["s_per_step"] / out["multilevel"]["s_per_step"]
+    print(json.dumps({"fsi": out}), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -533,6 +586,7 @@ def main():
     ap.add_argument("--ml-options", default=None,
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
+    ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -542,6 +596,8 @@ def main():
         run_assembly_only(args)
     elif args.study:
         run_study(args)
+    elif args.fsi:
+        run_fsi(args)
     else:
         run_ours(args)
 

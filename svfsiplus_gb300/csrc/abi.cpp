@@ -648,6 +648,10 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   rc = gmres_mixed(ctx, Val32, R, R, st);
   if (rc) return rc;
   phase_mark(ctx, PH_OTHER);
+  if (ctx->zero_null_rows && ctx->learned_mode != 0) {
+    launch_zero_null_rows(ctx->stream, ctx->nNo, ctx->rowPtr.p, Val32, R);
+    ctx->launches++;
+  }
   if (collect && st->iNorm > ctx->absTol) {
     // exact pair (K X, X) of the preconditioned system: K X = Rs - r, with r the final
     // FP64 residual the solve left in kw.r64 (valid whether or not it converged)

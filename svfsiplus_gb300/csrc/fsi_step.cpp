@@ -148,6 +148,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
   ctx->mItr = ls_fsi.mItr;
   ctx->sD = ls_fsi.sD;
   ctx->resident_mixed = false;
+  ctx->zero_null_rows = mixed;  // the pressure rows of solid-only nodes are empty
 
   svgpu_solid_props sp = props->solid;
   int itr[2] = {0, 0};
@@ -226,6 +227,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
   ctx->absTol = saved.absTol;
   ctx->mItr = saved.mItr;
   ctx->sD = saved.sD;
+  ctx->zero_null_rows = false;
   if (rc) return rc;
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, w.An.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, w.Yn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));

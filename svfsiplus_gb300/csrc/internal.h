@@ -253,6 +253,9 @@ struct svgpu_ctx {
   // 3: as 2 with the learned network as the finest-level pre-smoother (+ initial guess)
   int learned_mode = 0;
   long long learned_rejects = 0;
+  // mixed solves of systems with empty rows (the FSI equation): zero the increment's
+  // entries of empty rows after flexible cycles (zero_null_rows_kernel)
+  bool zero_null_rows = false;
   // host staging
   svgpu::DevBuf<double> stage1, stage2;
 };
@@ -386,6 +389,7 @@ void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, cons
 void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, const double* g, const int* flags,
                       double* X);
 void launch_sub(cudaStream_t s, long n, const double* R, const double* y, double* r);
+void launch_zero_null_rows(cudaStream_t s, int nNo, const int* rowPtr, const float* Val, double* X);
 void launch_start_vector32(cudaStream_t s, long n, const double* r, const double* nrm2, float* u0, double* err0,
                            int* flags);
 

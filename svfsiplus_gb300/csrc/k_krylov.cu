@@ -722,6 +722,27 @@ __global__ void sub_kernel(long n, const double* __restrict__ R, const double* _
     r[i] = R[i] - y[i];
 }
 
+// X(r, i) = 0 for every row r of node i whose entries in the FP32 block row are all
+// zero.  Such a dof (the pressure of a node held only by solid elements of the FSI
+// equation: struct_3d leaves the fourth row and column of its blocks empty) has a zero
+// row and column and a zero right-hand side, so the reference's GMRES never moves it;
+// a flexible preconditioner's directions can, and nothing in K X would show it.
+__global__ void zero_null_rows_kernel(int nNo, const int* __restrict__ rowPtr, const float* __restrict__ Val,
+                                      double* __restrict__ X) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nNo) return;
+  bool nz[4] = {false, false, false, false};
+  for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++) {
+    const float4* b = reinterpret_cast<const float4*>(Val + 16L * k);
+    for (int r = 0; r < 4; r++) {
+      const float4 v = b[r];
+      nz[r] = nz[r] || v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f;
+    }
+  }
+  for (int r = 0; r < 4; r++)
+    if (!nz[r]) X[4L * i + r] = 0.0;
+}
+
 __global__ void start_vector32_kernel(long n, const double* __restrict__ r, const double* __restrict__ nrm2,
                                       float* __restrict__ u0, double* __restrict__ err0, int* flags) {
   const double nrm = sqrt(*nrm2);
@@ -782,6 +803,10 @@ void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, cons
 void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, const double* g, const int* flags,
                       double* X) {
   xupdate32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, sD, V, ldv, g, flags, X);
+}
+
+void launch_zero_null_rows(cudaStream_t s, int nNo, const int* rowPtr, const float* Val, double* X) {
+  zero_null_rows_kernel<<<(nNo + 255) / 256, 256, 0, s>>>(nNo, rowPtr, Val, X);
 }
 
 void launch_sub(cudaStream_t s, long n, const double* R, const double* y, double* r) {

@@ -307,8 +307,8 @@ SIZES = {
     # FSI pipes: lumen plus a 1 mm solid wall annulus (radius 0.5 -> 0.6)
     "fsi_tiny": dict(nc=2, nr=1, nz=3, nrs=1),
     "fsi_small": dict(nc=4, nr=2, nz=6, nrs=2),
-    # 4.15M fluid + 0.97M solid tets: the 4M + 1M-tet FSI pipe
-    "fsi5m": dict(nc=32, nr=20, nz=180, nrs=7, perturb_modes=8),
+    # 4.0M fluid + 1.0M solid tets: the 4M + 1M-tet FSI pipe
+    "fsi5m": dict(nc=32, nr=20, nz=186, nrs=7, perturb_modes=8),
 }
 
 
