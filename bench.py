@@ -291,12 +291,13 @@ def run_assembly_only(args):
     print(json.dumps(out), flush=True)
 
 
-def make_solver(api, mesh, rowPtr, colPtr, path, device=0):
+def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newton_max=None, lin_rel_tol=None):
     mode = PATH_MODES[path]
     precision = api.SVGPU_FP64 if mode < 0 else api.SVGPU_MIXED
-    s = api.PipeFluidSolver(mesh, device=device, sD=KRYLOV_DIM, mItr=MAX_RESTARTS, relTol=LIN_REL_TOL, absTol=1e-17,
-                            newton_min=1, newton_max=NEWTON_MAX, newton_tol=NEWTON_TOL, precision=precision,
-                            rowPtr=rowPtr, colPtr=colPtr)
+    s = api.PipeFluidSolver(mesh, device=device, sD=KRYLOV_DIM, mItr=MAX_RESTARTS,
+                            relTol=LIN_REL_TOL if lin_rel_tol is None else lin_rel_tol, absTol=1e-17,
+                            newton_min=1, newton_max=newton_max or NEWTON_MAX,
+                            newton_tol=newton_tol or NEWTON_TOL, precision=precision, rowPtr=rowPtr, colPtr=colPtr)
     if mode in (3, 4):
         s.enable_learning()
     if mode >= 0:
@@ -477,6 +478,51 @@ def run_study(args):
         s.ctx.close()
 
 
+def run_sweep(args):
+    """The mixed multilevel path (the headline's settings) on pipes of several sizes:
+    s per time step and, at every step, the per-field relative L2 difference from the
+    FP64 solution of the same steps.  The FP64 solution is the Newton iteration on the
+    FP64 residual driven to a tight tolerance (relative 1e-10, linear relative 1e-4): the
+    FP32 tangent and Krylov basis change only the path of that iteration, not its fixed
+    point, which the FP64 residual alone defines."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+
+    sizes = args.sweep.split(",")
+    for name in sizes:
+        mesh = named_pipe(name)
+        rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+        runs = {}
+        for kind in ("headline", "fp64_tight"):
+            tight = kind == "fp64_tight"
+            s, _ = make_solver(api, mesh, rowPtr, colPtr, "multilevel", newton_tol=1e-10 if tight else None,
+                               newton_max=14 if tight else None, lin_rel_tol=1e-4 if tight else None)
+            s.ctx.set_solver_mode(2)
+            recs = []
+            for k in range(args.steps):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                st = s.step(U_MEAN, U_AMP, U_FREQ)
+                torch.cuda.synchronize()
+                recs.append({"s": time.perf_counter() - t, "newton": len(st), "krylov": sum(q["itr"] for q in st),
+                             "final_over_first": st[-1]["iNorm"] / st[0]["iNorm"], "Y": s.Yn.copy()})
+            runs[kind] = recs
+            s.ctx.close()
+            torch.cuda.empty_cache()
+        rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+        steps = []
+        for a, b in zip(runs["headline"], runs["fp64_tight"]):
+            steps.append({"s": round(a["s"], 4), "newton": a["newton"], "krylov": a["krylov"],
+                          "final_over_first": a["final_over_first"],
+                          "velocity_rel_l2": rel(a["Y"][:, :3], b["Y"][:, :3]),
+                          "pressure_rel_l2": rel(a["Y"][:, 3], b["Y"][:, 3]),
+                          "fp64_newton": b["newton"], "fp64_final_over_first": b["final_over_first"]})
+        print(json.dumps({"sweep": name, "tets": mesh.nEl, "nodes": mesh.nNo, "blocks": int(colPtr.size),
+                          "s_per_step_after_first": float(np.mean([q["s"] for q in steps[1:]] or [steps[0]["s"]])),
+                          "steps": steps}), flush=True)
+
+
 def run_fsi(args):
     """The coupled ALE FSI pipe (lumen + 1 mm neo-Hookean wall, linear-elastic mesh
     motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s): s per time step through the C ABI
@@ -587,7 +633,12 @@ def main():
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
+    ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
+    ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     args = ap.parse_args()
+    if args.lin_rel_tol is not None:
+        global LIN_REL_TOL
+        LIN_REL_TOL = args.lin_rel_tol
     if args.impl == "reference":
         run_reference(args)
     elif args.spmv_only:
@@ -598,6 +649,8 @@ def main():
         run_study(args)
     elif args.fsi:
         run_fsi(args)
+    elif args.sweep:
+        run_sweep(args)
     else:
         run_ours(args)
 
