@@ -93,8 +93,9 @@ int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, in
 /* ---- solve --------------------------------------------------------------------- */
 /* Replaces fsils_solve (liner_solver/solve.cpp:50).  Ri (dof,nNo): in the residual,
  * out the increment.  Val (dof*dof,nnz) is scaled in place by the preconditioner, as
- * in the reference.  incL (nFaces): 0 switches a face off; res (nFaces): coupled
- * resistances (must be 0: coupled Neumann faces are not supported yet).
+ * in the reference.  incL (nFaces): 0 switches a face off; res (nFaces): resistances
+ * of coupled Neumann faces (a non-zero res on an included Neumann face adds the
+ * rank-one term of add_bc_mul.cpp:53 to every GMRES product; GMRES only).
  * Ri == NULL and Val == NULL solve the system resident in the context (the one the
  * svgpu_construct_* calls assembled) and leave the increment there. */
 int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec,
@@ -198,6 +199,48 @@ int svgpu_neu_bc_fluid(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* prop
  * (b_fluid, fluid.cpp:79-84).  R (4, nNo) and Val (16, nnz) are added to. */
 int svgpu_neu_bc_fluid_ale(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, double h, int tDof,
                            const double* Yg, const double* Do, double* R, double* Val);
+
+/* ---- coupled RCR outlet (the reference's pipe_RCR_3d outlet BC) ---------------------
+ * A three-element Windkessel on a Neumann face, coupled semi-implicitly as the
+ * reference does it (baf_ini.cpp:119-177, set_bc.cpp:50-790):
+ *   svgpu_rcr_create creates linear-solver face lsFace (fsils_bc_create with
+ *   BC_TYPE_Neu and the nodal normal integrals of mesh face meshFace, fsi_ls_ini
+ *   baf_ini.cpp:738-775), sets the 0D state to Xo (rcr_init without initRCR) and the
+ *   resistance dP/dQ by calc_der_cpl_bc's finite difference at flow rate Q0.
+ *   svgpu_fluid_step with opts.outletFace == meshFace then, every Newton iteration,
+ *   computes the face's flow rates of Yo and Yn, integrates the 0D model (RCR_Integ_X,
+ *   set_bc.cpp:460-547), applies the pressure as the face's Neumann value and solves
+ *   with res = gam dt dP/dQ on lsFace, which adds the rank-one term of add_bc_mul
+ *   (add_bc_mul.cpp:53) to every GMRES product.  Coupled faces need GMRES (FP64 or
+ *   the mixed path); CG and the NS solver reject them. */
+int svgpu_rcr_create(svgpu_ctx* ctx, int meshFace, int lsFace, double Rp, double C, double Rd, double Pd,
+                     double Xo, double dt, double Q0);
+/* out6 = {xo, xn, P, Qo, Qn, dP/dQ}: the 0D state at t and t + dt, the imposed
+ * pressure, the flow rates at t and t + dt of the last Newton iteration, the
+ * resistance.  svgpu_rcr_set_state sets xo (a restart). */
+int svgpu_rcr_state(svgpu_ctx* ctx, double* out6);
+int svgpu_rcr_set_state(svgpu_ctx* ctx, double xo);
+/* Host-only: RCR_Integ_X (set_bc.cpp:460-547) for one face over one time step dt from
+ * the state xo with flow rates Qo (t) and Qn (t + dt): the state xn and the pressure
+ * P = xn + Rp Qn; and calc_der_cpl_bc's finite-difference resistance dP/dQ at Qn. */
+int svgpu_rcr_integrate(double Rp, double C, double Rd, double Pd, double dt, double xo, double Qo, double Qn,
+                        double* xn, double* P);
+double svgpu_rcr_resistance(double Rp, double C, double Rd, double Pd, double dt, double xo, double Qo, double Qn);
+
+/* ---- restart files (output::write_restart, output.cpp:202-372; init_from_bin,
+ * initialize.cpp:78-245) -------------------------------------------------------------
+ * Host-only; ctx may be NULL (it only receives the error text).  stamp[7] = {processes
+ * (1), equations, meshes, nodes, 0D unknowns (cplBC.nX when coupled, else 0), tDof,
+ * dFlag}, the reference's com_mod.stamp (initialize.cpp:497).  The layout is the
+ * reference's for one process: stamp, cTS, time, cpu seconds, eq.iNorm per equation,
+ * the 0D state, Yn, An and, with dFlag, Dn twice (as the reference writes it for the
+ * fluid/FSI/mesh equations).  Reading checks the stamp first and fails with the
+ * reference's message ("The number of nodes ... don't match."). */
+int svgpu_write_restart(svgpu_ctx* ctx, const char* path, const int* stamp, int cTS, double time, double cpu_time,
+                        const double* iNorm, const double* xn, const double* Yn, const double* An,
+                        const double* Dn);
+int svgpu_read_restart(svgpu_ctx* ctx, const char* path, const int* stamp, int* cTS, double* time, double* cpu_time,
+                       double* iNorm, double* xo, double* Yo, double* Ao, double* Do);
 
 /* ---- learned preconditioner (no counterpart in the reference) ------------------------
  * A 3-layer message-passing network on the CSR graph (hidden width 64, BF16 weights,

@@ -14,7 +14,7 @@ FLAGS="-std=c++17 -O3 -w -include cstring -include stdexcept -include limits"
 SOLVER="fluid nn fs lhsa all_fun utils ComMod CmMod Array Vector Array3 Tensor4 consts FsilsLinearAlgebra
 LinearAlgebra eq_assem pic set_bc sv_struct mesh l_elas fsi mat_models mat_fun mat_fun_carray Simulation
 Parameters ls bf cep cep_ion CepMod CepModAp CepModBo CepModFn CepModTtp ChnlMod cmm heatf heats shells
-stokes ustruct fft nn_elem_props"
+stokes ustruct fft nn_elem_props baf_ini output"
 objs=()
 pids=()
 compile() { g++ $FLAGS $INC -c "$1" -o "$2"; }

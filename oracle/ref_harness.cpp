@@ -33,6 +33,9 @@
 #include "lhs.h"
 #include "mat_fun.h"
 #include "all_fun.h"
+#include "baf_ini.h"
+#include "set_bc.h"
+#include "output.h"
 
 #include <cmath>
 #include <cstdio>
@@ -42,6 +45,18 @@
 #include <string>
 #include <vector>
 #include <chrono>
+
+// The reference's own restart file (output::write_restart, output.cpp:202-360) of the
+// final state, with the stamp and record length initialize.cpp:488-519 sets up.
+static void dump_restart(Simulation& sim, const std::string& out) {
+  auto& com = sim.com_mod;
+  com.stFileName = out + "/stFile";
+  com.stFileRepl = true;
+  const int nX = com.cplBC.coupled ? com.cplBC.nX : 0;
+  com.stamp = {1, com.nEq, com.nMsh, com.tnNo, nX, com.tDof, com.dFlag ? 1 : 0};
+  std::array<double, 3> timeP = {0.0, 0.0, 0.0};
+  output::write_restart(&sim, timeP);
+}
 
 static std::map<std::string, std::string> read_params(const std::string& dir) {
   std::map<std::string, std::string> p;
@@ -621,6 +636,7 @@ static int run_fsi(const std::string& dir, const std::string& out, std::map<std:
     com.Yo = com.Yn;
     com.Do = com.Dn;
   }
+  dump_restart(sim, out);
   return 0;
 }
 
@@ -636,6 +652,7 @@ int main(int argc, char** argv) {
   if (P.count("mode") && P.at("mode").rfind("assemble_", 0) == 0) return assemble_only(dir, out, P);
   auto getd = [&](const char* k) { return std::stod(P.at(k)); };
   auto geti = [&](const char* k) { return std::stoi(P.at(k)); };
+  double log_rcr_r = 0.0;
 
   Simulation sim;
   auto& com = sim.com_mod;
@@ -730,7 +747,12 @@ int main(int argc, char** argv) {
   fsi_linear_solver::fsils_commu_create(commu, MPI_COMM_WORLD);
   Vector<int> gNodes(nNo);
   for (int a = 0; a < nNo; a++) gNodes(a) = a;
-  const int nFacesLS = 2;
+  // rcr=1: the outlet is a coupled RCR (Windkessel) Neumann BC, the reference's
+  // pipe_RCR_3d set-up (read_files.cpp:280-306, baf_ini.cpp:119-177): semi-implicit
+  // coupling, a resistance face of the linear solver (fsi_ls_ini) and the
+  // finite-difference resistance of calc_der_cpl_bc.
+  const bool rcr = P.count("rcr") && geti("rcr") == 1;
+  const int nFacesLS = rcr ? 3 : 2;
   fsi_linear_solver::fsils_lhs_create(com.lhs, commu, nNo, nNo, nnz, gNodes, com.rowPtr, com.colPtr, nFacesLS);
   for (int f = 0; f < 2; f++) {
     auto& fa = msh.fa[f];
@@ -738,6 +760,50 @@ int main(int argc, char** argv) {
     Vector<int> gN(fa.nNo);
     for (int a = 0; a < fa.nNo; a++) gN(a) = fa.gN(a);
     fsi_linear_solver::fsils_bc_create(com.lhs, f, fa.nNo, 3, fsi_linear_solver::BcType::BC_TYPE_Dir, gN, sVl);
+  }
+  if (rcr) {
+    eq.nBc = 1;
+    eq.bc.resize(1);
+    auto& bc = eq.bc[0];
+    bc.iFa = 2;
+    bc.iM = 0;
+    bc.bType = utils::ibset(bc.bType, consts::iBC_Neu);
+    bc.bType = utils::ibset(bc.bType, consts::iBC_RCR);
+    bc.RCR.Rp = getd("rcr_Rp");
+    bc.RCR.C = getd("rcr_C");
+    bc.RCR.Rd = getd("rcr_Rd");
+    bc.RCR.Pd = getd("rcr_Pd");
+    bc.RCR.Xo = getd("rcr_Xo");
+    bc.gx.resize(msh.fa[2].nNo);
+    bc.gx = 1.0;
+    bc.cplBCptr = 0;
+    auto& cpl = com.cplBC;
+    cpl.coupled = true;
+    cpl.nFa = 1;
+    cpl.schm = consts::CplBCType::cplBC_SI;
+    cpl.nX = 1;
+    cpl.nXp = 2;
+    cpl.xo.resize(1);
+    cpl.xp.resize(2);
+    cpl.xn.resize(1);
+    cpl.initRCR = false;
+    cpl.fa.resize(1);
+    cpl.fa[0].name = "outlet";
+    cpl.fa[0].y = 0.0;
+    cpl.fa[0].bGrp = consts::CplBCType::cplBC_Neu;
+    bc.bType = utils::ibset(bc.bType, consts::iBC_res);
+    cpl.fa[0].RCR.Rp = bc.RCR.Rp;
+    cpl.fa[0].RCR.C = bc.RCR.C;
+    cpl.fa[0].RCR.Rd = bc.RCR.Rd;
+    cpl.fa[0].RCR.Pd = bc.RCR.Pd;
+    cpl.fa[0].RCR.Xo = bc.RCR.Xo;
+    com.Yo = 0.0;
+    com.Yn = 0.0;
+    set_bc::rcr_init(com, sim.cm_mod);
+    set_bc::calc_der_cpl_bc(com, sim.cm_mod);
+    int lsPtr = 1;
+    baf_ini_ns::fsi_ls_ini(com, sim.cm_mod, bc, msh.fa[2], lsPtr);
+    log_rcr_r = bc.r;
   }
   // ls_type: "gmres" (default) or "ns" (ns_solver.cpp:167, with its GM/CG defaults)
   const bool use_ns = P.count("ls_type") && P.at("ls_type") == "ns";
@@ -759,6 +825,11 @@ int main(int argc, char** argv) {
 
   std::ofstream log(out + "/log.txt");
   log.precision(17);
+  if (rcr) {
+    log << "rcr_r " << log_rcr_r << "\n";
+    const auto& fv = com.lhs.face[2].val;
+    write_raw(out + "/rcr_face_val.bin", fv.data(), (size_t)fv.size());
+  }
   double time = 0.0;
   double t_asm = 0.0, t_solve = 0.0;
   auto wall0 = std::chrono::steady_clock::now();
@@ -787,15 +858,21 @@ int main(int argc, char** argv) {
     }
     int inner = 1;
     while (true) {
+      if (rcr) set_bc::set_bc_cpl(com, sim.cm_mod);  // main.cpp:385-392 (Dirichlet values unchanged)
       pic::pici(&sim, Ag, Yg, Dg);
       ls_ns::ls_alloc(com, eq);
       auto t0 = std::chrono::steady_clock::now();
       eq_assem::global_eq_assem(com, sim.get_cep_mod(), msh, Ag, Yg, Dg);
-      hg = 0.0;
-      eq_assem::b_assem_neu_bc(com, msh.fa[2], hg, Yg);
+      if (rcr) {
+        set_bc::set_bc_neu(com, sim.cm_mod, Yg, Dg);
+      } else {
+        hg = 0.0;
+        eq_assem::b_assem_neu_bc(com, msh.fa[2], hg, Yg);
+      }
       auto t1 = std::chrono::steady_clock::now();
       incL = 1;
       res = 0.0;
+      if (rcr) res(eq.bc[0].lsPtr) = eq.gam * com.dt * eq.bc[0].r;  // main.cpp:566-573
       if (cTS == dump_step && inner == dump_iter) {
         write_raw(out + "/R_asm.bin", com.R.data(), (size_t)com.R.size());
         write_raw(out + "/Val_asm.bin", com.Val.data(), (size_t)com.Val.size());
@@ -812,6 +889,7 @@ int main(int argc, char** argv) {
       log << "step " << cTS << " iter " << inner << " iNorm " << RI.iNorm << " fNorm " << RI.fNorm
           << " itr " << RI.itr << " suc " << RI.suc;
       if (use_ns) log << " gm_itr " << eq.FSILS.GM.itr << " cg_itr " << eq.FSILS.CG.itr << " dB " << RI.dB;
+      if (rcr) log << " P " << eq.bc[0].g << " Qo " << com.cplBC.fa[0].Qo << " Qn " << com.cplBC.fa[0].Qn;
       log << "\n";
       if (cTS == dump_step && inner == dump_iter) {
         write_raw(out + "/dX.bin", com.R.data(), (size_t)com.R.size());
@@ -827,7 +905,9 @@ int main(int argc, char** argv) {
     write_raw(out + "/Yn_" + std::to_string(cTS) + ".bin", com.Yn.data(), (size_t)com.Yn.size());
     com.Ao = com.An;
     com.Yo = com.Yn;
+    if (rcr) com.cplBC.xo = com.cplBC.xn;  // main.cpp:758
   }
+  dump_restart(sim, out);
   double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
   log << "timing steps " << nSteps << " wall_s " << wall << " assembly_s " << t_asm << " solve_s " << t_solve << "\n";
   return 0;

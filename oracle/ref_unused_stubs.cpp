@@ -18,4 +18,5 @@ void fib_strech(Simulation*, const int, const mshType&, const Array<double>&, Ve
 }
 namespace svZeroD {
 void calc_svZeroD(ComMod&, const CmMod&, char) { throw std::runtime_error("oracle harness: 0D coupling not linked"); }
+void init_svZeroD(ComMod&, const CmMod&) { throw std::runtime_error("oracle harness: 0D coupling not linked"); }
 }

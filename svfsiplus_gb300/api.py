@@ -240,6 +240,18 @@ class Context:
         self._check(lib().svgpu_neu_bc_fluid(self._h, int(face_id), C.byref(props), C.c_double(h), _ptr(Yg),
                                              _ptr(R), _ptr(Val)), "b_assem_neu_bc")
 
+    def rcr_create(self, mesh_face, ls_face, Rp, Cap, Rd, Pd=0.0, Xo=0.0, dt=1e-3, Q0=0.0):
+        """A coupled RCR outlet on mesh face `mesh_face` with linear-solver face `ls_face`
+        (the reference's RCR Neumann BC, semi-implicit coupling); Cap is the capacitance."""
+        self._check(lib().svgpu_rcr_create(self._h, int(mesh_face), int(ls_face),
+                                           *(C.c_double(v) for v in (Rp, Cap, Rd, Pd, Xo, dt, Q0))), "rcr_create")
+
+    def rcr_state(self):
+        """{xo, xn, P, Qo, Qn, r} of the RCR outlet after the last Newton iteration."""
+        out = (C.c_double * 6)()
+        self._check(lib().svgpu_rcr_state(self._h, out), "rcr_state")
+        return dict(zip(("xo", "xn", "P", "Qo", "Qn", "r"), list(out)))
+
     def b_assem_neu_bc_ale(self, face_id, props, h, tDof, Yg, Do, R, Val):
         """b_assem_neu_bc on the moving mesh: face at x + Do(4..6), backflow relative to Yg(4..6)."""
         self._check(lib().svgpu_neu_bc_fluid_ale(self._h, int(face_id), C.byref(props), C.c_double(h), int(tDof),
@@ -365,6 +377,71 @@ class Context:
 FACE_INLET, FACE_WALL, FACE_OUTLET = 0, 1, 2
 
 
+def rcr_integrate(Rp, C_, Rd, Pd, dt, xo, Qo, Qn):
+    """RCR_Integ_X (set_bc.cpp:460-547) on the host: (xn, P)."""
+    xn, P = C.c_double(), C.c_double()
+    rc = lib().svgpu_rcr_integrate(*(C.c_double(v) for v in (Rp, C_, Rd, Pd, dt, xo, Qo, Qn)), C.byref(xn), C.byref(P))
+    if rc != SVGPU_OK:
+        raise RuntimeError(f"rcr_integrate failed ({rc})")
+    return xn.value, P.value
+
+
+def rcr_resistance(Rp, C_, Rd, Pd, dt, xo, Qo, Qn):
+    """calc_der_cpl_bc's finite-difference dP/dQ (set_bc.cpp:50-240) on the host."""
+    lib().svgpu_rcr_resistance.restype = C.c_double
+    return float(lib().svgpu_rcr_resistance(*(C.c_double(v) for v in (Rp, C_, Rd, Pd, dt, xo, Qo, Qn))))
+
+
+def restart_stamp(nEq, nNo, tDof, dFlag, nX=0, nMsh=1):
+    """com_mod.stamp of a one-process run (initialize.cpp:497)."""
+    return np.array([1, nEq, nMsh, nNo, nX, tDof, 1 if dFlag else 0], dtype=np.int32)
+
+
+def write_restart(path, stamp, cTS, time, iNorm, Yn, An, Dn=None, xn=None, cpu_time=0.0):
+    """The reference's restart file (output::write_restart) of one process.  Arrays are
+    node-major (nNo, tDof) -- the reference's column-major (tDof, nNo)."""
+    st = np.ascontiguousarray(stamp, dtype=np.int32)
+    iN = np.ascontiguousarray(np.atleast_1d(iNorm), dtype=np.float64)
+    x = None if xn is None else np.ascontiguousarray(np.atleast_1d(xn), dtype=np.float64)
+    arr = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (Yn, An, Dn)]
+    rc = lib().svgpu_write_restart(None, str(path).encode(), _ptr(st), int(cTS), C.c_double(time),
+                                   C.c_double(cpu_time), _ptr(iN), _ptr(x), *(_ptr(a) for a in arr))
+    if rc != SVGPU_OK:
+        raise RuntimeError(f"write_restart failed ({rc}): {path}")
+
+
+def read_restart(path, stamp):
+    """init_from_bin (initialize.cpp:78-245): dict of cTS, time, cpu_time, iNorm, xo, Yo,
+    Ao, Do for the given stamp; RuntimeError with the reference's message on a mismatch."""
+    st = np.ascontiguousarray(stamp, dtype=np.int32)
+    nEq, nNo, nX, tDof, dFlag = int(st[1]), int(st[3]), int(st[4]), int(st[5]), int(st[6])
+    out = {"iNorm": np.zeros(nEq), "xo": np.zeros(max(nX, 1)), "Yo": np.zeros((nNo, tDof)),
+           "Ao": np.zeros((nNo, tDof)), "Do": np.zeros((nNo, tDof)) if dFlag else None}
+    cts, t, cpu = C.c_int(), C.c_double(), C.c_double()
+    rc = lib().svgpu_read_restart(None, str(path).encode(), _ptr(st), C.byref(cts), C.byref(t), C.byref(cpu),
+                                  _ptr(out["iNorm"]), _ptr(out["xo"]), _ptr(out["Yo"]), _ptr(out["Ao"]),
+                                  _ptr(out["Do"]))
+    if rc != SVGPU_OK:
+        raise RuntimeError(_restart_error(path, st))
+    out.update(cTS=cts.value, time=t.value, cpu_time=cpu.value)
+    out["xo"] = out["xo"][:nX]
+    return out
+
+
+def _restart_error(path, stamp):
+    """The reference's message for a restart file that does not fit (initialize.cpp:213-238)."""
+    what = ["The number of processors ", "The number of equations ", "The number of meshes ", "The number of nodes ",
+            "The number of ncplBC.x ", "The number of dof ", "The dFlag specification "]
+    try:
+        t = np.fromfile(path, dtype=np.int32, count=7)
+    except OSError:
+        return f"read_restart: cannot open {path}"
+    for i in range(min(7, t.size)):
+        if t[i] != stamp[i]:
+            return f"{what[i]} {t[i]} read from '{path}' don't match."
+    return f"read_restart: file too short: {path}"
+
+
 def csr_pattern(nNo: int, ien: np.ndarray):
     """lhsa (lhsa.cpp:153): rowPtr/colPtr of the element cliques, sorted columns
     (native svgpu_lhsa)."""
@@ -430,7 +507,9 @@ class PipeFluidSolver:
 
     def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, sD=50, mItr=100, relTol=1e-8, absTol=1e-17,
                  newton_min=3, newton_max=3, newton_tol=1e-11, precision=SVGPU_FP64, rowPtr=None, colPtr=None,
-                 ls_type=LS_TYPE_GMRES):
+                 ls_type=LS_TYPE_GMRES, rcr=None):
+        """rcr: None for a traction-free outlet, or dict(Rp, C, Rd, Pd, Xo) for a coupled
+        RCR outlet (linear-solver face 2)."""
         self.mesh = mesh
         self.props = props or fluid_props()
         self.ctx = Context(device)
@@ -438,13 +517,16 @@ class PipeFluidSolver:
         if rowPtr is None:
             rowPtr, colPtr = csr_pattern(nNo, mesh.ien)
         self.rowPtr, self.colPtr = rowPtr, colPtr
-        self.ctx.fsils_lhs_create(nNo, rowPtr, colPtr, 2)
+        self.ctx.fsils_lhs_create(nNo, rowPtr, colPtr, 3 if rcr else 2)
         self.ctx.fsils_bc_create(0, mesh.faces["inlet"].gN, 3, BC_TYPE_Dir)
         self.ctx.fsils_bc_create(1, mesh.faces["wall"].gN, 3, BC_TYPE_Dir)
         self.ctx.fsils_ls_create(ls_type, relTol, absTol, mItr, sD)
         self.ctx.mesh_create(mesh.x, mesh.ien)
         out = mesh.faces["outlet"]
         self.ctx.face_create(FACE_OUTLET, out.ien, out.gE)
+        if rcr:
+            self.ctx.rcr_create(FACE_OUTLET, 2, rcr["Rp"], rcr["C"], rcr["Rd"], rcr.get("Pd", 0.0), rcr.get("Xo", 0.0),
+                                self.props.dt, 0.0)
         self.dir_nodes, self.dir_prof = dirichlet_nodes(mesh)
         self.ctx.set_dirichlet(self.dir_nodes)
         self.opts = NewtonOpts(newton_min, newton_max, newton_tol, precision, FACE_OUTLET, 0.0)

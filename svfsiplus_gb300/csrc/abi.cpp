@@ -121,6 +121,7 @@ struct CycleGraph {
   const void* vbase = nullptr;  // the basis the graph was captured on
   long n = 0;
   int sD = 0, dof = 0;
+  long long coupled_sig = 0;  // coupled faces baked into the captured products
   long long kernels = 0;  // kernel nodes in the graph (launches counted per graph launch)
   ~CycleGraph() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -138,12 +139,56 @@ std::map<const svgpu_ctx*, CtxGraphs>& graphs() {
   return g;
 }
 
+}  // namespace
+
+void svgpu::add_coupled(svgpu_ctx* ctx, int dof, const double* X, double* Y, const int* flags) {
+  for (int f : ctx->coupled) {
+    LsFace& fa = ctx->faces[f];
+    launch_add_bc_mul(ctx->stream, fa.nNo, fa.dof, dof, fa.d_glob.p, fa.d_valM.p, fa.d_res.p, X, Y, flags);
+    ctx->launches++;
+  }
+}
+
+void svgpu::add_coupled32(svgpu_ctx* ctx, const float* X, float* Y, const int* flags) {
+  for (int f : ctx->coupled) {
+    LsFace& fa = ctx->faces[f];
+    launch_add_bc_mul32(ctx->stream, fa.nNo, fa.dof, 4, fa.d_glob.p, fa.d_valM.p, fa.d_res.p, X, Y, flags);
+    ctx->launches++;
+  }
+}
+
+namespace {
+
+// coupledFlag of every face for this solve (solve.cpp:60-93): a Neumann face that the
+// solve includes and whose resistance is non-zero; valM = val * W (precond.cpp:246-256)
+int setup_coupled(svgpu_ctx* ctx, int dof, const int* incL, const double* res, const double* W) {
+  ctx->coupled.clear();
+  ctx->coupled_sig = 0;
+  if (!res) return SVGPU_OK;
+  for (int f = 0; f < ctx->nFaces; f++) {
+    LsFace& fa = ctx->faces[f];
+    if (!fa.created || fa.bGrp != SVGPU_BC_NEU || (incL && incL[f] == 0) || res[f] == 0.0) continue;
+    fa.res = res[f];
+    SVGPU_CUDA(ctx, fa.d_res.resize(1));
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(fa.d_res.p, &fa.res, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    SVGPU_CUDA(ctx, fa.d_valM.resize((size_t)fa.dof * std::max(fa.nNo, 1)));
+    launch_face_valm(ctx->stream, fa.nNo, fa.dof, dof, fa.d_glob.p, fa.d_val.p, W, fa.d_valM.p);
+    ctx->launches++;
+    ctx->coupled.push_back(f);
+    ctx->coupled_sig = ctx->coupled_sig * 131 + f + 1;
+  }
+  // the host value behind d_res must not change before the copy runs
+  if (!ctx->coupled.empty()) SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
 void spmv_any(svgpu_ctx* ctx, int dof, const double* Val, const double* x, double* y, const int* flags) {
   if (dof == 4)
     launch_spmv4_f64_flag(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val, x, y, flags);
   else
     launch_spmv_generic(ctx->stream, ctx->nNo, dof, ctx->rowPtr.p, ctx->colPtr.p, Val, x, y);
   ctx->launches++;
+  add_coupled(ctx, dof, x, y, flags);  // add_bc_mul after every product (gmres.cpp:510,539)
 }
 
 // Enqueues the Arnoldi iterations i = 0..sD-1 (gmres.cpp:529-593).
@@ -175,7 +220,8 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val, int slot_index = 0) {
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
-  if (!g.exec || g.val != Val || g.vbase != ctx->kw.V.p || g.n != n || g.sD != ctx->kw.sD || g.dof != dof) {
+  if (!g.exec || g.val != Val || g.vbase != ctx->kw.V.p || g.n != n || g.sD != ctx->kw.sD || g.dof != dof ||
+      g.coupled_sig != ctx->coupled_sig) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -202,6 +248,7 @@ int run_cycle(svgpu_ctx* ctx, int dof, const double* Val, int slot_index = 0) {
     g.n = n;
     g.sD = ctx->kw.sD;
     g.dof = dof;
+    g.coupled_sig = ctx->coupled_sig;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
   ctx->launches += g.kernels;
@@ -364,6 +411,7 @@ void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
     float* ui = kw.V32.p + (long)i * n;
     float* ui1 = kw.V32.p + (long)(i + 1) * n;
     launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, ui, ui1, kw.flags.p);
+    add_coupled32(ctx, ui, ui1, kw.flags.p);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
                                        kw.flags.p);
     launch_reduce_partials_flag(ctx->stream, ctas, i + 2, kw.partial.p, hraw, kw.flags.p);
@@ -392,6 +440,7 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
       amg_vcycle(ctx, ui, zi, kw.flags.p);
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_SPMV);
     launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
+    add_coupled32(ctx, zi, ui1, kw.flags.p);
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_ORTHO);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
                                        kw.flags.p);
@@ -415,7 +464,8 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
   if (!slot) slot.reset(new CycleGraph());
   CycleGraph& g = *slot;
   const long n = (long)ctx->kw.n;
-  if (!g.exec || g.val != Val32 || g.vbase != ctx->kw.V32.p || g.n != n || g.sD != ctx->kw.sD) {
+  if (!g.exec || g.val != Val32 || g.vbase != ctx->kw.V32.p || g.n != n || g.sD != ctx->kw.sD ||
+      g.coupled_sig != ctx->coupled_sig) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -443,6 +493,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     g.n = n;
     g.sD = ctx->kw.sD;
     g.dof = 4;
+    g.coupled_sig = ctx->coupled_sig;
   }
   SVGPU_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
   ctx->launches += g.kernels;
@@ -539,6 +590,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     ctx->launches += 3;
     if ((rc = gnn_apply_device(ctx, nullptr, Rs, g.scal.p, nullptr, kw.X.p, nullptr))) return rc;
     launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+    add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
     launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
     ctx->launches += 2;
     const double n0 = device_norm(ctx, n, kw.r64.p, rc);
@@ -558,6 +610,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     phase_mark(ctx, PH_RESTART);
     if (l > 0) {
       launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+    add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
       launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
       ctx->launches += 2;
       nrm = device_norm(ctx, n, kw.r64.p, rc);
@@ -600,6 +653,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
     if (l + 1 == ctx->mItr) {  // final true residual
       launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+    add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
       launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
       ctx->launches += 2;
       nrm = device_norm(ctx, n, kw.r64.p, rc);
@@ -616,7 +670,8 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
 // fsils_solve for the FP32 resident matrix: diagonal preconditioning computed in FP64
 // from the FP32 diagonal, Val32 scaled in place, R scaled and solved in the FP64
 // defect-correction loop, R <- W X.
-int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st) {
+int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
+                       const double* res = nullptr) {
   auto t0 = std::chrono::steady_clock::now();
   const long n = 4L * ctx->nNo;
   int rc = ensure_krylov(ctx, n, ctx->sD);
@@ -636,6 +691,7 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   launch_scale_val32(ctx->stream, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, kw.Wc.p, Val32);
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches += 3;
+  if ((rc = setup_coupled(ctx, 4, incL, res, kw.Wc.p))) return rc;
   if (ctx->learned_mode >= 2) {
     if (!ctx->amg && (rc = amg_build(ctx))) return rc;
     ctx->amg->gnn_smoother = ctx->learned_mode == 3 && ctx->gnn;
@@ -646,6 +702,8 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   const bool collect = ctx->gnn && ctx->gnn->collect;
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
   rc = gmres_mixed(ctx, Val32, R, R, st);
+  ctx->coupled.clear();
+  ctx->coupled_sig = 0;
   if (rc) return rc;
   phase_mark(ctx, PH_OTHER);
   if (ctx->zero_null_rows && ctx->learned_mode != 0) {
@@ -669,7 +727,7 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
 
 // fsils_solve on device arrays (solve.cpp:50-193).
 int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, const int* incL,
-                 svgpu_ls_stats* st) {
+                 svgpu_ls_stats* st, const double* res = nullptr) {
   auto t0 = std::chrono::steady_clock::now();
   const long n = (long)ctx->nNo * dof;
   int rc = ensure_krylov(ctx, n, ctx->sD);
@@ -695,6 +753,12 @@ int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, cons
     launch_fill(ctx->stream, n, 1.0, kw.Wc.p);
     ctx->launches++;
   }
+  if ((rc = setup_coupled(ctx, dof, incL, res, kw.Wc.p))) return rc;
+  if (!ctx->coupled.empty() && ctx->lsType != SVGPU_LS_GMRES) {
+    ctx->coupled.clear();
+    ctx->coupled_sig = 0;
+    return set_err(ctx, SVGPU_EINVAL, "fsils_solve: coupled Neumann faces need GMRES");
+  }
   if (ctx->lsType == SVGPU_LS_CG)
     rc = cg_device(ctx, dof, Val, R, st);
   else if (ctx->lsType == SVGPU_LS_NS)
@@ -702,6 +766,8 @@ int solve_device(svgpu_ctx* ctx, int dof, double* R, double* Val, int prec, cons
                   : set_err(ctx, SVGPU_EINVAL, "NS solver: dof must be 4 (3 velocity + pressure)");
   else
     rc = gmres_device(ctx, dof, Val, R, st);
+  ctx->coupled.clear();
+  ctx->coupled_sig = 0;
   if (rc) return rc;
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches++;
@@ -766,12 +832,14 @@ int backflow_device(svgpu_ctx* ctx, int faceId, const svgpu_fluid_props* props, 
 
 }  // namespace
 
-int svgpu::solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st) {
-  return solve_device(ctx, dof, R, Val, SVGPU_PREC_FSILS, incL, st);
+int svgpu::solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st,
+                      const double* res) {
+  return solve_device(ctx, dof, R, Val, SVGPU_PREC_FSILS, incL, st, res);
 }
 
-int svgpu::solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st) {
-  return solve_device_mixed(ctx, R, Val32, incL, st);
+int svgpu::solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
+                       const double* res) {
+  return solve_device_mixed(ctx, R, Val32, incL, st, res);
 }
 
 svgpu::FluidConsts svgpu::fluid_consts_of(const svgpu_fluid_props* p) { return fluid_consts(p); }
@@ -941,10 +1009,6 @@ int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec
     return set_err(ctx, SVGPU_EINVAL, "fsils_solve: device arrays must be 16-byte aligned");
   if (ctx->nNo == 0 || !ctx->ls_created) return set_err(ctx, SVGPU_ESTATE, "fsils_solve before lhs/ls create");
   if (dof < 1 || dof > 8) return set_err(ctx, SVGPU_EINVAL, "fsils_solve: dof must be 1..8");
-  if (res)
-    for (int f = 0; f < ctx->nFaces; f++)
-      if (res[f] != 0.0 && ctx->faces[f].bGrp == SVGPU_BC_NEU && (!incL || incL[f] != 0))
-        return set_err(ctx, SVGPU_EINVAL, "fsils_solve: coupled Neumann faces are not supported");
   svgpu_ls_stats local;
   svgpu_ls_stats* st = stats ? stats : &local;
   std::memset(st, 0, sizeof(*st));
@@ -954,8 +1018,8 @@ int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec
   if (!Ri && !Val) {
     if (dof != 4 || !ctx->R.p || (!ctx->Val.p && !ctx->Val32.p))
       return set_err(ctx, SVGPU_ESTATE, "no resident system to solve");
-    if (ctx->resident_mixed) return solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL, st);
-    return solve_device(ctx, dof, ctx->R.p, ctx->Val.p, prec, incL, st);
+    if (ctx->resident_mixed) return solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL, st, res);
+    return solve_device(ctx, dof, ctx->R.p, ctx->Val.p, prec, incL, st, res);
   }
   if (!Ri || !Val) return set_err(ctx, SVGPU_EINVAL, "fsils_solve: Ri and Val must both be given");
   const bool dR = is_device_ptr(Ri), dV = is_device_ptr(Val);
@@ -969,7 +1033,7 @@ int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec
     if ((rc = to_device(ctx, ctx->stage2, Val, nv))) return rc;
     Vd = ctx->stage2.p;
   }
-  rc = solve_device(ctx, dof, Rd, Vd, prec, incL, st);
+  rc = solve_device(ctx, dof, Rd, Vd, prec, incL, st, res);
   if (rc) return rc;
   if (!dR) SVGPU_CUDA(ctx, cudaMemcpyAsync(Ri, Rd, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (!dV) SVGPU_CUDA(ctx, cudaMemcpyAsync(Val, Vd, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1505,10 +1569,15 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
   launch_set_dirichlet(ctx->stream, ctx->nDir, ctx->dirNodes.p, ctx->dirY.p, ctx->dirA.p, ctx->An.p, ctx->Yn.p);
   ctx->launches += 2;
   std::vector<int> incL(ctx->nFaces, 1);
+  // a coupled RCR outlet: resistance term of its linear-solver face (main.cpp:566-573)
+  const bool rcr = ctx->rcr && opts->outletFace == ctx->rcr->meshFace;
+  std::vector<double> res(ctx->nFaces, 0.0);
+  if (rcr) res[ctx->rcr->lsFace] = props->gam * props->dt * ctx->rcr->r;
   int itr = 0;
   for (;;) {
     itr++;
     phase_mark(ctx, PH_OTHER);
+    if (rcr && (rc = rcr_update(ctx, ctx->Yo.p, ctx->Yn.p, 4, props->dt))) return rc;  // set_bc_cpl, main.cpp:385-392
     launch_pic_initiate(ctx->stream, n4, props->am, props->af, ctx->Ao.p, ctx->An.p, ctx->Yo.p, ctx->Yn.p, ctx->Ag.p,
                         ctx->Yg.p);
     ctx->launches++;
@@ -1516,7 +1585,9 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr, opts->precision)))
       return rc;
     if (opts->outletFace >= 0) {
-      rc = backflow_device(ctx, opts->outletFace, props, opts->outletH, ctx->Yg.p, ctx->R.p,
+      // the RCR pressure enters as the Neumann value -P on every face node (set_bc_neu_l, set_bc.cpp:1377-1418)
+      const double h = rcr ? -ctx->rcr->y : opts->outletH;
+      rc = backflow_device(ctx, opts->outletFace, props, h, ctx->Yg.p, ctx->R.p,
                            opts->precision == SVGPU_FP64 ? ctx->Val.p : nullptr,
                            opts->precision == SVGPU_FP64 ? nullptr : ctx->Val32.p);
       if (rc) return rc;
@@ -1524,9 +1595,9 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     svgpu_ls_stats st;
     std::memset(&st, 0, sizeof(st));
     if (opts->precision == SVGPU_FP64)
-      rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st);
+      rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st, res.data());
     else
-      rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st);
+      rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st, res.data());
     if (rc) return rc;
     phase_mark(ctx, PH_OTHER);
     if (stats) stats[itr - 1] = st;
@@ -1545,6 +1616,7 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                l4 = itr >= opts->minItr;
     if (l1 || ((l2 || l3) && l4)) break;
   }
+  if (rcr) ctx->rcr->xo = ctx->rcr->xn;  // cplBC.xo = cplBC.xn at the end of the step (main.cpp:758)
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, ctx->An.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, ctx->Yn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, ctx->Dn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));

@@ -63,7 +63,28 @@ struct LsFace {
   std::vector<double> val;  // (dof, nNo)
   DevBuf<int> d_glob;
   DevBuf<double> d_val;
+  // coupled Neumann face of the current solve (coupledFlag, solve.cpp:80-92): its
+  // resistance res and valM = val * W (precond.cpp:246-256)
+  double res = 0.0;
+  DevBuf<double> d_res, d_valM;
 };
+
+// A coupled RCR (Windkessel) outlet (cplBCType with one RCR face, ComMod.h:775-800):
+// the mesh face its flow rate and pressure act on, the linear-solver face of its
+// resistance term, the 0D parameters and state.
+struct RcrOutlet {
+  int meshFace = -1, lsFace = -1;
+  double Rp = 0, C = 0, Rd = 0, Pd = 0;
+  double xo = 0, xn = 0;      // 0D state at t and t + dt (cplBC.xo / xn)
+  double y = 0;               // imposed pressure (cplBC.fa.y, bc.g)
+  double Qo = 0, Qn = 0;      // outlet flow rates
+  double r = 0;               // resistance dP/dQ (calc_der_cpl_bc)
+  DevBuf<double> part, q;     // flux partial sums, device results
+};
+// RCR_Integ_X (set_bc.cpp:460-547) for one face: the 0D state xn at t + dt and the
+// pressure y from xo and the flow rates at t and t + dt (rcr.cpp)
+void rcr_integrate(double Rp, double C, double Rd, double Pd, double dt, double xo, double Qo, double Qn, double* xn,
+                   double* y);
 
 // A boundary face of the mesh (faceType, ComMod.h:520) with its scatter data.
 struct MeshFace {
@@ -245,6 +266,9 @@ struct svgpu_ctx {
   svgpu::DevBuf<int> cg_f;              // CG: stop, last_i, suc, next iteration
   std::unique_ptr<svgpu::GnnState> gnn;
   std::unique_ptr<svgpu::FsiWork> fsi;  // coupled FSI time step
+  std::unique_ptr<svgpu::RcrOutlet> rcr;  // coupled RCR outlet of the fluid step
+  std::vector<int> coupled;             // coupled Neumann faces of the current solve
+  long long coupled_sig = 0;            // their signature (captured cycles depend on it)
   std::unique_ptr<struct svgpu::AmgState> amg;
   const float* amg_val0 = nullptr;  // level-0 matrix of the current numeric set-up
   // 0: GMRES + diagonal preconditioner (the reference's method)
@@ -337,10 +361,12 @@ int schur_cg_device(svgpu_ctx* ctx, const double* G, const double* D, const doub
 int ns_solve_device(svgpu_ctx* ctx, const double* Val, double* R, svgpu_ls_stats* st);
 // fsils_solve with the diagonal preconditioner on device arrays (abi.cpp), with the
 // context's current linear-solver settings
-int solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st);
+int solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st,
+               const double* res = nullptr);
 // the mixed-precision solve of a dof-4 system with an FP32 tangent (abi.cpp), with the
 // context's solver mode
-int solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st);
+int solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
+                const double* res = nullptr);
 // k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
 int cg_parts(long n);
 void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
@@ -390,6 +416,22 @@ void launch_xupdate32(cudaStream_t s, long n, int sD, const float* V, long ldv, 
                       double* X);
 void launch_sub(cudaStream_t s, long n, const double* R, const double* y, double* r);
 void launch_zero_null_rows(cudaStream_t s, int nNo, const int* rowPtr, const float* Val, double* X);
+// ---- k_coupled.cu: coupled Neumann faces ------------------------------------------
+void launch_add_bc_mul(cudaStream_t s, int nNo, int fdof, int dof, const int* glob, const double* valM,
+                       const double* res, const double* X, double* Y, const int* flags);
+void launch_add_bc_mul32(cudaStream_t s, int nNo, int fdof, int dof, const int* glob, const double* valM,
+                         const double* res, const float* X, float* Y, const int* flags);
+void launch_face_valm(cudaStream_t s, int nNo, int fdof, int dof, const int* glob, const double* val, const double* W,
+                      double* valM);
+void launch_face_flux(cudaStream_t s, int ne, const int* fien, const int* inner, const double* x4, int ld,
+                      const double* Y, double* part, double* out);
+// set_bc_cpl for the context's RCR outlet: flow rates of Yo and Yn ((ld, nNo) arrays),
+// the 0D step, the outlet pressure (rcr.cpp)
+int rcr_update(svgpu_ctx* ctx, const double* Yo, const double* Yn, int ld, double dt);
+// the rank-one terms of the current solve's coupled faces on an operator product
+// Y = K X (abi.cpp); flags may be NULL
+void add_coupled(svgpu_ctx* ctx, int dof, const double* X, double* Y, const int* flags);
+void add_coupled32(svgpu_ctx* ctx, const float* X, float* Y, const int* flags);
 void launch_start_vector32(cudaStream_t s, long n, const double* r, const double* nrm2, float* u0, double* err0,
                            int* flags);
 

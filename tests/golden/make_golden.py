@@ -46,6 +46,11 @@ CASES = {
                     ls_max_itr=10),
     "small_ns": dict(mesh="small", n_steps=3, dump_step=1, dump_iter=1, u_amp=5.0, ls_type="ns",
                      ls_rel_tol=1e-4, ls_max_itr=10),
+    # a coupled RCR (Windkessel) outlet with the reference's pipe_RCR_3d values
+    # (tests/cases/fluid/pipe_RCR_3d/solver.xml): semi-implicit coupling, the outlet's
+    # resistance term in every GMRES product (add_bc_mul.cpp:53)
+    "small_rcr": dict(mesh="small", n_steps=3, dump_step=2, dump_iter=2, u_amp=5.0, rcr=1, rcr_Rp=121.0,
+                      rcr_C=1.5e-5, rcr_Rd=1212.0, rcr_Pd=0.0, rcr_Xo=0.0),
 }
 
 
@@ -198,6 +203,7 @@ def run_fsi_steps(name, mesh_name):
         for s in range(1, params["n_steps"] + 1):
             for k in ("An", "Yn", "Dn"):
                 out[f"{k}_{s}"] = rd(f"{k}_{s}.bin", np.float64).reshape(nNo, tDof)
+        out["restart_bin"] = rd("stFile_last.bin", np.uint8)
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
         print(name, "nNo", nNo, "nEl", mesh.nEl, "solid", int((mesh.eid == 2).sum()))
         print(log)
@@ -239,14 +245,23 @@ def run_case(name):
         for line in log.splitlines():
             t = line.split()
             if t[0] == "step":
+                kv = dict(zip(t[0::2], t[1::2]))
                 row = [int(t[1]), int(t[3]), float(t[5]), float(t[7]), int(t[9]), int(t[11])]
-                if len(t) > 12:  # NS: inner GMRES and CG iteration totals, dB
-                    row += [int(t[13]), int(t[15]), float(t[17])]
+                if "gm_itr" in kv:  # NS: inner GMRES and CG iteration totals, dB
+                    row += [int(kv["gm_itr"]), int(kv["cg_itr"]), float(kv["dB"])]
+                if "P" in kv:  # RCR outlet: coupled pressure and the outlet flows at n and n+1
+                    row += [float(kv["P"]), float(kv["Qo"]), float(kv["Qn"])]
                 its.append(row)
+            elif t[0] == "rcr_r":
+                out["rcr_r"] = np.array(float(t[1]))
         out["newton_log"] = np.array(its, dtype=np.float64)
         rd = lambda f, dt: np.fromfile(os.path.join(odir, f), dtype=dt)  # noqa: E731
         out["rowPtr"] = rd("rowPtr.bin", np.int32)
         out["colPtr"] = rd("colPtr.bin", np.int32)
+        if params.get("rcr") == 1:
+            out["rcr_face_val"] = rd("rcr_face_val.bin", np.float64).reshape(-1, 3)
+        # the reference's restart file of the final state (output::write_restart)
+        out["restart_bin"] = rd("stFile_last.bin", np.uint8)
         out["Ag"] = rd("Ag.bin", np.float64).reshape(nNo, 4)
         out["Yg"] = rd("Yg.bin", np.float64).reshape(nNo, 4)
         out["R_asm"] = rd("R_asm.bin", np.float64).reshape(nNo, 4)
