@@ -246,6 +246,10 @@ class Context:
         self._check(lib().svgpu_rcr_create(self._h, int(mesh_face), int(ls_face),
                                            *(C.c_double(v) for v in (Rp, Cap, Rd, Pd, Xo, dt, Q0))), "rcr_create")
 
+    def rcr_set_state(self, xo):
+        """Set the RCR outlet's 0D state (a restart)."""
+        self._check(lib().svgpu_rcr_set_state(self._h, C.c_double(xo)), "rcr_set_state")
+
     def rcr_state(self):
         """{xo, xn, P, Qo, Qn, r} of the RCR outlet after the last Newton iteration."""
         out = (C.c_double * 6)()
@@ -534,6 +538,26 @@ class PipeFluidSolver:
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.norms = [0.0, 0.0]
         self.time = 0.0
+        self.cTS = 0
+        self.has_rcr = bool(rcr)
+
+    def _stamp(self):
+        return restart_stamp(1, self.mesh.nNo, 4, False, nX=1 if self.has_rcr else 0)
+
+    def save_restart(self, path):
+        """The reference's restart file of the current state (output::write_restart)."""
+        xn = self.ctx.rcr_state()["xo"] if self.has_rcr else None
+        write_restart(path, self._stamp(), self.cTS, self.time, [self.norms[0]], self.Yo, self.Ao, xn=xn)
+
+    def load_restart(self, path):
+        """Continue from a restart file (init_from_bin): state, time, step count, the
+        equation's iNorm and the 0D state."""
+        r = read_restart(path, self._stamp())
+        self.Yo[:], self.Ao[:] = r["Yo"], r["Ao"]
+        self.time, self.cTS = r["time"], r["cTS"]
+        self.norms[0] = float(r["iNorm"][0])
+        if self.has_rcr:
+            self.ctx.rcr_set_state(float(r["xo"][0]))
 
     def enable_learning(self, seed=1):
         """Create the learned preconditioner and start collecting (residual, increment)
@@ -543,6 +567,7 @@ class PipeFluidSolver:
 
     def step(self, u_mean=10.0, u_amp=0.0, freq=1.0):
         self.time += self.props.dt
+        self.cTS += 1
         dirY, dirA = inflow(self.dir_prof, self.time, u_mean, u_amp, freq)
         stats = self.ctx.fluid_step(self.props, self.opts, dirY, dirA, self.Ao, self.Yo, self.Do,
                                     self.An, self.Yn, self.Dn, self.norms)
@@ -625,9 +650,22 @@ class PipeFsiSolver:
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.iNorm, self.pNorm = [0.0, 0.0], [0.0, 0.0]
         self.time = 0.0
+        self.cTS = 0
+
+    def save_restart(self, path):
+        """The reference's restart file (two equations, tDof 7, dFlag)."""
+        write_restart(path, restart_stamp(2, self.mesh.nNo, 7, True), self.cTS, self.time, self.iNorm, self.Yo,
+                      self.Ao, Dn=self.Do)
+
+    def load_restart(self, path):
+        r = read_restart(path, restart_stamp(2, self.mesh.nNo, 7, True))
+        self.Yo[:], self.Ao[:], self.Do[:] = r["Yo"], r["Ao"], r["Do"]
+        self.time, self.cTS = r["time"], r["cTS"]
+        self.iNorm[:] = [float(v) for v in r["iNorm"]]
 
     def step(self, u_mean=15.0, u_amp=5.0, freq=1.0):
         self.time += self.props.fluid.dt
+        self.cTS += 1
         dY, dA = inflow(self.profF, self.time, u_mean, u_amp, freq)
         zm = np.zeros((self.dirM.size, 3))
         stats = self.ctx.fsi_step(self.props, self.opts, (self.dirF, dY, dA), (self.dirM, zm, zm), self.Ao, self.Yo,
