@@ -242,6 +242,14 @@ int svgpu_write_restart(svgpu_ctx* ctx, const char* path, const int* stamp, int 
 int svgpu_read_restart(svgpu_ctx* ctx, const char* path, const int* stamp, int* cTS, double* time, double* cpu_time,
                        double* iNorm, double* xo, double* Yo, double* Ao, double* Do);
 
+/* ---- result files (write_vtus, vtk_xml.cpp:800-1010, without the VTK library) -------
+ * Host-only; ctx may be NULL.  A VTK XML UnstructuredGrid of nNo points x (3,nNo) and
+ * nEl linear tets (eNoN 4) or triangles (eNoN 3) ien (eNoN,nEl), with nFields point
+ * fields data[f] (ncomp[f], nNo) named names[f] (the reference's names: "Velocity",
+ * "Pressure", "Displacement", ...); raw appended data with UInt64 headers. */
+int svgpu_write_vtu(svgpu_ctx* ctx, const char* path, int nNo, const double* x, int nEl, int eNoN, const int* ien,
+                    int nFields, const char* const* names, const int* ncomp, const double* const* data);
+
 /* ---- learned preconditioner (no counterpart in the reference) ------------------------
  * A 3-layer message-passing network on the CSR graph (hidden width 64, BF16 weights,
  * FP32 accumulation) trained online on (residual, increment) pairs of the

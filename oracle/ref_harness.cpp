@@ -36,6 +36,7 @@
 #include "baf_ini.h"
 #include "set_bc.h"
 #include "output.h"
+#include "fft.h"
 
 #include <cmath>
 #include <cstdio>
@@ -640,6 +641,41 @@ static int run_fsi(const std::string& dir, const std::string& out, std::map<std:
   return 0;
 }
 
+// Fourier representation of a temporal values file (fft / ifft, fft.cpp:36-140): the
+// coefficients and the value and derivative at the requested times.
+static int run_fourier(const std::string& dir, const std::string& out, std::map<std::string, std::string>& P) {
+  auto tv = read_raw<double>(dir + "/tv.bin");  // (t, q) pairs
+  auto times = read_raw<double>(dir + "/times.bin");
+  const int np = (int)tv.size() / 2;
+  std::vector<std::vector<double>> temporal_values(np);
+  for (int i = 0; i < np; i++) temporal_values[i] = {tv[2 * i], tv[2 * i + 1]};
+  Simulation sim;
+  fcType gt;
+  gt.d = 1;
+  gt.n = std::stoi(P.at("n_modes"));
+  gt.lrmp = std::stoi(P.at("ramp")) != 0;
+  if (gt.lrmp) gt.n = 1;
+  gt.qi.resize(1);
+  gt.qs.resize(1);
+  gt.r.resize(1, gt.n);
+  gt.i.resize(1, gt.n);
+  fft(np, temporal_values, gt);
+  std::vector<double> res;
+  Vector<double> Y(1), dY(1);
+  for (double t : times) {
+    sim.com_mod.time = t;
+    ifft(sim.com_mod, gt, Y, dY);
+    res.push_back(Y(0));
+    res.push_back(dY(0));
+  }
+  write_raw(out + "/eval.bin", res.data(), res.size());
+  std::vector<double> coef = {gt.ti, gt.T, gt.qi(0), gt.qs(0)};
+  for (int k = 0; k < gt.n; k++) coef.push_back(gt.r(0, k));
+  for (int k = 0; k < gt.n; k++) coef.push_back(gt.i(0, k));
+  write_raw(out + "/coef.bin", coef.data(), coef.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::fprintf(stderr, "usage: %s CASE_DIR OUT_DIR\n", argv[0]);
@@ -649,6 +685,7 @@ int main(int argc, char** argv) {
   auto P = read_params(dir);
   if (P.count("mode") && P.at("mode") == "assemble_fsi") return assemble_fsi(dir, out, P);
   if (P.count("mode") && P.at("mode") == "fsi_run") return run_fsi(dir, out, P);
+  if (P.count("mode") && P.at("mode") == "fourier") return run_fourier(dir, out, P);
   if (P.count("mode") && P.at("mode").rfind("assemble_", 0) == 0) return assemble_only(dir, out, P);
   auto getd = [&](const char* k) { return std::stod(P.at(k)); };
   auto geti = [&](const char* k) { return std::stoi(P.at(k)); };

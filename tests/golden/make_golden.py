@@ -211,6 +211,37 @@ def run_fsi_steps(name, mesh_name):
         shutil.rmtree(tmp)
 
 
+# Fourier representation of a pulsatile inflow waveform (fft/ifft, fft.cpp): a seeded
+# synthetic flow curve of one period (a cardiac-like pulse: systolic peak, dicrotic
+# notch), 10 modes, evaluated at times across three periods; and the ramp variant.
+def run_fourier(name):
+    rng = np.random.default_rng(31)
+    t = np.linspace(0.0, 1.0, 41)
+    q = -(5.0 + 20.0 * np.exp(-((t - 0.18) / 0.07) ** 2) + 3.0 * np.exp(-((t - 0.45) / 0.05) ** 2))
+    q += 0.2 * rng.standard_normal(t.size)
+    q[-1] = q[0]
+    times = np.concatenate([np.linspace(0.0, 3.0, 61), [0.0005, 1.2345, 2.999]])
+    out = {}
+    for ramp in (0, 1):
+        tmp = tempfile.mkdtemp(prefix=f"golden_{name}_")
+        try:
+            cdir, odir = os.path.join(tmp, "case"), os.path.join(tmp, "out")
+            os.makedirs(cdir)
+            os.makedirs(odir)
+            np.stack([t, q], axis=1).astype(np.float64).tofile(os.path.join(cdir, "tv.bin"))
+            times.astype(np.float64).tofile(os.path.join(cdir, "times.bin"))
+            with open(os.path.join(cdir, "params.txt"), "w") as fh:
+                fh.write(f"mode=fourier\nn_modes=10\nramp={ramp}\n")
+            subprocess.run([HARNESS, cdir, odir], check=True)
+            out[f"eval_ramp{ramp}"] = np.fromfile(os.path.join(odir, "eval.bin"), dtype=np.float64).reshape(-1, 2)
+            out[f"coef_ramp{ramp}"] = np.fromfile(os.path.join(odir, "coef.bin"), dtype=np.float64)
+        finally:
+            shutil.rmtree(tmp)
+    out.update(t=t, q=q, times=times)
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+    print(name, out["coef_ramp0"][:6])
+
+
 def write_case(mesh, d, params):
     os.makedirs(d, exist_ok=True)
     mesh.x.astype(np.float64).tofile(os.path.join(d, "x.bin"))
@@ -284,11 +315,13 @@ if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: oracle/build_ref.sh")
     for n in (sys.argv[1:] or list(CASES) + ["struct_small", "mesh_small", "mesh_cg_small", "mesh_cg7_small",
-                                             "fsi_small", "fsi_run_small"]):
+                                             "fsi_small", "fsi_run_small", "fourier"]):
         if n == "fsi_small":
             run_fsi(n)
         elif n == "fsi_run_small":
             run_fsi_steps(n, "fsi_small")
+        elif n == "fourier":
+            run_fourier(n)
         elif n == "struct_small":
             run_assembly(n, "struct")
         elif n == "mesh_small":
