@@ -200,9 +200,17 @@ def spmv_roofline(ctx, colPtr, nNo, mode, stream, reps=20):
     bytes_ = spmv_bytes(colPtr.size, nNo, vb, vb)
     peak, kind = peaks()
     achieved = bytes_ / (ms * 1e-3) / 1e9
+    # DRAM bytes per launch of this kernel on the 8M-tet pipe from one ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches)
+    traffic = TRAFFIC_SPMV4_F32_PIPE8M if (mode >= 0 and colPtr.size == BLOCKS_PIPE8M) else None
     return {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_kind": kind, "traffic": None, "launch_ms": ms,
+            "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
+            "traffic_source": "ncu capture of spmv4_f32_kernel on pipe8m" if traffic else None, "launch_ms": ms,
             "algorithmic_bytes": bytes_, "launches_timed": reps}
+
+
+BLOCKS_PIPE8M = 20334561
+TRAFFIC_SPMV4_F32_PIPE8M = 1.5249e9
 
 
 def kernel_breakdown(step_fn, path):
@@ -537,13 +545,13 @@ def run_fsi(args):
     mesh = named_pipe(name)
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
     out = {"workload": name, "tets": mesh.nEl, "solid_tets": int((mesh.eid == 2).sum()), "nodes": mesh.nNo,
-           "blocks": int(colPtr.size)}
+           "blocks": int(colPtr.size), "mesh_cg_rel_tol": args.mesh_cg_tol}
     fields = {}
     for path in ("multilevel", "plain"):
         mixed = path == "multilevel"
         s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=(1, NEWTON_MAX, NEWTON_TOL),
                               mesh_newton=(1, NEWTON_MAX, NEWTON_TOL),
-                              gmres=(LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM), cg=(1e-6, 1e-17, 5000),
+                              gmres=(LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM), cg=(args.mesh_cg_tol, 1e-17, 5000),
                               rowPtr=rowPtr, colPtr=colPtr, precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64)
         if mixed:
             s.ctx.set_solver_mode(2)
@@ -556,6 +564,8 @@ def run_fsi(args):
             dt = time.perf_counter() - t
             rec = {"s": round(dt, 4), "fsi_its": [d["itr"] for q, d in st if q == 0],
                    "mesh_its": [d["itr"] for q, d in st if q == 1],
+                   "fsi_solve_s": round(sum(d["callD"] for q, d in st if q == 0), 4),
+                   "mesh_solve_s": round(sum(d["callD"] for q, d in st if q == 1), 4),
                    "fsi_final_over_first": [d["iNorm"] for q, d in st if q == 0][-1] /
                                            [d["iNorm"] for q, d in st if q == 0][0],
                    "timed": k >= args.warmup}
@@ -633,6 +643,7 @@ def main():
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
+    ap.add_argument("--mesh-cg-tol", type=float, default=1e-6, help="--fsi: relative tolerance of the mesh CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     args = ap.parse_args()
