@@ -643,7 +643,7 @@ def main():
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
-    ap.add_argument("--mesh-cg-tol", type=float, default=1e-6, help="--fsi: relative tolerance of the mesh CG")
+    ap.add_argument("--mesh-cg-tol", type=float, default=1e-3, help="--fsi: relative tolerance of the mesh CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     args = ap.parse_args()
