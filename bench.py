@@ -61,6 +61,7 @@ NEWTON_TOL = 1e-6
 NEWTON_MAX = 8
 LIN_REL_TOL = 1e-2
 KRYLOV_DIM = 50
+REUSE_TANGENT = False  # mixed paths: tangent of a step's first Newton iteration kept (--reuse-tangent)
 MAX_RESTARTS = 40
 PATH_MODES = {"multilevel": 2, "learned": 4, "learned-smoother": 3, "mixed": 0, "plain": -1}
 U_MEAN, U_AMP, U_FREQ = 10.0, 5.0, 1.0
@@ -299,13 +300,16 @@ def run_assembly_only(args):
     print(json.dumps(out), flush=True)
 
 
-def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newton_max=None, lin_rel_tol=None):
+def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newton_max=None, lin_rel_tol=None,
+                reuse_tangent=None):
     mode = PATH_MODES[path]
     precision = api.SVGPU_FP64 if mode < 0 else api.SVGPU_MIXED
+    reuse = REUSE_TANGENT if reuse_tangent is None else reuse_tangent
     s = api.PipeFluidSolver(mesh, device=device, sD=KRYLOV_DIM, mItr=MAX_RESTARTS,
                             relTol=LIN_REL_TOL if lin_rel_tol is None else lin_rel_tol, absTol=1e-17,
                             newton_min=1, newton_max=newton_max or NEWTON_MAX,
-                            newton_tol=newton_tol or NEWTON_TOL, precision=precision, rowPtr=rowPtr, colPtr=colPtr)
+                            newton_tol=newton_tol or NEWTON_TOL, precision=precision, rowPtr=rowPtr, colPtr=colPtr,
+                            reuse_tangent=reuse and mode >= 0)
     if mode in (3, 4):
         s.enable_learning()
     if mode >= 0:
@@ -646,10 +650,14 @@ def main():
     ap.add_argument("--mesh-cg-tol", type=float, default=1e-3, help="--fsi: relative tolerance of the mesh CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
+    ap.add_argument("--reuse-tangent", type=int, default=None,
+                    help="1: mixed paths keep the tangent of a step's first Newton iteration (modified Newton)")
     args = ap.parse_args()
+    global LIN_REL_TOL, REUSE_TANGENT
     if args.lin_rel_tol is not None:
-        global LIN_REL_TOL
         LIN_REL_TOL = args.lin_rel_tol
+    if args.reuse_tangent is not None:
+        REUSE_TANGENT = bool(args.reuse_tangent)
     if args.impl == "reference":
         run_reference(args)
     elif args.spmv_only:

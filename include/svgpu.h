@@ -311,6 +311,12 @@ typedef struct {
   int precision;             /* SVGPU_FP64 or SVGPU_MIXED */
   int outletFace;            /* face id of the traction-free outlet, -1 for none */
   double outletH;            /* Neumann value on it */
+  /* SVGPU_MIXED only, no reference counterpart: 1 assembles the tangent (and the
+   * diagonal scaling and multilevel set-up) at a step's first Newton iteration only and
+   * reuses it for the later ones, which assemble the FP64 residual alone (a modified
+   * Newton iteration; the residual and the convergence test are unchanged).  0: every
+   * iteration, as the reference. */
+  int reuse_tangent;
 } svgpu_newton_opts;
 
 /* Strong-Dirichlet node set (the velocity rows removed by the Dirichlet faces). */

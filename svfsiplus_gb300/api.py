@@ -102,7 +102,7 @@ class DirichletSet(C.Structure):
 
 class NewtonOpts(C.Structure):
     _fields_ = [("minItr", C.c_int), ("maxItr", C.c_int), ("tol", C.c_double), ("precision", C.c_int),
-                ("outletFace", C.c_int), ("outletH", C.c_double)]
+                ("outletFace", C.c_int), ("outletH", C.c_double), ("reuse_tangent", C.c_int)]
 
 
 def genalpha_first_order(rho_inf: float):
@@ -511,7 +511,7 @@ class PipeFluidSolver:
 
     def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, sD=50, mItr=100, relTol=1e-8, absTol=1e-17,
                  newton_min=3, newton_max=3, newton_tol=1e-11, precision=SVGPU_FP64, rowPtr=None, colPtr=None,
-                 ls_type=LS_TYPE_GMRES, rcr=None):
+                 ls_type=LS_TYPE_GMRES, rcr=None, reuse_tangent=False):
         """rcr: None for a traction-free outlet, or dict(Rp, C, Rd, Pd, Xo) for a coupled
         RCR outlet (linear-solver face 2)."""
         self.mesh = mesh
@@ -533,7 +533,7 @@ class PipeFluidSolver:
                                 self.props.dt, 0.0)
         self.dir_nodes, self.dir_prof = dirichlet_nodes(mesh)
         self.ctx.set_dirichlet(self.dir_nodes)
-        self.opts = NewtonOpts(newton_min, newton_max, newton_tol, precision, FACE_OUTLET, 0.0)
+        self.opts = NewtonOpts(newton_min, newton_max, newton_tol, precision, FACE_OUTLET, 0.0, int(reuse_tangent))
         z = lambda: np.zeros((nNo, 4))  # noqa: E731
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.norms = [0.0, 0.0]

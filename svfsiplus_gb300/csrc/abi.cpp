@@ -671,13 +671,20 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
 // from the FP32 diagonal, Val32 scaled in place, R scaled and solved in the FP64
 // defect-correction loop, R <- W X.
 int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
-                       const double* res = nullptr) {
+                       const double* res = nullptr, bool reuse = false) {
   auto t0 = std::chrono::steady_clock::now();
   const long n = 4L * ctx->nNo;
   int rc = ensure_krylov(ctx, n, ctx->sD);
   if (rc) return rc;
   KrylovWork& kw = ctx->kw;
   phase_mark(ctx, PH_PRECOND);
+  if (reuse) {
+    // the tangent of an earlier Newton iteration: Val32, W and the multilevel hierarchy
+    // are already scaled and set up; only the new residual is scaled
+    launch_vmul(ctx->stream, n, kw.Wc.p, R);
+    ctx->launches++;
+    if ((rc = setup_coupled(ctx, 4, incL, res, kw.Wc.p))) return rc;
+  } else {
   launch_fill(ctx->stream, n, 1.0, kw.mask.p);
   ctx->launches++;
   for (int f = 0; f < ctx->nFaces; f++) {
@@ -698,6 +705,7 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
     ctx->amg_val0 = Val32;
     phase_mark(ctx, PH_AMG_SETUP);
     if ((rc = amg_numeric(ctx, Val32))) return rc;
+  }
   }
   const bool collect = ctx->gnn && ctx->gnn->collect;
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1582,14 +1590,29 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                         ctx->Yg.p);
     ctx->launches++;
     phase_mark(ctx, PH_ASSEMBLY);
-    if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr, opts->precision)))
+    const bool reuse = opts->reuse_tangent && opts->precision == SVGPU_MIXED && itr > 1;
+    if (reuse) {  // FP64 residual rows only; the tangent of the step's first iteration stays
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, n4 * sizeof(double), ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
+      MeshData& m = *ctx->mesh;
+      const FluidConsts fc = fluid_consts(props);
+      for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+        launch_fluid_residual(ctx->stream, fc, m.color_start[k], m.color_start[k + 1] - m.color_start[k], m.ien.p,
+                              m.boff.p, m.elem_id.p, m.x4.p, ctx->Ag.p, ctx->Yg.p, nullptr, ctx->rowPtr.p, ctx->R.p,
+                              ctx->errflag.p);
+        ctx->launches++;
+      }
+      if ((rc = check_errflag(ctx))) return rc;
+    } else if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr,
+                                           opts->precision))) {
       return rc;
+    }
     if (opts->outletFace >= 0) {
       // the RCR pressure enters as the Neumann value -P on every face node (set_bc_neu_l, set_bc.cpp:1377-1418)
       const double h = rcr ? -ctx->rcr->y : opts->outletH;
       rc = backflow_device(ctx, opts->outletFace, props, h, ctx->Yg.p, ctx->R.p,
                            opts->precision == SVGPU_FP64 ? ctx->Val.p : nullptr,
-                           opts->precision == SVGPU_FP64 ? nullptr : ctx->Val32.p);
+                           (opts->precision == SVGPU_FP64 || reuse) ? nullptr : ctx->Val32.p);
       if (rc) return rc;
     }
     svgpu_ls_stats st;
@@ -1597,7 +1620,7 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     if (opts->precision == SVGPU_FP64)
       rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st, res.data());
     else
-      rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st, res.data());
+      rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st, res.data(), reuse);
     if (rc) return rc;
     phase_mark(ctx, PH_OTHER);
     if (stats) stats[itr - 1] = st;

@@ -448,6 +448,10 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
                            const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
                            const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,
                            double* R, double* Val64, float* Val32, int* errflag);
+// FP64 residual rows only (the mixed path's Newton iterations that keep the tangent)
+void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
+                           const int* elem_id, const double* x4, const double* Ag, const double* Yg, const double* Bf,
+                           const int* rowPtr, double* R, int* errflag);
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
                          const int* fien, const int* inner, const uint8_t* boff, const double* x4,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32);

@@ -413,6 +413,7 @@ __global__ void neu_backflow_kernel(FluidConsts c, double h, int e0, int ne, con
   for (int a = 0; a < 3; a++) {
     double* Ra = R + 4L * nd[a];
     for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
+    if (!Val) continue;  // residual only (the tangent is kept from an earlier iteration)
     const int rowbase = rowPtr[nd[a]];
     for (int b = 0; b < 3; b++) {
       TV blk[16] = {0};
@@ -494,6 +495,14 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
   }
 }
 
+void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
+                           const int* elem_id, const double* x4, const double* Ag, const double* Yg, const double* Bf,
+                           const int* rowPtr, double* R, int* errflag) {
+  if (ne <= 0) return;
+  fluid_p1_kernel<double, double, true, false, false><<<(ne + 127) / 128, 128, 0, s>>>(
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
+}
+
 void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
                                const uint8_t* boff, const int* elem_id, const double* x4, int ld, const double* Ag,
                                const double* Yg, const double* Dg, const double* Bf, const int* rowPtr, double* R,
@@ -508,7 +517,7 @@ void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32) {
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
-  if (Val64)
+  if (Val64 || !Val32)  // both NULL: residual rows only
     neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, 4, Yg, nullptr, rowPtr, R,
                                                      Val64);
   else

@@ -83,3 +83,26 @@ def test_spar_mul_f32_matches_fp64():
     assert rel(KU.cpu().double().numpy(), y64) <= 1e-5
     with pytest.raises(RuntimeError, match="device arrays only"):
         ctx.spar_mul32(K, U, KU)
+
+
+def test_reuse_tangent_reaches_the_reference_solution(golden):
+    """Modified Newton on the mixed path (svgpu_newton_opts.reuse_tangent: the tangent,
+    scaling and multilevel set-up of a step's first iteration kept for its later
+    iterations, the FP64 residual recomputed every iteration) converged to 1e-10 of the
+    step's first residual: velocity and pressure within 1e-6 of the reference's after
+    every step, the same tolerance as the plain path."""
+    g = golden("small")
+    ps = eval(str(g["params"]))
+    m = named_pipe("small")
+    s = api.PipeFluidSolver(m, sD=50, mItr=100, relTol=1e-3, absTol=1e-17, newton_min=3, newton_max=12,
+                            newton_tol=1e-10, precision=api.SVGPU_MIXED, reuse_tangent=True)
+    s.ctx.set_solver_mode(2)
+    for step in range(1, ps["n_steps"] + 1):
+        st = s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"])
+        ref = g[f"Yn_{step}"]
+        ev = float(np.linalg.norm(s.Yn[:, :3] - ref[:, :3]) / np.linalg.norm(ref[:, :3]))
+        ep = float(np.linalg.norm(s.Yn[:, 3] - ref[:, 3]) / np.linalg.norm(ref[:, 3]))
+        print("step", step, "Newton", len(st), "rel", st[-1]["iNorm"] / st[0]["iNorm"], "errors", ev, ep)
+        assert st[-1]["iNorm"] / st[0]["iNorm"] <= 1e-10 * 10
+        assert ev <= 1e-6 and ep <= 1e-6
+    s.ctx.close()
