@@ -2,15 +2,15 @@
 reference solver itself) and against the CPU oracle, through the C ABI.
 
 Tolerances:
-* assembly, FP64: relative 1e-12 on R and Val (BASELINE: assembled residual rel err
-  <= 1e-12).  The GPU sums the Gauss-point integrand in a different order and uses
+* assembly, FP64: relative 1e-12 on R and Val (the target for the assembled
+  residual).  The GPU sums the Gauss-point integrand in a different order and uses
   fused multiply-add, so it is not bitwise.
 * assembly, mixed (FP32 element integrals): relative 2e-5.
 * one GMRES solve: both sides stop at ||r||/||r0|| <= 1e-8 of the preconditioned
   system; the increments agree to 1e-5 relative (the Krylov iterates drift apart
   slowly once the reduction order differs).
 * time stepping: velocity and pressure relative L2 <= 1e-6 after every step
-  (BASELINE: <= 1e-6 after 10 steps).
+  (the target: <= 1e-6 after 10 steps).
 """
 import numpy as np
 import pytest
