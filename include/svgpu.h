@@ -312,10 +312,11 @@ typedef struct {
   int outletFace;            /* face id of the traction-free outlet, -1 for none */
   double outletH;            /* Neumann value on it */
   /* SVGPU_MIXED only, no reference counterpart: 1 assembles the tangent (and the
-   * diagonal scaling and multilevel set-up) at a step's first Newton iteration only and
+   * diagonal scaling and multilevel set-up) at a step's first Newton iteration and
    * reuses it for the later ones, which assemble the FP64 residual alone (a modified
-   * Newton iteration; the residual and the convergence test are unchanged).  0: every
-   * iteration, as the reference. */
+   * Newton iteration; the residual and the convergence test are unchanged); when an
+   * iteration with the kept tangent lowers the preconditioned residual less than
+   * tenfold, the next iteration reassembles it.  0: every iteration, as the reference. */
   int reuse_tangent;
 } svgpu_newton_opts;
 

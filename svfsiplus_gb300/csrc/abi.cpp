@@ -1582,6 +1582,8 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
   std::vector<double> res(ctx->nFaces, 0.0);
   if (rcr) res[ctx->rcr->lsFace] = props->gam * props->dt * ctx->rcr->r;
   int itr = 0;
+  bool refresh = false;  // modified Newton: reassemble the tangent at the next iteration
+  double prev_iN = 0.0;
   for (;;) {
     itr++;
     phase_mark(ctx, PH_OTHER);
@@ -1590,7 +1592,7 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                         ctx->Yg.p);
     ctx->launches++;
     phase_mark(ctx, PH_ASSEMBLY);
-    const bool reuse = opts->reuse_tangent && opts->precision == SVGPU_MIXED && itr > 1;
+    const bool reuse = opts->reuse_tangent && opts->precision == SVGPU_MIXED && itr > 1 && !refresh;
     if (reuse) {  // FP64 residual rows only; the tangent of the step's first iteration stays
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, n4 * sizeof(double), ctx->stream));
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
@@ -1638,6 +1640,9 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     const bool l1 = itr >= opts->maxItr, l2 = r1 <= opts->tol, l3 = r1 <= opts->tol * *pNorm,
                l4 = itr >= opts->minItr;
     if (l1 || ((l2 || l3) && l4)) break;
+    // a kept tangent serves while every iteration lowers the residual at least tenfold
+    refresh = reuse && iN > 0.1 * prev_iN;
+    prev_iN = iN;
   }
   if (rcr) ctx->rcr->xo = ctx->rcr->xn;  // cplBC.xo = cplBC.xn at the end of the step (main.cpp:758)
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, ctx->An.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
