@@ -657,13 +657,10 @@ def main():
     ap.add_argument("--mesh-cg-tol", type=float, default=1e-3, help="--fsi: relative tolerance of the mesh CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
-    ap.add_argument("--krylov-dim", type=int, default=None, help="(F)GMRES restart length of every solve")
     ap.add_argument("--reuse-tangent", type=int, default=None,
                     help="1: mixed paths keep the tangent of a step's first Newton iteration (modified Newton)")
     args = ap.parse_args()
-    global LIN_REL_TOL, REUSE_TANGENT, KRYLOV_DIM
-    if args.krylov_dim is not None:
-        KRYLOV_DIM = args.krylov_dim
+    global LIN_REL_TOL, REUSE_TANGENT
     if args.lin_rel_tol is not None:
         LIN_REL_TOL = args.lin_rel_tol
     if args.reuse_tangent is not None:

@@ -508,34 +508,6 @@ __global__ void scale_val32_kernel(long nnz, const int* __restrict__ blkRow, con
   Val[t] = (float)(((double)Val[t] * W[4L * blkRow[k] + r]) * W[4L * colPtr[k] + c]);
 }
 
-// L2 cache policies of the block SpMVs: the matrix is read once per product and goes
-// first when L2 needs room; the gathered vector x is read ~15 times per product (once
-// per block of its column) and should stay.
-__device__ __forceinline__ uint64_t l2_evict_first_policy() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_evict_last_policy() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float4 ld_f4_policy(const float* p, uint64_t pol) {
-  float4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ float4 ld_f4_keep(const float* p, uint64_t pol) {
-  float4 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "l"(p), "l"(pol));
-  return v;
-}
-
 // y = K x, FP32 matrix and vectors, FP32 accumulation; 4 threads per block row, one
 // 128-bit load of the block row and one of x per block.
 __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __restrict__ rowPtr,
@@ -549,7 +521,6 @@ __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __re
   const int r = (int)(t & 3);
   if (row >= nNo) return;
   const int s = rowPtr[row], e = rowPtr[row + 1];
-  const uint64_t pol_stream = l2_evict_first_policy(), pol_keep = l2_evict_last_policy();
   float acc = 0.f;
   int k = s;
   for (; k + 3 < e; k += 4) {  // four blocks per step, loads first (see spmv4_f64_kernel)
@@ -558,9 +529,9 @@ __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __re
 #pragma unroll
     for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
 #pragma unroll
-    for (int u = 0; u < 4; u++) v[u] = ld_f4_policy(Val + 16L * (k + u) + 4 * r, pol_stream);
+    for (int u = 0; u < 4; u++) v[u] = __ldcs(reinterpret_cast<const float4*>(Val + 16L * (k + u) + 4 * r));
 #pragma unroll
-    for (int u = 0; u < 4; u++) xv[u] = ld_f4_keep(x + 4L * c[u], pol_keep);
+    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       acc = fmaf(v[u].x, xv[u].x, acc);
@@ -571,8 +542,8 @@ __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __re
   }
   for (; k < e; k++) {
     const int col = __ldg(colPtr + k);
-    const float4 v = ld_f4_policy(Val + 16L * k + 4 * r, pol_stream);
-    const float4 xv = ld_f4_keep(x + 4L * col, pol_keep);
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
+    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
     acc = fmaf(v.x, xv.x, acc);
     acc = fmaf(v.y, xv.y, acc);
     acc = fmaf(v.z, xv.z, acc);
