@@ -582,7 +582,13 @@ def run_fsi(args):
                    "timed": k >= args.warmup}
             steps.append(rec)
         timed = [r["s"] for r in steps if r["timed"]]
-        out[path] = {"s_per_step": float(np.mean(timed)), "steps": steps}
+        # phases of one more step (CUDA events at phase boundaries, outside the timed steps)
+        s.ctx.phase_timing(True)
+        s.ctx.phase_times()
+        s.step(15.0, 5.0, 1.0)
+        phases = {k: round(v[0], 2) for k, v in s.ctx.phase_times().items() if v[1]}
+        s.ctx.phase_timing(False)
+        out[path] = {"s_per_step": float(np.mean(timed)), "steps": steps, "phases_ms_one_step": phases}
         fields[path] = (s.Yn.copy(), s.Dn.copy())
         solid = np.zeros(mesh.nNo, bool)
         solid[s.solid_nodes] = True

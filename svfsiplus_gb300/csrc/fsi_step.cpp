@@ -141,7 +141,19 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
                                   opts->dimKry[0]);
   LsSettings ls_mesh = ls_settings(opts->lsType[1], opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
                                    opts->dimKry[1]);
-  const LsSettings saved{ctx->lsType, ctx->relTol, ctx->absTol, ctx->mItr, ctx->sD};
+  // the context's own settings come back on every way out of this function
+  struct Restore {
+    svgpu_ctx* ctx;
+    LsSettings saved;
+    ~Restore() {
+      ctx->lsType = saved.lsType;
+      ctx->relTol = saved.relTol;
+      ctx->absTol = saved.absTol;
+      ctx->mItr = saved.mItr;
+      ctx->sD = saved.sD;
+      ctx->zero_null_rows = false;
+    }
+  } restore{ctx, {ctx->lsType, ctx->relTol, ctx->absTol, ctx->mItr, ctx->sD}};
   ctx->lsType = ls_fsi.lsType;
   ctx->relTol = ls_fsi.relTol;
   ctx->absTol = ls_fsi.absTol;
@@ -222,12 +234,6 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     // both equations are coupled: the next one in turn (pic.cpp:292-318)
     cEq = (cEq + 1) % 2;
   }
-  ctx->lsType = saved.lsType;
-  ctx->relTol = saved.relTol;
-  ctx->absTol = saved.absTol;
-  ctx->mItr = saved.mItr;
-  ctx->sD = saved.sD;
-  ctx->zero_null_rows = false;
   if (rc) return rc;
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, w.An.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, w.Yn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
