@@ -542,6 +542,46 @@ def run_sweep(args):
                           "steps": steps}), flush=True)
 
 
+def run_config1(args):
+    """The CPU-runnable case of the reference's settings: the 50k-tet pipe, 10 time steps,
+    3 Newton iterations each, GMRES(50) + diagonal preconditioner to relative 1e-8, FP64
+    -- timed on the GPU through the C ABI, its fields after step 10 against the
+    reference's own (tests/golden/ref_pipe50k.npz, made by the compiled reference, whose
+    log holds its single-core CPU time for the same run); and the same steps on the
+    mixed multilevel path."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ref_pipe50k.npz"))
+    ps = eval(str(g["params"]))
+    ref_line = str(g["log"]).strip().splitlines()[-1].split()
+    ref_cpu_s = float(ref_line[ref_line.index("wall_s") + 1])
+    mesh = named_pipe("pipe50k")
+    out = {"workload": "pipe50k", "tets": mesh.nEl, "nodes": mesh.nNo, "steps": ps["n_steps"],
+           "reference_cpu_s": ref_cpu_s, "reference_cpu_note": "the compiled reference, 1 rank on 1 x86 core, "
+           "when its fixture was made (same settings and steps)"}
+    for path, prec, mode in (("fp64_gmres_diag", api.SVGPU_FP64, -1), ("mixed_multilevel", api.SVGPU_MIXED, 2)):
+        s = api.PipeFluidSolver(mesh, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
+                                absTol=ps["ls_abs_tol"], newton_min=ps["newton_min"], newton_max=ps["newton_max"],
+                                newton_tol=ps["newton_tol"], precision=prec)
+        if mode >= 0:
+            s.ctx.set_solver_mode(mode)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        its = 0
+        for _ in range(ps["n_steps"]):
+            its += sum(q["itr"] for q in s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"]))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        ref = g[f"Yn_{ps['n_steps']}"]
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        out[path] = {"s_total": round(dt, 4), "krylov_iters": its, "speedup_vs_reference_cpu": round(ref_cpu_s / dt, 1),
+                     "velocity_rel_l2": rel(s.Yn[:, :3], ref[:, :3]), "pressure_rel_l2": rel(s.Yn[:, 3], ref[:, 3])}
+        s.ctx.close()
+    print(json.dumps({"config1": out}), flush=True)
+
+
 def run_fsi(args):
     """The coupled ALE FSI pipe (lumen + 1 mm neo-Hookean wall, linear-elastic mesh
     motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s): s per time step through the C ABI
@@ -660,6 +700,7 @@ def main():
                     help="study: ';'-separated multilevel options 'omega,coarse_sweeps,coarsest_nodes[,pre_sweeps]'")
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
+    ap.add_argument("--config1", action="store_true", help="the 50k-tet pipe at the reference's settings, 10 steps")
     ap.add_argument("--mesh-cg-tol", type=float, default=1e-3, help="--fsi: relative tolerance of the mesh CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
@@ -681,6 +722,8 @@ def main():
         run_study(args)
     elif args.fsi:
         run_fsi(args)
+    elif args.config1:
+        run_config1(args)
     elif args.sweep:
         run_sweep(args)
     else:

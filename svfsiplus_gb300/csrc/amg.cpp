@@ -21,6 +21,14 @@ int amg_build(svgpu_ctx* ctx) {
   std::vector<int> rowPtr = ctx->h_rowPtr, colPtr = ctx->h_colPtr;
   int n = ctx->nNo;
   int rc;
+  // node labels for the aggregation: solid-domain nodes (svgpu_mesh_domains) apart
+  std::vector<int> label, clabel;
+  const bool labelled = ctx->mesh && ctx->mesh->n_solid_nodes > 0;
+  if (labelled) {
+    std::vector<uint8_t> sn;
+    if ((rc = to_host(ctx, sn, ctx->mesh->solid_node.p, (size_t)n))) return rc;
+    label.assign(sn.begin(), sn.end());
+  }
   for (int l = 0; l < kMaxLevels; l++) {
     st->lv.emplace_back();
     AmgLevel& L = st->lv.back();
@@ -44,7 +52,7 @@ int amg_build(svgpu_ctx* ctx) {
     }
     if (n <= ctx->ml_coarsest || l == kMaxLevels - 1) break;
     std::vector<int> agg;
-    const int nc = aggregate_nodes(n, rowPtr, colPtr, agg);
+    const int nc = aggregate_nodes(n, rowPtr, colPtr, agg, labelled ? &label : nullptr, &clabel);
     if (nc >= n || nc < 1) break;
     std::vector<int> cRow, cCol, sumPtr, sumIdx;
     coarse_pattern(n, nc, rowPtr, colPtr, agg, cRow, cCol, sumPtr, sumIdx);
@@ -70,6 +78,7 @@ int amg_build(svgpu_ctx* ctx) {
     }
     rowPtr.swap(cRow);
     colPtr.swap(cCol);
+    label.swap(clabel);
     n = nc;
   }
   AmgLevel& C = st->lv.back();

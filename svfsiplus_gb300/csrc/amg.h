@@ -42,7 +42,8 @@ struct AmgState {
   bool gnn_smoother = false;    // pre-smooth on level 0 with the learned network
 };
 
-int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg);
+int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg,
+                    const std::vector<int>* label = nullptr, std::vector<int>* clabel = nullptr);
 void coarse_pattern(int n, int nc, const std::vector<int>& rowPtr, const std::vector<int>& colPtr,
                     const std::vector<int>& agg, std::vector<int>& cRow, std::vector<int>& cCol,
                     std::vector<int>& sumPtr, std::vector<int>& sumIdx);

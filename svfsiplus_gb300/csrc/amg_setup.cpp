@@ -15,28 +15,45 @@ namespace svgpu {
 // Greedy aggregation (Vanek, Mandel & Brezina 1996, phases 1-3 without strength
 // filtering): root nodes whose neighbourhood is untouched form an aggregate with all
 // their neighbours; left-over nodes join a neighbouring aggregate; the rest stand alone.
-int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg) {
+// With labels (one per node), only neighbours of the root's label take part: the
+// fluid-only and the solid nodes of the FSI equation, whose rows have different scales
+// and physics, never share an aggregate.  clabel receives the aggregates' labels.
+int aggregate_nodes(int n, const std::vector<int>& rowPtr, const std::vector<int>& colPtr, std::vector<int>& agg,
+                    const std::vector<int>* label, std::vector<int>* clabel) {
+  auto same = [&](int i, int j) { return !label || (*label)[i] == (*label)[j]; };
   agg.assign(n, -1);
   int na = 0;
+  std::vector<int> root;
   for (int i = 0; i < n; i++) {
     bool free_nbhd = true;
-    for (int k = rowPtr[i]; k < rowPtr[i + 1] && free_nbhd; k++) free_nbhd = agg[colPtr[k]] < 0;
+    for (int k = rowPtr[i]; k < rowPtr[i + 1] && free_nbhd; k++)
+      free_nbhd = !same(i, colPtr[k]) || agg[colPtr[k]] < 0;
     if (!free_nbhd) continue;
-    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++) agg[colPtr[k]] = na;
+    for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++)
+      if (same(i, colPtr[k])) agg[colPtr[k]] = na;
+    root.push_back(i);
     na++;
   }
   std::vector<int> agg2 = agg;
   for (int i = 0; i < n; i++) {
     if (agg[i] >= 0) continue;
     for (int k = rowPtr[i]; k < rowPtr[i + 1]; k++)
-      if (agg[colPtr[k]] >= 0) {
+      if (agg[colPtr[k]] >= 0 && same(i, colPtr[k])) {
         agg2[i] = agg[colPtr[k]];
         break;
       }
   }
   for (int i = 0; i < n; i++)
-    if (agg2[i] < 0) agg2[i] = na++;
+    if (agg2[i] < 0) {
+      agg2[i] = na++;
+      root.push_back(i);
+    }
   agg.swap(agg2);
+  if (clabel) {
+    clabel->assign(na, 0);
+    if (label)
+      for (int c = 0; c < na; c++) (*clabel)[c] = (*label)[root[c]];
+  }
   return na;
 }
 
