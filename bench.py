@@ -596,14 +596,17 @@ def run_fsi(args):
     mesh = named_pipe(name)
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
     out = {"workload": name, "tets": mesh.nEl, "solid_tets": int((mesh.eid == 2).sum()), "nodes": mesh.nNo,
-           "blocks": int(colPtr.size), "mesh_cg_rel_tol": args.mesh_cg_tol}
+           "blocks": int(colPtr.size), "mesh_rel_tol": args.mesh_cg_tol,
+           "mesh_solver_mixed_path": "multilevel FGMRES" if args.mesh_multilevel else "CG + diagonal"}
     fields = {}
     for path in ("multilevel", "plain"):
         mixed = path == "multilevel"
         s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=(1, NEWTON_MAX, NEWTON_TOL),
                               mesh_newton=(1, NEWTON_MAX, NEWTON_TOL),
                               gmres=(LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM), cg=(args.mesh_cg_tol, 1e-17, 5000),
-                              rowPtr=rowPtr, colPtr=colPtr, precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64)
+                              rowPtr=rowPtr, colPtr=colPtr, precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
+                              mesh_gmres=(args.mesh_cg_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM)
+                              if (mixed and args.mesh_multilevel) else None)
         if mixed:
             s.ctx.set_solver_mode(2)
         steps = []
@@ -701,7 +704,10 @@ def main():
     ap.add_argument("--breakdown", default=None, help="write a per-kernel trace summary of one more step here")
     ap.add_argument("--fsi", action="store_true", help="the coupled ALE FSI pipe (default workload fsi5m)")
     ap.add_argument("--config1", action="store_true", help="the 50k-tet pipe at the reference's settings, 10 steps")
-    ap.add_argument("--mesh-cg-tol", type=float, default=1e-3, help="--fsi: relative tolerance of the mesh CG")
+    ap.add_argument("--mesh-cg-tol", type=float, default=1e-3,
+                    help="--fsi: relative tolerance of the mesh equation's solves")
+    ap.add_argument("--mesh-multilevel", type=int, default=1,
+                    help="--fsi: 1 solves the mixed path's mesh equation by the multilevel FGMRES, 0 by CG")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     ap.add_argument("--reuse-tangent", type=int, default=None,

@@ -362,9 +362,12 @@ typedef struct {
   const int* incL[2];
   int outletFace;   /* mesh face (svgpu_face_create) of the lumen outlet, -1 for none */
   double outletH;   /* Neumann value on it; backflow stabilisation in the moving configuration */
-  /* FSI equation's solve: SVGPU_FP64 (fsils_solve as the reference) or SVGPU_MIXED (an
-   * FP32 copy of the FP64-assembled tangent in the FP64 defect-correction loop, with
-   * the context's solver mode, svgpu_set_solver_mode, as preconditioner; GMRES only) */
+  /* SVGPU_FP64 (fsils_solve as the reference) or SVGPU_MIXED: the FSI equation's solve
+   * takes an FP32 copy of the FP64-assembled tangent in the FP64 defect-correction loop,
+   * with the context's solver mode (svgpu_set_solver_mode) as preconditioner (GMRES
+   * only); a mesh equation set to GMRES is solved the same way, its dof-3 system padded
+   * to 4x4 blocks (a fourth unknown with a unit diagonal), in a solver context of its
+   * own on the same stream.  A mesh equation set to CG keeps the reference's FP64 CG. */
   int precision;
 } svgpu_fsi_opts;
 

@@ -605,7 +605,9 @@ class PipeFsiSolver:
 
     def __init__(self, mesh: _mesh.PipeMesh, props=None, device=0, newton=(3, 3, 1e-11), mesh_newton=(3, 3, 1e-11),
                  gmres=(1e-10, 1e-17, 100, 50), cg=(1e-10, 1e-17, 2000), rowPtr=None, colPtr=None,
-                 precision=SVGPU_FP64):
+                 precision=SVGPU_FP64, mesh_gmres=None):
+        """mesh_gmres (relTol, absTol, restarts, Krylov dimension): solve the mesh equation
+        by GMRES instead of CG (with precision SVGPU_MIXED: the mixed multilevel FGMRES)."""
         if mesh.eid is None:
             raise ValueError("PipeFsiSolver needs an FSI pipe (mesh.make_pipe with nrs > 0)")
         self.mesh = mesh
@@ -630,10 +632,15 @@ class PipeFsiSolver:
         self.opts = FsiOpts()
         for q, (mn, mx, tol) in enumerate((newton, mesh_newton)):
             self.opts.minItr[q], self.opts.maxItr[q], self.opts.tol[q] = mn, mx, tol
-        self.opts.lsType[0], self.opts.lsType[1] = LS_TYPE_GMRES, LS_TYPE_CG
+        self.opts.lsType[0] = LS_TYPE_GMRES
         self.opts.relTol[0], self.opts.absTol[0], self.opts.lsMaxItr[0], self.opts.dimKry[0] = gmres
-        self.opts.relTol[1], self.opts.absTol[1], self.opts.lsMaxItr[1] = cg
-        self.opts.dimKry[1] = -1
+        if mesh_gmres:
+            self.opts.lsType[1] = LS_TYPE_GMRES
+            self.opts.relTol[1], self.opts.absTol[1], self.opts.lsMaxItr[1], self.opts.dimKry[1] = mesh_gmres
+        else:
+            self.opts.lsType[1] = LS_TYPE_CG
+            self.opts.relTol[1], self.opts.absTol[1], self.opts.lsMaxItr[1] = cg
+            self.opts.dimKry[1] = -1
         self._incl = FSI_INCL
         self.opts.incL[0] = self._incl[0].ctypes.data
         self.opts.incL[1] = self._incl[1].ctypes.data

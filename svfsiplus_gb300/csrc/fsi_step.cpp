@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <utility>
 
 #include "internal.h"
@@ -65,6 +66,53 @@ int upload_dir(svgpu_ctx* ctx, const svgpu_dirichlet_set* d, DevBuf<int>& nodes,
   if ((rc = to_device(ctx, nodes, h.data(), h.size()))) return rc;
   if ((rc = to_device(ctx, Y, d->Y, 3L * d->n))) return rc;
   return to_device(ctx, A, d->A, 3L * d->n);
+}
+
+// The mesh equation's own context for its mixed-precision multilevel solve: the same
+// block pattern, linear-solver faces, multilevel options and solid-node labels as the
+// parent, GMRES settings of the mesh equation, the parent's stream.
+int mesh_context(svgpu_ctx* ctx, const svgpu_fsi_opts* opts, FsiWork& w) {
+  int rc;
+  if (w.mctx) {  // the mesh equation's linear-solver settings of this call
+    svgpu_ctx* m = w.mctx.get();
+    if ((rc = svgpu_ls_create(m, SVGPU_LS_GMRES, opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
+                              opts->dimKry[1])))
+      return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
+    m->learned_mode = ctx->learned_mode == 0 ? 0 : 2;
+    return SVGPU_OK;
+  }
+  svgpu_ctx* m = nullptr;
+  rc = svgpu_create(&m, ctx->device);
+  if (rc) return set_err(ctx, rc, "fsi_step: cannot create the mesh equation's solver context");
+  w.mctx.reset(m);
+  svgpu_set_stream(m, ctx->stream);
+  if ((rc = svgpu_lhs_create(m, ctx->nNo, ctx->nNo, ctx->nnz, nullptr, ctx->h_rowPtr.data(), ctx->h_colPtr.data(),
+                             ctx->nFaces)))
+    return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
+  for (int f = 0; f < ctx->nFaces; f++) {
+    const LsFace& fa = ctx->faces[f];
+    if (!fa.created) continue;
+    if ((rc = svgpu_bc_create(m, f, fa.nNo, fa.dof, fa.bGrp, fa.glob.data(), fa.val.data())))
+      return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
+  }
+  if ((rc = svgpu_ls_create(m, SVGPU_LS_GMRES, opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
+                            opts->dimKry[1])))
+    return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
+  m->learned_mode = ctx->learned_mode == 0 ? 0 : 2;
+  m->ml_omega = ctx->ml_omega;
+  m->ml_coarse_sweeps = ctx->ml_coarse_sweeps;
+  m->ml_coarsest = ctx->ml_coarsest;
+  m->ml_pre_sweeps = ctx->ml_pre_sweeps;
+  auto md = std::make_unique<MeshData>();  // only the node labels of the aggregation
+  md->nNo = ctx->nNo;
+  md->n_solid_nodes = ctx->mesh->n_solid_nodes;
+  SVGPU_CUDA(ctx, md->solid_node.resize(ctx->nNo));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(md->solid_node.p, ctx->mesh->solid_node.p, ctx->nNo, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+  m->mesh = std::move(md);
+  SVGPU_CUDA(ctx, m->R.resize(4L * ctx->nNo));
+  SVGPU_CUDA(ctx, m->Val32.resize((size_t)16 * ctx->nnz));
+  return SVGPU_OK;
 }
 
 }  // namespace
@@ -209,10 +257,28 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
       rc = svgpu_construct_mesh(ctx, props->mesh_E, props->mesh_nu, props->mesh_rho, dt, am[1], af[1], beta[1], 7, 4,
                                 w.Ag.p, w.Dg.p, w.Do.p, w.R3.p, w.Val9.p);
       if (rc) break;
-      swap_in(ctx, ls_mesh, w.kw_mesh);
-      rc = solve_fp64(ctx, 3, w.R3.p, w.Val9.p, opts->incL[1], &st);
-      swap_in(ctx, ls_mesh, w.kw_mesh);
-      if (rc) break;
+      if (mixed && opts->lsType[1] == SVGPU_LS_GMRES) {
+        // mixed precision with the multilevel FGMRES, on the system padded to 4x4 blocks
+        if ((rc = mesh_context(ctx, opts, w))) break;
+        svgpu_ctx* mc = w.mctx.get();
+        launch_pad_mesh_system(ctx->stream, nNo, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, w.Val9.p, w.R3.p,
+                               mc->Val32.p, mc->R.p);
+        ctx->launches += 2;
+        const long long l0 = mc->launches;
+        rc = solve_mixed(mc, mc->R.p, mc->Val32.p, opts->incL[1], &st);
+        ctx->launches += mc->launches - l0;
+        if (rc) {
+          rc = set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + mc->err);
+          break;
+        }
+        launch_unpad_vec(ctx->stream, nNo, mc->R.p, w.R3.p);
+        ctx->launches++;
+      } else {
+        swap_in(ctx, ls_mesh, w.kw_mesh);
+        rc = solve_fp64(ctx, 3, w.R3.p, w.Val9.p, opts->incL[1], &st);
+        swap_in(ctx, ls_mesh, w.kw_mesh);
+        if (rc) break;
+      }
       phase_mark(ctx, PH_OTHER);
       launch_mesh_correct(ctx->stream, nNo, gam[1] * dt, beta[1] * dt * dt, w.R3.p, w.An.p, w.Yn.p, w.Dn.p);
       ctx->launches++;

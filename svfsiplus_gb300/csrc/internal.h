@@ -131,7 +131,14 @@ struct AmgState;
 // Work of the coupled FSI time step (fsi_step.cpp): the 7-row state arrays, the mesh
 // equation's system and its own Krylov work (swapped into ctx->kw while it solves, so
 // that the captured FSI and mesh solver graphs both stay valid).
+struct CtxDeleter {
+  void operator()(svgpu_ctx* c) const { svgpu_destroy(c); }
+};
+
 struct FsiWork {
+  // the mesh equation's mixed-precision multilevel solve runs in a context of its own
+  // (its own Krylov work, hierarchy and captured cycles) on the parent's stream
+  std::unique_ptr<svgpu_ctx, CtxDeleter> mctx;
   DevBuf<double> Ao, Yo, Do, An, Yn, Dn, Ag, Yg, Dg;  // (7, nNo)
   DevBuf<double> R3, Val9;                             // mesh equation: (3, nNo), (9, nnz)
   DevBuf<int> dirF, dirM;                              // Dirichlet node lists (FSI rows 0..2, mesh rows 4..6)
@@ -486,6 +493,9 @@ void launch_fsi_correct(cudaStream_t s, int nNo, double c0, double c1, const dou
                         double* An, double* Yn, double* Dn);
 void launch_mesh_correct(cudaStream_t s, int nNo, double c0, double c1, const double* R, double* An, double* Yn,
                          double* Dn);
+void launch_pad_mesh_system(cudaStream_t s, int nNo, long nnz, const int* blkRow, const int* colPtr,
+                            const double* Val9, const double* R3, float* Val16, double* R4);
+void launch_unpad_vec(cudaStream_t s, int nNo, const double* R4, double* R3);
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn);
 void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,

@@ -98,7 +98,50 @@ __global__ void mesh_correct_kernel(int nNo, double c0, double c1, const double*
   }
 }
 
+// The mesh equation's dof-3 system embedded in 4x4 blocks for the mixed-precision
+// multilevel solver: each 3x3 block in the upper left, a fourth unknown that only its
+// own unit diagonal touches (zero right-hand side, zero solution).
+__global__ void pad_mesh_matrix_kernel(long nnz, const int* __restrict__ blkRow, const int* __restrict__ colPtr,
+                                       const double* __restrict__ Val9, float* __restrict__ Val16) {
+  const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  const double* a = Val9 + 9 * k;
+  float4* o = reinterpret_cast<float4*>(Val16 + 16 * k);
+  const float d = blkRow[k] == colPtr[k] ? 1.f : 0.f;
+  o[0] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+  o[1] = make_float4((float)a[3], (float)a[4], (float)a[5], 0.f);
+  o[2] = make_float4((float)a[6], (float)a[7], (float)a[8], 0.f);
+  o[3] = make_float4(0.f, 0.f, 0.f, d);
+}
+
+__global__ void pad_vec_kernel(int nNo, const double* __restrict__ R3, double* __restrict__ R4) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nNo) return;
+  R4[4L * a] = R3[3L * a];
+  R4[4L * a + 1] = R3[3L * a + 1];
+  R4[4L * a + 2] = R3[3L * a + 2];
+  R4[4L * a + 3] = 0.0;
+}
+
+__global__ void unpad_vec_kernel(int nNo, const double* __restrict__ R4, double* __restrict__ R3) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nNo) return;
+  R3[3L * a] = R4[4L * a];
+  R3[3L * a + 1] = R4[4L * a + 1];
+  R3[3L * a + 2] = R4[4L * a + 2];
+}
+
 }  // namespace
+
+void launch_pad_mesh_system(cudaStream_t s, int nNo, long nnz, const int* blkRow, const int* colPtr,
+                            const double* Val9, const double* R3, float* Val16, double* R4) {
+  pad_mesh_matrix_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, Val9, Val16);
+  pad_vec_kernel<<<(nNo + 255) / 256, 256, 0, s>>>(nNo, R3, R4);
+}
+
+void launch_unpad_vec(cudaStream_t s, int nNo, const double* R4, double* R3) {
+  unpad_vec_kernel<<<(nNo + 255) / 256, 256, 0, s>>>(nNo, R4, R3);
+}
 
 void launch_fsi_predict(cudaStream_t s, int nNo, const FsiCoefs& c, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn) {

@@ -177,3 +177,33 @@ def test_gpu_fsi_steps_mixed_multilevel(golden):
         print("step", step, "FSI Krylov its", its, {k: f"{v:.2e}" for k, v in errs.items()})
         assert max(errs.values()) <= 1e-6, errs
     s.ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden):
+    """The mixed path with the mesh equation solved by the multilevel FGMRES as well (its
+    dof-3 system padded to 4x4 blocks in a solver context of its own): per-field
+    relative L2 within 1e-6 of the reference's fields after every step."""
+    from svfsiplus_gb300 import api
+    g = golden("fsi_run_small")
+    ps = _run_params(g)
+    m = named_pipe("fsi_small")
+    p = api.fsi_props(ps["rho_f"], ps["mu"], ps["backflow_beta"], ps["rho_s"], ps["E"], ps["nu"], ps["dt"],
+                      ps["rho_inf"], ps["mesh_E"], ps["mesh_nu"], ps["mesh_rho"])
+    s = api.PipeFsiSolver(m, p, newton=(3, 3, 1e-11), mesh_newton=(3, 3, 1e-11),
+                          gmres=(ps["ls_rel_tol"], ps["ls_abs_tol"], ps["ls_max_itr"], ps["ls_krylov_dim"]),
+                          precision=api.SVGPU_MIXED, mesh_gmres=(1e-10, 1e-17, 100, 50))
+    s.ctx.set_solver_mode(2)
+    solid = np.zeros(m.nNo, bool)
+    solid[s.solid_nodes] = True
+    for step in (1, 2, 3):
+        st = s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"])
+        assert all(d["suc"] == 1 for _, d in st)
+        Yr, Dr = g[f"Yn_{step}"], g[f"Dn_{step}"]
+        errs = {"velocity": rel(s.Yn[~solid, 0:3], Yr[~solid, 0:3]), "pressure": rel(s.Yn[:, 3], Yr[:, 3]),
+                "solid displacement": rel(s.Dn[solid, 0:3], Dr[solid, 0:3]),
+                "mesh displacement": rel(s.Dn[:, 4:7], Dr[:, 4:7])}
+        mesh_its = [d["itr"] for q, d in st if q == 1]
+        print("step", step, "mesh Krylov its", mesh_its, {k: f"{v:.2e}" for k, v in errs.items()})
+        assert max(errs.values()) <= 1e-6, errs
+    s.ctx.close()
