@@ -410,10 +410,41 @@ def run_ours(args):
     phases["krylov_iters"] = sum(q["itr"] for q in pst)
     phases["newton_iters"] = len(pst)
 
+    # the learned path (the network trained online on the solver's own pairs, then the
+    # initial guess of every multilevel FGMRES solve, rejected when it does not lower the
+    # FP64 residual) from the same state: two steps collecting pairs, 100 Adam steps, two
+    # timed steps
+    learned = None
+    if args.compare_plain and mode == 2:
+        s.ctx.close()
+        torch.cuda.empty_cache()
+        sl, _ = make_solver(api, mesh, rowPtr, colPtr, "learned", local)
+        sl.Ao[:], sl.Yo[:], sl.time, sl.norms = (state_after_timed[0], state_after_timed[1], state_after_timed[2],
+                                                 state_after_timed[3])
+        sl.ctx.set_solver_mode(2)
+        for _ in range(2):
+            sl.step(U_MEAN, U_AMP, U_FREQ)
+            loss = sl.ctx.gnn_train(50, 1e-3)
+        sl.ctx.set_solver_mode(4)
+        rej0 = sl.ctx.learned_rejects
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        lst = [sl.step(U_MEAN, U_AMP, U_FREQ) for _ in range(2)]
+        torch.cuda.synchronize()
+        tl = (time.perf_counter() - tl) / 2
+        learned = {"s_per_step": tl, "newton_iters": [len(q) for q in lst],
+                   "krylov_iters": [[r["itr"] for r in q] for q in lst],
+                   "final_over_first_residual": [q[-1]["iNorm"] / q[0]["iNorm"] for q in lst],
+                   "training_loss": loss, "learned_guesses_rejected": sl.ctx.learned_rejects - rej0,
+                   "note": "mode 4 after two collecting steps and 100 Adam steps, two steps through the C ABI"}
+        sl.ctx.close()
+        torch.cuda.empty_cache()
+
     # the plain FP64 GPU path (the reference's method) from the same state, one step
     plain = None
     if args.compare_plain and mode >= 0:
-        s.ctx.close()
+        if learned is None:
+            s.ctx.close()
         torch.cuda.empty_cache()
         sp, _ = make_solver(api, mesh, rowPtr, colPtr, "plain", local)
         sp.Ao[:], sp.Yo[:], sp.time, sp.norms = state_after_timed[0], state_after_timed[1], state_after_timed[2], state_after_timed[3]
@@ -447,6 +478,7 @@ def run_ours(args):
         "newton_iters": newton, "newton_final_over_first": conv,
         "learned_rejects_after_timed": rejects if mode in (3, 4) else None,
         "plain_gpu": plain,
+        "learned_gpu": learned,
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
         "gpu_launches": launches,
