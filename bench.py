@@ -12,20 +12,27 @@ to 1e-6 of its value at the step's first iteration. There are at most 8 Newton i
 Each linear solve is inexact (relative tolerance 1e-2), as in inexact Newton.
 
 Paths (--path):
-  multilevel -- the headline: mixed precision (FP32 tangent/Krylov basis, FP64 residual
+  learned    -- the headline: mixed precision (FP32 tangent/Krylov basis, FP64 residual
                 and defect correction) with FGMRES(50) preconditioned by an aggregation
-                multilevel V-cycle (solver mode 2); the tangent of a step's first Newton
-                iteration serves its later iterations (modified Newton; the FP64 residual
-                is assembled every iteration);
-  learned    -- the same with the learned network as the initial guess of every solve
-                (mode 4), trained online on the solver's own pairs during the warm-up
-                steps;
-  learned-smoother -- the network also as finest-level pre-smoother (mode 3);
+                multilevel V-cycle, started from the learned initial guess (solver mode
+                4): the minimal-residual combination of the previous time step's
+                increment of the same Newton iteration and the network's correction of
+                it (the correction is used at a Newton iteration only while the solves
+                with it need fewer Krylov iterations than those without).  The network
+                is trained online (Adam, lr 1e-3) on the solver's own
+                (residual, prior, increment) triples during the warm-up steps.  The
+                tangent of a step's first Newton iteration serves its later iterations
+                (modified Newton; the FP64 residual is assembled every iteration);
+  history    -- the same initial guess without the network (mode 5);
+  multilevel -- the same solver with a zero initial guess (mode 2);
+  learned-smoother -- the network as finest-level pre-smoother (mode 3);
   mixed      -- mixed precision, GMRES(50) + diagonal preconditioner (mode 0);
   plain      -- FP64, GMRES(50) + diagonal preconditioner: the reference's method.
 
-The default run times the headline path, and runs the plain FP64 GPU path beside it
-from the same state for comparison (`plain_gpu`).
+The default run times the headline path; from the state after its timed steps it then
+times the history and multilevel paths on the same context (`history_gpu`,
+`multilevel_gpu`: the learned part left out step by step) and the plain FP64 GPU path
+(`plain_gpu`).
 
 Our arm prints one JSON line:
   value    -- s per time step, device-resident state, CUDA events on the library's
@@ -68,7 +75,8 @@ KRYLOV_DIM = 50
 # it every iteration as the reference does (the plain path always does)
 REUSE_TANGENT = True
 MAX_RESTARTS = 40
-PATH_MODES = {"multilevel": 2, "learned": 4, "learned-smoother": 3, "mixed": 0, "plain": -1}
+PATH_MODES = {"learned": 4, "history": 5, "multilevel": 2, "learned-smoother": 3, "mixed": 0, "plain": -1}
+TRAIN_ITERS, TRAIN_LR = 100, 1e-3  # Adam steps after every warm-up step that stored triples
 U_MEAN, U_AMP, U_FREQ = 10.0, 5.0, 1.0
 
 
@@ -322,6 +330,60 @@ def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newt
     return s, mode
 
 
+def train_online(api, s):
+    """Adam steps on the triples stored so far (none after the first step: it has no
+    history); returns (mean loss before, after) over the stored triples or None."""
+    if api.lib().svgpu_gnn_pair_count(s.ctx._h) == 0:
+        return None
+    e0 = s.ctx.gnn_eval()
+    s.ctx.gnn_train(TRAIN_ITERS, TRAIN_LR)
+    return (e0, s.ctx.gnn_eval())
+
+
+def device_stepper(api, s):
+    """One time step on device-resident state (Ao/Yo/Do copied to the GPU once)."""
+    import torch
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    st_ = {"Ao": dev(s.Ao), "Yo": dev(s.Yo), "Do": dev(s.Do)}
+    st_.update(An=torch.empty_like(st_["Ao"]), Yn=torch.empty_like(st_["Yo"]), Dn=torch.empty_like(st_["Do"]))
+
+    def dev_step():
+        s.time += s.props.dt
+        dirY, dirA = api.inflow(s.dir_prof, s.time, U_MEAN, U_AMP, U_FREQ)
+        st = s.ctx.fluid_step(s.props, s.opts, dev(dirY), dev(dirA), st_["Ao"], st_["Yo"], st_["Do"], st_["An"],
+                              st_["Yn"], st_["Dn"], s.norms)
+        st_["Ao"].copy_(st_["An"])
+        st_["Yo"].copy_(st_["Yn"])
+        return st
+    return dev_step, st_
+
+
+def ablation_arm(api, mesh, rowPtr, colPtr, path, local, stream, warmup, steps):
+    """The same workload, warm-up and timed steps (CUDA events, device-resident state)
+    on another solver path, from rest: the learned part left out."""
+    import torch
+    s, mode = make_solver(api, mesh, rowPtr, colPtr, path, local)
+    api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
+    dev_step, _ = device_stepper(api, s)
+    for _ in range(warmup):
+        dev_step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stats = [dev_step() for _ in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    res = {"s_per_step": ev0.elapsed_time(ev1) / 1e3 / steps, "path": path, "solver_mode": mode,
+           "newton_iters": [len(q) for q in stats],
+           "krylov_iters_per_step": [sum(r["itr"] for r in q) for q in stats],
+           "krylov_iters": [[r["itr"] for r in q] for q in stats],
+           "x0_rel": [[round(r["x0_rel"], 4) for r in q] for q in stats] if mode == 5 else None,
+           "note": "same warm-up and timed steps from rest, device-resident state, CUDA events"}
+    s.ctx.close()
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_ours(args):
     import torch
     from svfsiplus_gb300 import api
@@ -343,24 +405,16 @@ def run_ours(args):
     api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
     setup_s = time.time() - t0
     nNo = mesh.nNo
-    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
-    dAo, dYo, dDo = dev(s.Ao), dev(s.Yo), dev(s.Do)
-    dAn, dYn, dDn = torch.empty_like(dAo), torch.empty_like(dYo), torch.empty_like(dDo)
+    dev_step, dstate = device_stepper(api, s)
+    dAo, dYo = dstate["Ao"], dstate["Yo"]
 
-    def dev_step():
-        s.time += s.props.dt
-        dirY, dirA = api.inflow(s.dir_prof, s.time, U_MEAN, U_AMP, U_FREQ)
-        st = s.ctx.fluid_step(s.props, s.opts, dev(dirY), dev(dirA), dAo, dYo, dDo, dAn, dYn, dDn, s.norms)
-        dAo.copy_(dAn)
-        dYo.copy_(dYn)
-        return st
-
-    warm_stats = []
+    warm_stats, train_log = [], []
     for k in range(args.warmup):
         warm_stats.append(dev_step())
-        if mode in (3, 4):  # online training on the pairs of the warm-up steps, then learned mode
-            s.ctx.gnn_train(50, 1e-3)
+        if mode in (3, 4):  # online training on the triples of the warm-up steps, then learned mode
+            train_log.append(train_online(api, s))
             if k == args.warmup - 1:
+                s.ctx.gnn_collect(False)
                 s.ctx.set_solver_mode(mode)
     torch.cuda.synchronize()
     if world > 1:
@@ -377,7 +431,7 @@ def run_ours(args):
         torch.cuda.synchronize()
     dev_ms = ev0.elapsed_time(ev1)
     launches = s.ctx.kernel_launches - launches0
-    rejects = s.ctx.learned_rejects
+    guesses = s.ctx.guess_stats
     if world > 1:
         t = torch.tensor([dev_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -410,41 +464,10 @@ def run_ours(args):
     phases["krylov_iters"] = sum(q["itr"] for q in pst)
     phases["newton_iters"] = len(pst)
 
-    # the learned path (the network trained online on the solver's own pairs, then the
-    # initial guess of every multilevel FGMRES solve, rejected when it does not lower the
-    # FP64 residual) from the same state: two steps collecting pairs, 100 Adam steps, two
-    # timed steps
-    learned = None
-    if args.compare_plain and mode == 2:
-        s.ctx.close()
-        torch.cuda.empty_cache()
-        sl, _ = make_solver(api, mesh, rowPtr, colPtr, "learned", local)
-        sl.Ao[:], sl.Yo[:], sl.time, sl.norms = (state_after_timed[0], state_after_timed[1], state_after_timed[2],
-                                                 state_after_timed[3])
-        sl.ctx.set_solver_mode(2)
-        for _ in range(2):
-            sl.step(U_MEAN, U_AMP, U_FREQ)
-            loss = sl.ctx.gnn_train(50, 1e-3)
-        sl.ctx.set_solver_mode(4)
-        rej0 = sl.ctx.learned_rejects
-        torch.cuda.synchronize()
-        tl = time.perf_counter()
-        lst = [sl.step(U_MEAN, U_AMP, U_FREQ) for _ in range(2)]
-        torch.cuda.synchronize()
-        tl = (time.perf_counter() - tl) / 2
-        learned = {"s_per_step": tl, "newton_iters": [len(q) for q in lst],
-                   "krylov_iters": [[r["itr"] for r in q] for q in lst],
-                   "final_over_first_residual": [q[-1]["iNorm"] / q[0]["iNorm"] for q in lst],
-                   "training_loss": loss, "learned_guesses_rejected": sl.ctx.learned_rejects - rej0,
-                   "note": "mode 4 after two collecting steps and 100 Adam steps, two steps through the C ABI"}
-        sl.ctx.close()
-        torch.cuda.empty_cache()
-
     # the plain FP64 GPU path (the reference's method) from the same state, one step
     plain = None
     if args.compare_plain and mode >= 0:
-        if learned is None:
-            s.ctx.close()
+        s.ctx.close()
         torch.cuda.empty_cache()
         sp, _ = make_solver(api, mesh, rowPtr, colPtr, "plain", local)
         sp.Ao[:], sp.Yo[:], sp.time, sp.norms = state_after_timed[0], state_after_timed[1], state_after_timed[2], state_after_timed[3]
@@ -458,6 +481,14 @@ def run_ours(args):
                  "final_over_first_residual": pst[-1]["iNorm"] / pst[0]["iNorm"],
                  "note": "one step from the state after the timed steps; Newton capped at %d iterations" % NEWTON_MAX}
         sp.ctx.close()
+        torch.cuda.empty_cache()
+
+    # the learned part left out step by step: the history guess without the network
+    # (mode 5), then no initial guess (mode 2), each on the same warm-up and timed steps
+    ablation = {}
+    if args.compare_plain and mode == 4:
+        for name, p in (("history_gpu", "history"), ("multilevel_gpu", "multilevel")):
+            ablation[name] = ablation_arm(api, mesh, rowPtr, colPtr, p, local, stream, args.warmup, args.steps)
 
     its = [q["itr"] for st in stats for q in st]
     newton = [len(st) for st in stats]
@@ -476,9 +507,12 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (Val is 1.3-2.6 GB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "krylov_iters_per_step": [sum(q["itr"] for q in st) for st in stats], "krylov_iters": its,
         "newton_iters": newton, "newton_final_over_first": conv,
-        "learned_rejects_after_timed": rejects if mode in (3, 4) else None,
+        "initial_guesses": dict(zip(("tried", "rejected", "with_network"), guesses)) if mode in (4, 5) else None,
+        "x0_rel_timed": [[round(q["x0_rel"], 4) for q in st] for st in stats] if mode in (4, 5) else None,
+        "training": {"adam_steps_per_warmup_step": TRAIN_ITERS, "lr": TRAIN_LR,
+                     "loss_before_after": train_log} if mode in (3, 4) else None,
         "plain_gpu": plain,
-        "learned_gpu": learned,
+        **ablation,
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
         "gpu_launches": launches,
@@ -525,7 +559,7 @@ def run_study(args):
                               "phases_ms": {k: round(v[0], 2) for k, v in s.ctx.phase_times().items() if v[1]}}),
                   flush=True)
             if mode in (3, 4) and k < 2:
-                s.ctx.gnn_train(50, 1e-3)
+                train_online(api, s)
         s.ctx.close()
 
 
@@ -724,7 +758,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="svgpu", choices=["svgpu", "reference"])
-    ap.add_argument("--path", default="multilevel", choices=list(PATH_MODES))
+    ap.add_argument("--path", default="learned", choices=list(PATH_MODES))
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")

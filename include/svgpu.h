@@ -46,6 +46,9 @@ typedef struct {
   int itr;           /* Krylov iterations incl. restarts (RI.itr) */
   int suc;           /* converged (RI.suc) */
   double true_rel;   /* ||R - K dX|| / ||R|| of the unpreconditioned FP64 system (not in the reference) */
+  double x0_rel;     /* FP64 residual of a tried initial guess over iNorm, 0 if none was tried (modes 4, 5) */
+  int x0_kept;       /* the initial guess was kept */
+  int pad_;
 } svgpu_ls_stats;
 
 /* Physical properties of a fluid domain: dmnType::prop (ComMod.h:431-462) with a
@@ -252,32 +255,61 @@ int svgpu_write_vtu(svgpu_ctx* ctx, const char* path, int nNo, const double* x, 
 
 /* ---- learned preconditioner (no counterpart in the reference) ------------------------
  * A 3-layer message-passing network on the CSR graph (hidden width 64, BF16 weights,
- * FP32 accumulation) trained online on (residual, increment) pairs of the
- * Jacobi-scaled system that the mixed-precision solves store.  node_features (4,nNo):
- * scaled coordinates and wall distance.  Parameters are an FP32 vector of
- * svgpu_gnn_param_count() floats. */
+ * FP32 accumulation) trained online on (residual, prior, increment) triples of the
+ * Jacobi-scaled system that the mixed-precision solves store.  The prior is the
+ * previous time step's increment of the same Newton iteration times its
+ * minimal-residual coefficient (null where there is none); the network predicts a
+ * correction: M(r, p) = p + s_o * net(r / s_r, p / s_p, features), s_o = s_p with a
+ * prior, s_r = ||r|| / sqrt(n) without.  node_features (4,nNo): scaled coordinates and
+ * wall distance.  Parameters are an FP32 vector of svgpu_gnn_param_count() floats. */
 int svgpu_gnn_param_count(void);
 int svgpu_gnn_create(svgpu_ctx* ctx, const float* node_features, unsigned long long seed);
 int svgpu_gnn_get_params(svgpu_ctx* ctx, float* params, int n);
 int svgpu_gnn_set_params(svgpu_ctx* ctx, const float* params, int n);
-/* z = M(r) for a (4,nNo) vector */
-int svgpu_gnn_apply(svgpu_ctx* ctx, const double* r, double* z);
-/* relative squared error of M(r) against x and its gradient (params floats) */
-int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* x, double* loss, float* grad);
-/* store a training pair; switch storing of the solver's own pairs on or off */
-int svgpu_gnn_add_pair(svgpu_ctx* ctx, const double* r, const double* x);
+/* z = M(r, p) - p, the network's correction, for (4,nNo) vectors; p may be null */
+int svgpu_gnn_apply(svgpu_ctx* ctx, const double* r, const double* p, double* z);
+/* relative squared error |p + z - x|^2 / |x|^2 of the correction z = M(r, p) - p,
+ * and its gradient (params floats); p may be null */
+int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* p, const double* x, double* loss,
+                        float* grad);
+/* store a training triple (p may be null); storing of the solver's own triples: 0 off,
+ * 1 every mixed solve, 2 only solves with a prior */
+int svgpu_gnn_add_pair(svgpu_ctx* ctx, const double* r, const double* p, const double* x);
 int svgpu_gnn_collect(svgpu_ctx* ctx, int on);
-/* iters Adam steps (Kingma & Ba) over the stored pairs, learning rate lr; mean loss out */
+/* mean loss of the network over the stored triples (no training) */
+int svgpu_gnn_eval(svgpu_ctx* ctx, double* loss);
+/* the stored triples, oldest first (k = 0 .. count-1), widened to FP64 (p zero where
+ * the triple has no prior) */
+int svgpu_gnn_pair_count(const svgpu_ctx* ctx);
+int svgpu_gnn_get_pair(svgpu_ctx* ctx, int k, double* r, double* p, double* x);
+/* iters Adam steps (Kingma & Ba) over the stored triples, learning rate lr; mean loss out */
 int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
 /* Solver of the mixed-precision path: 0 GMRES + diagonal preconditioner (the
- * reference's method); 1 FGMRES with the network as right preconditioner and initial
- * guess; 2 FGMRES with an aggregation multilevel V-cycle (block-Jacobi smoothing) as
- * right preconditioner; 3 as 2 with the network as finest-level pre-smoother and
- * initial guess; 4 as 2 with the network as initial guess only.  Learned initial
- * guesses and learned cycles that do not lower the FP64 residual are rejected (plain
- * cycles finish the solve). */
+ * reference's method); 1 FGMRES with the network as right preconditioner; 2 FGMRES
+ * with an aggregation multilevel V-cycle (block-Jacobi smoothing) as right
+ * preconditioner; 3 as 2 with the network as finest-level pre-smoother; 4 as 2 with
+ * the learned initial guess: the minimal-residual combination of the previous step's
+ * increment g of the same Newton iteration and the network's correction
+ * M(r, a g) - a g (the network runs where a g alone leaves more than a fifth of the
+ * residual, and at a Newton iteration's slot only while the solves with the correction
+ * needed fewer Krylov iterations on average than those without: each is tried twice,
+ * then the better one is kept and the other retried every eighth visit); 5 as 2 with
+ * the minimal-residual multiple of g alone (no network).
+ * Initial guesses and flexible cycles that do not lower the FP64 residual are rejected
+ * (plain cycles finish the solve). */
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
-/* Options of the multilevel preconditioner (modes 2-4): damping of the block-Jacobi
+/* History of modes 4 and 5: the slot (0..15) whose previous increment the next mixed
+ * solves use and replace; svgpu_fluid_step and svgpu_fsi_step set it to the Newton
+ * iteration for their own solves.  -1 (the default): none.  svgpu_history_clear
+ * forgets every slot.  svgpu_guess_stats: initial guesses tried, rejected, and those
+ * with the network's correction (net_used may be null). */
+int svgpu_history_slot(svgpu_ctx* ctx, int slot);
+int svgpu_history_clear(svgpu_ctx* ctx);
+int svgpu_guess_stats(const svgpu_ctx* ctx, long long* used, long long* rejected, long long* net_used);
+/* An initial guess is kept when its FP64 residual is below accept times the
+ * residual without it (default 1: whenever it lowers the residual). */
+int svgpu_guess_options(svgpu_ctx* ctx, double accept);
+/* Options of the multilevel preconditioner (modes 2-5): damping of the block-Jacobi
  * smoother (default 0.7), block-Jacobi sweeps on a coarsest level too large for the
  * dense inverse (30), the node count at or below which coarsening stops (256), and the
  * finest level's pre-smoothing sweeps (1; 0 leaves it out, post-smoothing stays).  A

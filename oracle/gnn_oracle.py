@@ -2,7 +2,9 @@
 
 A numpy restatement of the message-passing network the GPU kernels implement
 (svfsiplus_gb300/csrc/k_gnn.cu), forward and backward, used to check the GPU loss and
-gradients.  It reproduces the GPU's storage precisions: weights rounded to BF16,
+gradients.  Inputs per node: the residual r / s_r, the prior p / s_p (zero without a
+prior) and 4 static features; the output out is the correction scaled by s_o
+(s_p with a prior, s_r without): M(r, p) = p + s_o * out.  It reproduces the GPU's storage precisions: weights rounded to BF16,
 activations h stored in BF16, the neighbour mean m used in FP32 by the forward pass and
 stored in BF16 for the weight gradient; arithmetic is FP64 here (FP32 on the GPU).
 """
@@ -10,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-H, NIN = 64, 8
+H, NIN = 64, 12
 LAYER = 2 * H * H + H
 OFF_W0, OFF_B0 = 0, NIN * H
 
@@ -55,13 +57,25 @@ def _mean_gather(rowPtr, colPtr, h):
     return s / deg[:, None], deg
 
 
-def forward(p, rowPtr, colPtr, r, stat):
-    """r (nNo,4) FP64 input; stat (nNo,4).  Returns (out_raw (nNo,4), scale s, cache)."""
-    W0, b0, Ws, bs, Wd, bd = unpack(p)
+def scales(r, prior):
+    """(s_r, s_p or None, s_o) of a residual and an optional prior (both as stored)."""
     n = r.size
-    s = np.sqrt(np.sum(r.astype(np.float64) ** 2) / n)
-    s = s if s > 0 else 1.0
-    x = np.concatenate([np.asarray(r, np.float32).astype(np.float64) / s, stat.astype(np.float64)], axis=1)
+    sr = np.sqrt(np.sum(np.asarray(r, np.float64) ** 2) / n)
+    sr = sr if sr > 0 else 1.0
+    if prior is None:
+        return sr, None, sr
+    sp = np.sqrt(np.sum(np.asarray(prior, np.float32).astype(np.float64) ** 2) / n)
+    return (sr, sp, sp) if sp > 0 else (sr, None, sr)
+
+
+def forward(p, rowPtr, colPtr, r, stat, prior=None):
+    """r (nNo,4) FP64 input; prior (nNo,4) or None; stat (nNo,4).
+    Returns (out_raw (nNo,4), output scale s_o, cache)."""
+    W0, b0, Ws, bs, Wd, bd = unpack(p)
+    sr, sp, so = scales(r, prior)
+    pin = np.zeros_like(np.asarray(r, np.float64)) if sp is None else \
+        np.asarray(prior, np.float32).astype(np.float64) / sp
+    x = np.concatenate([np.asarray(r, np.float32).astype(np.float64) / sr, pin, stat.astype(np.float64)], axis=1)
     z0 = x @ W0 + b0
     h = [bf16(np.maximum(z0, 0.0))]
     masks = [z0 > 0]
@@ -73,15 +87,20 @@ def forward(p, rowPtr, colPtr, r, stat):
         ms.append(bf16(m))
         h.append(bf16(h[-1] + np.maximum(z, 0.0)))
     out = h[3] @ Wd + bd
-    return out, s, dict(x=x, h=h, ms=ms, masks=masks)
+    return out, so, dict(x=x, h=h, ms=ms, masks=masks)
 
 
-def loss_grad(p, rowPtr, colPtr, r, xt, stat):
-    """Relative squared error sum|out - xt/s|^2 / sum|xt/s|^2 and its gradient."""
+def loss_grad(p, rowPtr, colPtr, r, xt, stat, prior=None):
+    """Relative squared error sum|out - t|^2 / sum|xt / s_o|^2 with t = (xt - prior) / s_o,
+    and its gradient."""
     W0, b0, Ws, bs, Wd, bd = unpack(p)
-    out, s, c = forward(p, rowPtr, colPtr, r, stat)
-    t = np.asarray(xt, np.float32).astype(np.float64) / s
-    E = np.sum(t * t)
+    out, s, c = forward(p, rowPtr, colPtr, r, stat, prior)
+    xs = np.asarray(xt, np.float32).astype(np.float64)
+    t = xs
+    if prior is not None and scales(r, prior)[1] is not None:
+        t = t - np.asarray(prior, np.float32).astype(np.float64)
+    t = t / s
+    E = np.sum((xs / s) ** 2)
     loss = np.sum((out - t) ** 2) / E
     dout = 2.0 * (out - t) / E
     g = np.zeros(NPARAM)

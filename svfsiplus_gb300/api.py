@@ -48,7 +48,8 @@ def lib():
 
 class LsStats(C.Structure):
     _fields_ = [("iNorm", C.c_double), ("fNorm", C.c_double), ("dB", C.c_double), ("callD", C.c_double),
-                ("itr", C.c_int), ("suc", C.c_int), ("true_rel", C.c_double)]
+                ("itr", C.c_int), ("suc", C.c_int), ("true_rel", C.c_double), ("x0_rel", C.c_double),
+                ("x0_kept", C.c_int), ("pad_", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -276,23 +277,58 @@ class Context:
         p = np.ascontiguousarray(p, dtype=np.float32)
         self._check(lib().svgpu_gnn_set_params(self._h, _ptr(p), int(p.size)), "gnn_set_params")
 
-    def gnn_apply(self, r, z):
-        self._check(lib().svgpu_gnn_apply(self._h, _ptr(r), _ptr(z)), "gnn_apply")
+    def gnn_apply(self, r, z, p=None):
+        """z = the network's correction M(r, p) - p (p: the prior, or None)."""
+        self._check(lib().svgpu_gnn_apply(self._h, _ptr(r), None if p is None else _ptr(np.ascontiguousarray(p)),
+                                          _ptr(z)), "gnn_apply")
 
-    def gnn_loss_grad(self, r, x):
+    def gnn_loss_grad(self, r, x, p=None):
         n = lib().svgpu_gnn_param_count()
         g = np.zeros(n, dtype=np.float32)
         loss = C.c_double()
-        self._check(lib().svgpu_gnn_loss_grad(self._h, _ptr(np.ascontiguousarray(r)), _ptr(np.ascontiguousarray(x)),
-                                              C.byref(loss), _ptr(g)), "gnn_loss_grad")
+        pp = None if p is None else _ptr(np.ascontiguousarray(p))
+        self._check(lib().svgpu_gnn_loss_grad(self._h, _ptr(np.ascontiguousarray(r)), pp,
+                                              _ptr(np.ascontiguousarray(x)), C.byref(loss), _ptr(g)),
+                    "gnn_loss_grad")
         return loss.value, g
 
-    def gnn_add_pair(self, r, x):
-        self._check(lib().svgpu_gnn_add_pair(self._h, _ptr(np.ascontiguousarray(r)), _ptr(np.ascontiguousarray(x))),
-                    "gnn_add_pair")
+    def gnn_add_pair(self, r, x, p=None):
+        pp = None if p is None else _ptr(np.ascontiguousarray(p))
+        self._check(lib().svgpu_gnn_add_pair(self._h, _ptr(np.ascontiguousarray(r)), pp,
+                                             _ptr(np.ascontiguousarray(x))), "gnn_add_pair")
 
     def gnn_collect(self, on=True):
-        self._check(lib().svgpu_gnn_collect(self._h, int(bool(on))), "gnn_collect")
+        """Store the solves' triples: False off, True every solve, 2 only solves with a prior."""
+        self._check(lib().svgpu_gnn_collect(self._h, int(on)), "gnn_collect")
+
+    def gnn_eval(self):
+        """Mean loss of the network over the stored triples."""
+        loss = C.c_double()
+        self._check(lib().svgpu_gnn_eval(self._h, C.byref(loss)), "gnn_eval")
+        return loss.value
+
+    def gnn_pairs(self):
+        """The stored (residual, prior, increment) triples of the scaled system, oldest
+        first; the prior is zero where a triple has none."""
+        out = []
+        for k in range(lib().svgpu_gnn_pair_count(self._h)):
+            r, p, x = (np.zeros((self.nNo, 4)) for _ in range(3))
+            self._check(lib().svgpu_gnn_get_pair(self._h, k, _ptr(r), _ptr(p), _ptr(x)), "gnn_get_pair")
+            out.append((r, p, x))
+        return out
+
+    def history_slot(self, slot):
+        self._check(lib().svgpu_history_slot(self._h, int(slot)), "history_slot")
+
+    def history_clear(self):
+        self._check(lib().svgpu_history_clear(self._h), "history_clear")
+
+    @property
+    def guess_stats(self):
+        """(initial guesses tried, rejected, with the network's correction) of modes 4 and 5."""
+        u, r, k = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self._check(lib().svgpu_guess_stats(self._h, C.byref(u), C.byref(r), C.byref(k)), "guess_stats")
+        return u.value, r.value, k.value
 
     def gnn_train(self, iters, lr=1e-3):
         loss = C.c_double()
@@ -301,7 +337,9 @@ class Context:
 
     def set_solver_mode(self, mode):
         """0 plain GMRES + diagonal, 1 learned FGMRES, 2 multilevel FGMRES, 3 multilevel
-        with the learned smoother (modes 1-3 act on the mixed-precision path)."""
+        with the learned smoother, 4 multilevel with the learned initial guess (previous
+        step's increment + network correction), 5 multilevel with the previous step's
+        increment alone as initial guess (modes 1-5 act on the mixed-precision path)."""
         self._check(lib().svgpu_set_solver_mode(self._h, int(mode)), "set_solver_mode")
 
     def multilevel_options(self, omega=0.7, coarse_sweeps=30, coarsest_nodes=256, pre_sweeps=1):
@@ -559,11 +597,11 @@ class PipeFluidSolver:
         if self.has_rcr:
             self.ctx.rcr_set_state(float(r["xo"][0]))
 
-    def enable_learning(self, seed=1):
-        """Create the learned preconditioner and start collecting (residual, increment)
-        pairs from the plain solves."""
+    def enable_learning(self, seed=1, collect=2):
+        """Create the learned preconditioner and start collecting the solves'
+        (residual, prior, increment) triples (2: only solves with a prior)."""
         self.ctx.gnn_create(pipe_node_features(self.mesh), seed)
-        self.ctx.gnn_collect(True)
+        self.ctx.gnn_collect(collect)
 
     def step(self, u_mean=10.0, u_amp=0.0, freq=1.0):
         self.time += self.props.dt

@@ -422,7 +422,7 @@ void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
 }
 
 // Flexible cycle with the learned right preconditioner: z_i = M(u_i) (the network on
-// the unit-norm basis vector, scale 1/sqrt(n)), u_{i+1} = K z_i, then the same
+// the unit-norm basis vector without a prior, scale 1/sqrt(n)), u_{i+1} = K z_i, then the same
 // Gram-Schmidt and Givens steps; the solution is updated from the z_i (FGMRES).
 void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
   KrylovWork& kw = ctx->kw;
@@ -435,7 +435,7 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
     float* zi = kw.zbasis.p + (long)i * n;
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_PRECOND);
     if (ctx->learned_mode == 1)
-      gnn_apply_device(ctx, ui, nullptr, ctx->gnn->scal.p + 4, zi, nullptr, kw.flags.p);
+      gnn_apply_device(ctx, ui, nullptr, nullptr, ctx->gnn->scal.p + 8, zi, nullptr, kw.flags.p);
     else
       amg_vcycle(ctx, ui, zi, kw.flags.p);
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_SPMV);
@@ -543,6 +543,117 @@ int run_cycle32(svgpu_ctx* ctx, const float* Val32) {
   return SVGPU_OK;
 }
 
+// Initial guess of solver modes 4 and 5 from the previous time step's increment g of
+// the same Newton iteration (history slot ctx->hist_slot): the minimal-residual
+// multiple a1 g (mode 5), or with the learned network (mode 4) the minimal-residual
+// combination of g and the network's correction d = M(r, a1 g) - a1 g (the network
+// runs where a1 g alone leaves more than a fifth of the residual, and at a slot only
+// while the solves that used it needed fewer Krylov iterations on average than those
+// that did not).  The guess is
+// kept only if it lowers the FP64 residual (below guess_accept times the residual
+// without it); X and r64 of the solve start from it.
+// With pair collection on, the prior a1 g of the stored pair is formed here as well.
+int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& nrm, svgpu_ls_stats* st) {
+  KrylovWork& kw = ctx->kw;
+  const int mode = ctx->learned_mode;
+  const long n = 4L * ctx->nNo;
+  const int slot = ctx->hist_slot;
+  const bool collect = ctx->gnn && ctx->gnn->collect;
+  const bool guess = mode == 4 || mode == 5;
+  const bool net = mode == 4 && ctx->gnn;
+  if (!(guess || collect) || slot < 0 || slot >= kHistSlots) return SVGPU_OK;
+  if (!ctx->guess) ctx->guess.reset(new GuessWork());
+  GuessWork& gw = *ctx->guess;
+  if (!gw.valid[slot] || gw.hist[slot].n != (size_t)n) return SVGPU_OK;
+  SVGPU_CUDA(ctx, gw.g.resize(n));
+  SVGPU_CUDA(ctx, gw.w1.resize(n));
+  SVGPU_CUDA(ctx, gw.part.resize(2 * (size_t)ctx->sm_count * 3));
+  SVGPU_CUDA(ctx, gw.coef.resize(8));
+  const cudaStream_t s = ctx->stream;
+  int rc = SVGPU_OK;
+  phase_mark(ctx, PH_GUESS);
+  launch_f32_to_f64(s, n, gw.hist[slot].p, gw.g.p);
+  launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.g.p, gw.w1.p);
+  add_coupled(ctx, 4, gw.g.p, gw.w1.p, nullptr);
+  {
+    const double* a[2] = {Rs, gw.w1.p};
+    const double* b[2] = {gw.w1.p, gw.w1.p};
+    launch_guess_dots(s, n, 2, a, b, gw.part.p, ctx->sm_count);
+  }
+  launch_guess_coef1(s, ctx->sm_count, gw.part.p, gw.coef.p);
+  ctx->launches += 4;
+  if (ctx->gnn && (net || collect)) {
+    SVGPU_CUDA(ctx, gw.prior.resize(n));
+    launch_scale_f32(s, n, gw.coef.p, gw.hist[slot].p, gw.prior.p);
+    ctx->launches++;
+    gw.prior_valid = true;
+  }
+  if (!guess) return SVGPU_OK;
+  const double* d = nullptr;
+  const double* w2 = nullptr;
+  bool use_net = false;
+  gw.last_slot = -1;
+  gw.last_arm = -1;
+  if (net) {
+    // the network only where the previous increment alone leaves more than a fifth of
+    // the residual: ||r - a1 K g||^2 / ||r||^2 = 1 - (r.Kg)^2 / (Kg.Kg ||r||^2)
+    double c[2];
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(c, gw.coef.p + 2, sizeof(c), cudaMemcpyDeviceToHost, s));
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(s));
+    const double left1 = c[1] > 0.0 ? 1.0 - c[0] * c[0] / (c[1] * nrm * nrm) : 1.0;
+    if (!(left1 <= 0.04)) {
+      // the arm with the fewer Krylov iterations on average at this slot; each arm is
+      // tried twice first, and the other arm again every eighth visit (the flow drifts)
+      const int* v = gw.arm_visits[slot];
+      const int visit = gw.visits[slot]++;
+      int arm;
+      if (v[0] < 2 || v[1] < 2)
+        arm = v[1] <= v[0] ? 1 : 0;
+      else
+        arm = gw.arm_its[slot][1] < gw.arm_its[slot][0] ? 1 : 0;
+      if (v[0] >= 2 && v[1] >= 2 && visit % 8 == 7) arm = 1 - arm;
+      use_net = arm == 1;
+      gw.last_slot = slot;
+      gw.last_arm = arm;
+    }
+  }
+  if (use_net) {
+    GnnState& g = *ctx->gnn;
+    SVGPU_CUDA(ctx, gw.d.resize(n));
+    SVGPU_CUDA(ctx, gw.w2.resize(n));
+    gnn_scales(s, n, nullptr, Rs, gw.prior.p, g.nrmp.p, g.scal.p, ctx->sm_count);
+    ctx->launches += 2;
+    if ((rc = gnn_apply_device(ctx, nullptr, Rs, gw.prior.p, g.scal.p, nullptr, gw.d.p, nullptr))) return rc;
+    launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.d.p, gw.w2.p);
+    add_coupled(ctx, 4, gw.d.p, gw.w2.p, nullptr);
+    const double* a[3] = {Rs, gw.w1.p, gw.w2.p};
+    const double* b[3] = {gw.w2.p, gw.w2.p, gw.w2.p};
+    launch_guess_dots(s, n, 3, a, b, gw.part.p, ctx->sm_count);
+    launch_guess_coef2(s, ctx->sm_count, gw.part.p, gw.coef.p);
+    ctx->launches += 3;
+    d = gw.d.p;
+    w2 = gw.w2.p;
+  }
+  launch_guess_apply(s, n, gw.coef.p, gw.g.p, d, gw.w1.p, w2, Rs, kw.X.p, kw.r64.p);
+  ctx->launches++;
+  const double n0 = device_norm(ctx, n, kw.r64.p, rc);
+  if (rc) return rc;
+  gw.used++;
+  if (use_net) gw.net_used++;
+  st->x0_rel = n0 / nrm;
+  st->x0_kept = n0 < ctx->guess_accept * nrm;
+  if (!st->x0_kept) {  // no (or too small a) drop of the FP64 residual: start from zero
+    gw.rejected++;
+    ctx->learned_rejects++;
+    SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), s));
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  } else {
+    nrm = n0;
+    st->fNorm = nrm;
+  }
+  return SVGPU_OK;
+}
+
 // Restarted GMRES with FP32 Arnoldi cycles inside an FP64 defect-correction loop:
 // every restart starts from the residual Rs - K X recomputed with FP64 arithmetic and
 // X accumulates in FP64; the test for convergence uses that FP64 residual.  Same
@@ -553,10 +664,9 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   const int sD = kw.sD;
   int rc = SVGPU_OK;
   const int mode = ctx->learned_mode;
-  const bool use_gnn = (mode == 1 || mode == 3 || mode == 4) && ctx->gnn != nullptr;
-  bool learned = mode != 0 && (use_gnn || mode == 2);  // flexible cycles
-  // mode 4 runs the cycles of mode 2 (multilevel V-cycle); only its initial guess is learned
-  const int cycle_kind = 1 + (mode == 4 ? 2 : mode);
+  bool learned = mode != 0;  // flexible cycles
+  // modes 4 and 5 run the cycles of mode 2 (multilevel V-cycle); only their initial guess differs
+  const int cycle_kind = 1 + (mode >= 4 ? 2 : mode);
   if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
   st->suc = 0;
   double nrm = device_norm(ctx, n, Rs, rc);
@@ -564,8 +674,11 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   st->iNorm = nrm;
   st->fNorm = nrm;
   st->itr = 0;
+  st->x0_rel = 0.0;
+  st->x0_kept = 0;
   const double eps = std::max(ctx->absTol, ctx->relTol * nrm);
   SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
+  if (ctx->guess) ctx->guess->prior_valid = false;
   if (st->iNorm <= ctx->absTol) {
     st->dB = 0.0;
     SVGPU_CUDA(ctx, cudaMemcpyAsync(Xout, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -575,35 +688,16 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.scal.p, &eps, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemsetAsync(kw.hess.p, 0, kw.hess.bytes(), ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  if (learned && !use_gnn) {
+  if (learned) {
     if (!kw.zbasis.p || kw.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, kw.zbasis.resize((size_t)n * sD));
   }
-  if (use_gnn) {
-    GnnState& g = *ctx->gnn;
-    if (!kw.zbasis.p || kw.zbasis.n != (size_t)n * sD) SVGPU_CUDA(ctx, kw.zbasis.resize((size_t)n * sD));
-    const double sv = 1.0 / std::sqrt((double)n);  // scale of a unit-norm basis vector
-    SVGPU_CUDA(ctx, cudaMemcpyAsync(g.scal.p + 4, &sv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    // learned initial guess X0 = M(Rs), kept only if it lowers the FP64 residual
-    phase_mark(ctx, PH_GUESS);
-    launch_norm2(ctx->stream, n, Rs, g.nrmp.p, g.scal.p + 1, ctx->sm_count);
-    gnn_scale(ctx->stream, g.scal.p + 1, n, g.scal.p);
-    ctx->launches += 3;
-    if ((rc = gnn_apply_device(ctx, nullptr, Rs, g.scal.p, nullptr, kw.X.p, nullptr))) return rc;
-    launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
-    add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
-    launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
-    ctx->launches += 2;
-    const double n0 = device_norm(ctx, n, kw.r64.p, rc);
-    if (rc) return rc;
-    if (!(n0 < nrm)) {
-      ctx->learned_rejects++;
-      SVGPU_CUDA(ctx, cudaMemsetAsync(kw.X.p, 0, n * sizeof(double), ctx->stream));
-      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, Rs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-    } else {
-      nrm = n0;
-      st->fNorm = nrm;
-    }
+  if ((mode == 1 || mode == 3) && ctx->gnn) {
+    // the network on unit-norm Krylov vectors: {s_r, 1/s_p, s_o} = {1/sqrt(n), 0, 1/sqrt(n)}
+    const double sv = 1.0 / std::sqrt((double)n);
+    const double sc[3] = {sv, 0.0, sv};
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(ctx->gnn->scal.p + 8, sc, sizeof(sc), cudaMemcpyHostToDevice, ctx->stream));
   }
+  if ((rc = history_guess(ctx, Val32, Rs, nrm, st))) return rc;
   double dB = nrm;
   double before = nrm;  // FP64 residual norm when the current cycle started
   for (int l = 0; l < ctx->mItr; l++) {
@@ -709,6 +803,10 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   }
   const bool collect = ctx->gnn && ctx->gnn->collect;
   if (collect) SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.rsave.p, R, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  // the increments of this solve become the history of the next time step's solve
+  // with the same slot (modes 4 and 5, or while pairs are collected)
+  const int slot = ctx->hist_slot;
+  const bool keep = slot >= 0 && slot < kHistSlots && (ctx->learned_mode >= 4 || collect);
   rc = gmres_mixed(ctx, Val32, R, R, st);
   ctx->coupled.clear();
   ctx->coupled_sig = 0;
@@ -718,12 +816,29 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
     launch_zero_null_rows(ctx->stream, ctx->nNo, ctx->rowPtr.p, Val32, R);
     ctx->launches++;
   }
-  if (collect && st->iNorm > ctx->absTol) {
+  if (ctx->guess && ctx->guess->last_arm >= 0) {
+    // the Krylov iterations this solve needed, for the slot's arm statistics
+    GuessWork& gw = *ctx->guess;
+    const int sl = gw.last_slot, a = gw.last_arm;
+    gw.arm_its[sl][a] = gw.arm_visits[sl][a] == 0 ? st->itr : 0.6 * gw.arm_its[sl][a] + 0.4 * st->itr;
+    gw.arm_visits[sl][a]++;
+    gw.last_arm = -1;
+  }
+  const float* prior = ctx->guess && ctx->guess->prior_valid ? ctx->guess->prior.p : nullptr;
+  if (collect && st->iNorm > ctx->absTol && (ctx->gnn->collect == 1 || prior)) {
     // exact pair (K X, X) of the preconditioned system: K X = Rs - r, with r the final
     // FP64 residual the solve left in kw.r64 (valid whether or not it converged)
     launch_sub(ctx->stream, n, kw.rsave.p, kw.r64.p, kw.rbak.p);
     ctx->launches++;
-    if ((rc = gnn_store_pair(ctx, kw.rbak.p, R))) return rc;
+    if ((rc = gnn_store_pair(ctx, kw.rbak.p, prior, R))) return rc;
+  }
+  if (keep) {
+    if (!ctx->guess) ctx->guess.reset(new GuessWork());
+    GuessWork& gw = *ctx->guess;
+    SVGPU_CUDA(ctx, gw.hist[slot].resize(n));
+    gnn_f64_to_f32(ctx->stream, n, R, gw.hist[slot].p);
+    ctx->launches++;
+    gw.valid[slot] = true;
   }
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches++;
@@ -1619,10 +1734,15 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     }
     svgpu_ls_stats st;
     std::memset(&st, 0, sizeof(st));
-    if (opts->precision == SVGPU_FP64)
+    if (opts->precision == SVGPU_FP64) {
       rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st, res.data());
-    else
+    } else {
+      // the Newton iteration is the history slot of the solve (initial guesses of modes 4, 5)
+      const int slot0 = ctx->hist_slot;
+      ctx->hist_slot = itr - 1 < kHistSlots ? itr - 1 : -1;
       rc = solve_device_mixed(ctx, ctx->R.p, ctx->Val32.p, incL.data(), &st, res.data(), reuse);
+      ctx->hist_slot = slot0;
+    }
     if (rc) return rc;
     phase_mark(ctx, PH_OTHER);
     if (stats) stats[itr - 1] = st;

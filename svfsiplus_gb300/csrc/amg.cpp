@@ -185,7 +185,7 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, 
   const bool pre = !fine || st.pre_sweeps > 0 || (st.gnn_smoother && ctx->gnn);
   if (pre) {
     if (l == 0 && st.gnn_smoother && ctx->gnn)
-      gnn_apply_device(ctx, b, nullptr, ctx->gnn->scal.p + 4, x, nullptr, fl);
+      gnn_apply_device(ctx, b, nullptr, nullptr, ctx->gnn->scal.p + 8, x, nullptr, fl);
     else
       amg_jacobi(s, A.n, st.omega, A.dinv.p, b, nullptr, x, 0, fl);
     if (marks) phase_mark(ctx, PH_VC_SPMV);

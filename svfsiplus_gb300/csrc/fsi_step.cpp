@@ -242,7 +242,10 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
       if (mixed) {
         launch_f64_to_f32(ctx->stream, (long)16 * ctx->nnz, ctx->Val.p, ctx->Val32.p);
         ctx->launches++;
+        const int slot0 = ctx->hist_slot;  // the equation's Newton iteration is the history slot
+        ctx->hist_slot = itr[0] - 1 < kHistSlots ? itr[0] - 1 : -1;
         rc = solve_mixed(ctx, ctx->R.p, ctx->Val32.p, opts->incL[0], &st);
+        ctx->hist_slot = slot0;
       } else {
         rc = solve_fp64(ctx, 4, ctx->R.p, ctx->Val.p, opts->incL[0], &st);
       }
@@ -265,6 +268,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
                                mc->Val32.p, mc->R.p);
         ctx->launches += 2;
         const long long l0 = mc->launches;
+        mc->hist_slot = itr[1] - 1 < kHistSlots ? itr[1] - 1 : -1;
         rc = solve_mixed(mc, mc->R.p, mc->Val32.p, opts->incL[1], &st);
         ctx->launches += mc->launches - l0;
         if (rc) {

@@ -1,6 +1,6 @@
 // Host side of the learned preconditioner: parameter set-up, inference, the
-// loss/gradient of one (residual, increment) pair, online training with Adam on the
-// pairs the solver stores, and the C-ABI entry points (include/svgpu.h).
+// loss/gradient of one (residual, prior, increment) triple, online training with Adam
+// on the triples the solver stores, and the C-ABI entry points (include/svgpu.h).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -14,9 +14,10 @@ namespace {
 __nv_bfloat16* bfp(DevBuf<uint16_t>& b) { return reinterpret_cast<__nv_bfloat16*>(b.p); }
 
 // Seeded initial weights: uniform(-a, a) with a = sqrt(6 / fan_in) (He) for the hidden
-// layers, a small scale for the decoder so the untrained network starts near zero.
+// layers; the decoder starts at zero, so the untrained network adds no correction to
+// its prior (and its first Adam steps move only the decoder).
 std::vector<float> init_params(int np, unsigned long long seed) {
-  const int H = 64, NIN = 8;
+  const int H = 64, NIN = 12;
   std::vector<float> p(np, 0.f);
   uint64_t st = seed ? seed : 0x9e3779b97f4a7c15ull;
   auto next = [&]() {  // splitmix64
@@ -36,8 +37,7 @@ std::vector<float> init_params(int np, unsigned long long seed) {
     fill(off, 2 * H * H, std::sqrt(6.0 / (2 * H)) * 0.5);
     off += 2 * H * H + H;
   }
-  fill(off, H * 4, 0.01);
-  return p;
+  return p;  // decoder weights and biases stay zero
 }
 
 int ensure_gnn_buffers(svgpu_ctx* ctx) {
@@ -52,8 +52,10 @@ int ensure_gnn_buffers(svgpu_ctx* ctx) {
   SVGPU_CUDA(ctx, g.in32.resize(4 * nNo));
   SVGPU_CUDA(ctx, g.tgt32.resize(4 * nNo));
   SVGPU_CUDA(ctx, g.lossbuf.resize(2 + 2 * 4 * (size_t)ctx->sm_count + 8));
-  SVGPU_CUDA(ctx, g.scal.resize(8));
-  SVGPU_CUDA(ctx, g.nrmp.resize(2 * (size_t)ctx->sm_count + 16));
+  // scal: [0..2] the scalars of a guess or training evaluation, [8..10] those of the
+  // network applied to unit Krylov vectors (modes 1 and 3)
+  SVGPU_CUDA(ctx, g.scal.resize(16));
+  SVGPU_CUDA(ctx, g.nrmp.resize(4 * (size_t)ctx->sm_count + 16));
   return SVGPU_OK;
 }
 
@@ -74,61 +76,50 @@ void hptrs(GnnState& g, __nv_bfloat16* h[4], __nv_bfloat16* m[4]) {
   }
 }
 
-// s = ||r|| / sqrt(n) of an FP32 or FP64 vector, into g.scal[0]
-int device_scale(svgpu_ctx* ctx, const float* r32, const double* r64) {
+// The scalars {s_r, 1/s_p, s_o} of residual r (FP32 or FP64) and prior p32, into g.scal[0..2]
+void device_scales(svgpu_ctx* ctx, const float* r32, const double* r64, const float* p32) {
   GnnState& g = *ctx->gnn;
-  const long n = 4L * g.nNo;
-  if (r64) {
-    launch_norm2(ctx->stream, n, r64, g.nrmp.p, g.scal.p + 1, ctx->sm_count);
-  } else {
-    // widen into the gradient scratch is not needed: norm of the FP32 copy via FP64 pass
-    DevBuf<double> tmp;
-    SVGPU_CUDA(ctx, tmp.resize(n));
-    launch_f32_to_f64(ctx->stream, n, r32, tmp.p);
-    launch_norm2(ctx->stream, n, tmp.p, g.nrmp.p, g.scal.p + 1, ctx->sm_count);
-    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  }
-  gnn_scale(ctx->stream, g.scal.p + 1, n, g.scal.p);
-  ctx->launches += 3;
-  return SVGPU_OK;
+  gnn_scales(ctx->stream, 4L * g.nNo, r32, r64, p32, g.nrmp.p, g.scal.p, ctx->sm_count);
+  ctx->launches += 2;
 }
 
-// One pair: forward with saved activations, loss and gradient into g.grad.
-int loss_grad_pair(svgpu_ctx* ctx, const float* r32, const float* x32) {
+// One triple: forward with saved activations, loss and gradient into g.grad.
+int loss_grad_pair(svgpu_ctx* ctx, const float* r32, const float* p32, const float* x32) {
   GnnState& g = *ctx->gnn;
   int rc;
   if ((rc = ensure_train_buffers(ctx))) return rc;
-  if ((rc = device_scale(ctx, r32, nullptr))) return rc;
+  device_scales(ctx, r32, nullptr, p32);
   __nv_bfloat16 *h[4], *m[4];
   hptrs(g, h, m);
-  gnn_forward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, nullptr, g.stat.p, g.scal.p, bfp(g.pbf), h, m,
-              g.mask.p, nullptr, nullptr, g.raw.p, ctx->sm_count, nullptr);
-  gnn_backward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, g.stat.p, g.scal.p, bfp(g.pbf), h, m, g.mask.p,
-               g.raw.p, x32, g.dA.p, g.dB.p, g.dC.p, g.part.p, g.lossbuf.p, g.grad.p, ctx->sm_count);
+  gnn_forward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, nullptr, p32, g.stat.p, g.scal.p, bfp(g.pbf),
+              h, m, g.mask.p, nullptr, nullptr, g.raw.p, ctx->sm_count, nullptr);
+  gnn_backward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, p32, g.stat.p, g.scal.p, bfp(g.pbf), h, m,
+               g.mask.p, g.raw.p, x32, g.dA.p, g.dB.p, g.dC.p, g.part.p, g.lossbuf.p, g.grad.p, ctx->sm_count);
   ctx->launches += 5 + 12;
   return SVGPU_OK;
 }
 
 }  // namespace
 
-int gnn_apply_device(svgpu_ctx* ctx, const float* r32, const double* r64, const double* scale, float* out32,
-                     double* out64, const int* flags) {
+int gnn_apply_device(svgpu_ctx* ctx, const float* r32, const double* r64, const float* p32, const double* scale,
+                     float* out32, double* out64, const int* flags) {
   GnnState& g = *ctx->gnn;
   __nv_bfloat16 *h[4], *m[4];
   hptrs(g, h, m);
-  gnn_forward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, r64, g.stat.p, scale, bfp(g.pbf), h, nullptr,
-              nullptr, out32, out64, nullptr, ctx->sm_count, flags);
+  gnn_forward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, r32, r64, p32, g.stat.p, scale, bfp(g.pbf), h,
+              nullptr, nullptr, out32, out64, nullptr, ctx->sm_count, flags);
   ctx->launches += 5;
   return SVGPU_OK;
 }
 
-// Stores (r, x) in FP32 in the ring of training pairs.
-int gnn_store_pair(svgpu_ctx* ctx, const double* r, const double* x) {
+int gnn_store_pair(svgpu_ctx* ctx, const double* r, const float* p, const double* x) {
   GnnState& g = *ctx->gnn;
   const long n = 4L * g.nNo;
   if ((int)g.pair_r.size() < g.max_pairs) {
     g.pair_r.resize(g.max_pairs);
+    g.pair_p.resize(g.max_pairs);
     g.pair_x.resize(g.max_pairs);
+    g.pair_has_p.resize(g.max_pairs, false);
   }
   const int k = g.next_pair;
   SVGPU_CUDA(ctx, g.pair_r[k].resize(n));
@@ -136,6 +127,11 @@ int gnn_store_pair(svgpu_ctx* ctx, const double* r, const double* x) {
   gnn_f64_to_f32(ctx->stream, n, r, g.pair_r[k].p);
   gnn_f64_to_f32(ctx->stream, n, x, g.pair_x[k].p);
   ctx->launches += 2;
+  g.pair_has_p[k] = p != nullptr;
+  if (p) {
+    SVGPU_CUDA(ctx, g.pair_p[k].resize(n));
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(g.pair_p[k].p, p, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   g.next_pair = (k + 1) % g.max_pairs;
   if (g.npairs < g.max_pairs) g.npairs++;
   return SVGPU_OK;
@@ -194,40 +190,55 @@ int svgpu_gnn_set_params(svgpu_ctx* ctx, const float* params, int n) {
   return SVGPU_OK;
 }
 
-int svgpu_gnn_apply(svgpu_ctx* ctx, const double* r, double* z) {
+int svgpu_gnn_apply(svgpu_ctx* ctx, const double* r, const double* p, double* z) {
   if (!ctx || !ctx->gnn) return SVGPU_ESTATE;
   cudaSetDevice(ctx->device);
   if (!r || !z) return SVGPU_EINVAL;
   GnnState& g = *ctx->gnn;
   const long n = 4L * g.nNo;
   int rc;
-  DevBuf<double> rin, zout;
+  DevBuf<double> rin, pin, zout;
+  DevBuf<float> p32;
   const double* rd = r;
   double* zd = z;
   if (!is_device_ptr(r)) { if ((rc = to_device(ctx, rin, r, n))) return rc; rd = rin.p; }
+  if (p) {
+    if ((rc = to_device(ctx, pin, p, n))) return rc;
+    SVGPU_CUDA(ctx, p32.resize(n));
+    gnn_f64_to_f32(ctx->stream, n, pin.p, p32.p);
+    ctx->launches++;
+  }
   const bool dz = is_device_ptr(z);
   if (!dz) { SVGPU_CUDA(ctx, zout.resize(n)); zd = zout.p; }
-  if ((rc = device_scale(ctx, nullptr, rd))) return rc;
-  if ((rc = gnn_apply_device(ctx, nullptr, rd, g.scal.p, nullptr, zd, nullptr))) return rc;
+  device_scales(ctx, nullptr, rd, p32.p);
+  if ((rc = gnn_apply_device(ctx, nullptr, rd, p32.p, g.scal.p, nullptr, zd, nullptr))) return rc;
   if (!dz) SVGPU_CUDA(ctx, cudaMemcpyAsync(z, zd, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
 }
 
-int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* x, double* loss, float* grad) {
+int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* p, const double* x, double* loss,
+                        float* grad) {
   if (!ctx || !ctx->gnn) return SVGPU_ESTATE;
   cudaSetDevice(ctx->device);
   if (!r || !x) return SVGPU_EINVAL;
   GnnState& g = *ctx->gnn;
   const long n = 4L * g.nNo;
   int rc;
-  DevBuf<double> rd, xd;
+  DevBuf<double> rd, pd, xd;
+  DevBuf<float> p32;
   if ((rc = to_device(ctx, rd, r, n))) return rc;
   if ((rc = to_device(ctx, xd, x, n))) return rc;
   gnn_f64_to_f32(ctx->stream, n, rd.p, g.in32.p);
   gnn_f64_to_f32(ctx->stream, n, xd.p, g.tgt32.p);
   ctx->launches += 2;
-  if ((rc = loss_grad_pair(ctx, g.in32.p, g.tgt32.p))) return rc;
+  if (p) {
+    if ((rc = to_device(ctx, pd, p, n))) return rc;
+    SVGPU_CUDA(ctx, p32.resize(n));
+    gnn_f64_to_f32(ctx->stream, n, pd.p, p32.p);
+    ctx->launches++;
+  }
+  if ((rc = loss_grad_pair(ctx, g.in32.p, p32.p, g.tgt32.p))) return rc;
   double lb[2];
   SVGPU_CUDA(ctx, cudaMemcpyAsync(lb, g.lossbuf.p, sizeof(lb), cudaMemcpyDeviceToHost, ctx->stream));
   if (grad) SVGPU_CUDA(ctx, cudaMemcpyAsync(grad, g.grad.p, g.nparam * sizeof(float), cudaMemcpyDefault, ctx->stream));
@@ -236,22 +247,84 @@ int svgpu_gnn_loss_grad(svgpu_ctx* ctx, const double* r, const double* x, double
   return SVGPU_OK;
 }
 
-int svgpu_gnn_add_pair(svgpu_ctx* ctx, const double* r, const double* x) {
+int svgpu_gnn_add_pair(svgpu_ctx* ctx, const double* r, const double* p, const double* x) {
   if (!ctx || !ctx->gnn) return SVGPU_ESTATE;
   cudaSetDevice(ctx->device);
+  if (!r || !x) return SVGPU_EINVAL;
   const long n = 4L * ctx->gnn->nNo;
   int rc;
-  DevBuf<double> rd, xd;
+  DevBuf<double> rd, pd, xd;
+  DevBuf<float> p32;
   if ((rc = to_device(ctx, rd, r, n))) return rc;
   if ((rc = to_device(ctx, xd, x, n))) return rc;
-  if ((rc = gnn_store_pair(ctx, rd.p, xd.p))) return rc;
+  if (p) {
+    if ((rc = to_device(ctx, pd, p, n))) return rc;
+    SVGPU_CUDA(ctx, p32.resize(n));
+    gnn_f64_to_f32(ctx->stream, n, pd.p, p32.p);
+    ctx->launches++;
+  }
+  if ((rc = gnn_store_pair(ctx, rd.p, p32.p, xd.p))) return rc;
+  SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SVGPU_OK;
+}
+
+int svgpu_gnn_pair_count(const svgpu_ctx* ctx) { return ctx && ctx->gnn ? ctx->gnn->npairs : 0; }
+
+int svgpu_gnn_get_pair(svgpu_ctx* ctx, int k, double* r, double* p, double* x) {
+  if (!ctx || !ctx->gnn) return SVGPU_ESTATE;
+  cudaSetDevice(ctx->device);
+  GnnState& g = *ctx->gnn;
+  if (k < 0 || k >= g.npairs) return set_err(ctx, SVGPU_EINVAL, "gnn_get_pair: index out of range");
+  if (!r || !p || !x) return SVGPU_EINVAL;
+  const int slot = (g.next_pair - g.npairs + k + g.max_pairs) % g.max_pairs;  // k = 0: the oldest
+  const long n = 4L * g.nNo;
+  DevBuf<double> w;
+  SVGPU_CUDA(ctx, w.resize(3 * n));
+  launch_f32_to_f64(ctx->stream, n, g.pair_r[slot].p, w.p);
+  launch_f32_to_f64(ctx->stream, n, g.pair_x[slot].p, w.p + n);
+  ctx->launches += 2;
+  if (g.pair_has_p[slot]) {
+    launch_f32_to_f64(ctx->stream, n, g.pair_p[slot].p, w.p + 2 * n);
+    ctx->launches++;
+  } else {
+    SVGPU_CUDA(ctx, cudaMemsetAsync(w.p + 2 * n, 0, n * sizeof(double), ctx->stream));
+  }
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(r, w.p, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(x, w.p + n, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemcpyAsync(p, w.p + 2 * n, n * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SVGPU_OK;
 }
 
 int svgpu_gnn_collect(svgpu_ctx* ctx, int on) {
   if (!ctx || !ctx->gnn) return SVGPU_ESTATE;
-  ctx->gnn->collect = on != 0;
+  if (on < 0 || on > 2) return set_err(ctx, SVGPU_EINVAL, "gnn_collect: 0 off, 1 every solve, 2 solves with a prior");
+  ctx->gnn->collect = on;
+  return SVGPU_OK;
+}
+
+int svgpu_gnn_eval(svgpu_ctx* ctx, double* loss) {
+  if (!ctx || !ctx->gnn || !loss) return SVGPU_ESTATE;
+  cudaSetDevice(ctx->device);
+  GnnState& g = *ctx->gnn;
+  if (g.npairs == 0) return set_err(ctx, SVGPU_ESTATE, "gnn_eval: no training pairs stored");
+  __nv_bfloat16 *h[4], *m[4];
+  hptrs(g, h, m);
+  double acc = 0.0;
+  for (int k = 0; k < g.npairs; k++) {
+    const int slot = (g.next_pair - g.npairs + k + g.max_pairs) % g.max_pairs;
+    const float* p32 = g.pair_has_p[slot] ? g.pair_p[slot].p : nullptr;
+    device_scales(ctx, g.pair_r[slot].p, nullptr, p32);
+    gnn_forward(ctx->stream, g.nNo, ctx->rowPtr.p, ctx->colPtr.p, g.pair_r[slot].p, nullptr, p32, g.stat.p,
+                g.scal.p, bfp(g.pbf), h, nullptr, nullptr, nullptr, nullptr, g.raw.p, ctx->sm_count, nullptr);
+    gnn_loss(ctx->stream, g.nNo, g.raw.p, g.pair_x[slot].p, p32, g.scal.p, g.lossbuf.p, ctx->sm_count);
+    ctx->launches += 7;
+    double lb[2];
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(lb, g.lossbuf.p, sizeof(lb), cudaMemcpyDeviceToHost, ctx->stream));
+    SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    acc += lb[0];
+  }
+  *loss = acc / g.npairs;
   return SVGPU_OK;
 }
 
@@ -264,7 +337,8 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss) {
   double acc = 0.0;
   for (int it = 0; it < iters; it++) {
     const int k = (g.adam_step + it) % g.npairs;
-    if ((rc = loss_grad_pair(ctx, g.pair_r[k].p, g.pair_x[k].p))) return rc;
+    if ((rc = loss_grad_pair(ctx, g.pair_r[k].p, g.pair_has_p[k] ? g.pair_p[k].p : nullptr, g.pair_x[k].p)))
+      return rc;
     gnn_adam(ctx->stream, lr, ++g.adam_step, g.grad.p, g.p32.p, g.adam_m.p, g.adam_v.p, bfp(g.pbf));
     ctx->launches++;
     double lb[2];
@@ -279,7 +353,7 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss) {
 
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode) {
   if (!ctx) return SVGPU_EINVAL;
-  if (mode < 0 || mode > 4) return set_err(ctx, SVGPU_EINVAL, "set_solver_mode: mode must be 0..4");
+  if (mode < 0 || mode > 5) return set_err(ctx, SVGPU_EINVAL, "set_solver_mode: mode must be 0..5");
   if ((mode == 1 || mode == 3 || mode == 4) && !ctx->gnn)
     return set_err(ctx, SVGPU_ESTATE, "set_solver_mode: the learned modes need a network (svgpu_gnn_create)");
   ctx->learned_mode = mode;
@@ -287,5 +361,41 @@ int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode) {
 }
 
 long long svgpu_learned_rejects(const svgpu_ctx* ctx) { return ctx ? ctx->learned_rejects : 0; }
+
+int svgpu_history_slot(svgpu_ctx* ctx, int slot) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (slot < -1 || slot >= kHistSlots)
+    return set_err(ctx, SVGPU_EINVAL, "history_slot: slot must be -1.." + std::to_string(kHistSlots - 1));
+  ctx->hist_slot = slot;
+  return SVGPU_OK;
+}
+
+int svgpu_guess_options(svgpu_ctx* ctx, double accept) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (!(accept > 0.0 && accept <= 1.0)) return set_err(ctx, SVGPU_EINVAL, "guess_options: accept must be in (0, 1]");
+  ctx->guess_accept = accept;
+  return SVGPU_OK;
+}
+
+int svgpu_history_clear(svgpu_ctx* ctx) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (ctx->guess) {
+    GuessWork& gw = *ctx->guess;
+    for (int k = 0; k < kHistSlots; k++) {
+      gw.valid[k] = false;
+      gw.visits[k] = gw.arm_visits[k][0] = gw.arm_visits[k][1] = 0;
+      gw.arm_its[k][0] = gw.arm_its[k][1] = 0.0;
+    }
+  }
+  return SVGPU_OK;
+}
+
+int svgpu_guess_stats(const svgpu_ctx* ctx, long long* used, long long* rejected, long long* net_used) {
+  if (!ctx || !used || !rejected) return SVGPU_EINVAL;
+  *used = ctx->guess ? ctx->guess->used : 0;
+  *rejected = ctx->guess ? ctx->guess->rejected : 0;
+  if (net_used) *net_used = ctx->guess ? ctx->guess->net_used : 0;
+  return SVGPU_OK;
+}
 
 }  // extern "C"

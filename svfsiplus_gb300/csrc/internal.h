@@ -200,6 +200,27 @@ struct PhaseTimer {
   long long intervals[PH_COUNT] = {};
 };
 
+// Previous-step increments per Newton iteration and the work of the initial guess
+// built from them (solver modes 4 and 5).  The increments are those of the scaled
+// system (before the W scaling of the result), in FP32.
+constexpr int kHistSlots = 16;
+struct GuessWork {
+  DevBuf<float> hist[kHistSlots];
+  bool valid[kHistSlots] = {};
+  DevBuf<double> g, w1, d, w2;  // FP64 directions and their products
+  DevBuf<float> prior;          // alpha g in FP32 (the network's prior)
+  DevBuf<double> part, coef;    // dot partials; coef = {a1, a2, r.w1, w1.w1, ...}
+  bool prior_valid = false;     // prior holds the prior of the current solve
+  // Whether the network's correction pays at a slot is learned from the Krylov
+  // iterations of the solves that follow: per slot and arm (0 without, 1 with the
+  // correction) a visit count and an exponential average of the iterations.
+  int arm_visits[kHistSlots][2] = {};
+  double arm_its[kHistSlots][2] = {};
+  int visits[kHistSlots] = {};
+  int last_slot = -1, last_arm = -1;  // the arm the current solve uses
+  long long used = 0, rejected = 0, net_used = 0;
+};
+
 // Learned preconditioner state (k_gnn.cu kernels).
 struct GnnState {
   int nNo = 0;
@@ -214,10 +235,11 @@ struct GnnState {
   DevBuf<float> part;                       // weight-gradient partial sums
   DevBuf<double> lossbuf, scal, nrmp;       // loss / scale scalars, norm partials
   DevBuf<float> zbasis;                     // flexible-GMRES directions Z (sD x 4 nNo)
-  std::vector<DevBuf<float>> pair_r, pair_x;  // training pairs (scaled space)
+  std::vector<DevBuf<float>> pair_r, pair_p, pair_x;  // training pairs (scaled space); pair_p: prior
+  std::vector<bool> pair_has_p;
   int npairs = 0, next_pair = 0, max_pairs = 64;
   int adam_step = 0;
-  bool collect = false;                     // store (residual, increment) pairs from plain solves
+  int collect = 0;  // store the solves' triples: 1 every solve, 2 only solves with a prior
   double last_loss = 0.0;
 };
 
@@ -279,11 +301,18 @@ struct svgpu_ctx {
   std::unique_ptr<struct svgpu::AmgState> amg;
   const float* amg_val0 = nullptr;  // level-0 matrix of the current numeric set-up
   // 0: GMRES + diagonal preconditioner (the reference's method)
-  // 1: FGMRES, right preconditioner = the learned network (+ learned initial guess)
+  // 1: FGMRES, right preconditioner = the learned network
   // 2: FGMRES, right preconditioner = aggregation multilevel V-cycle (block Jacobi)
-  // 3: as 2 with the learned network as the finest-level pre-smoother (+ initial guess)
+  // 3: as 2 with the learned network as the finest-level pre-smoother
+  // 4: as 2 with the learned initial guess (previous-step increment + network correction)
+  // 5: as 2 with the previous-step increment alone as initial guess (no network)
   int learned_mode = 0;
   long long learned_rejects = 0;
+  // history slot of the next mixed solves (the Newton iteration within the time step;
+  // -1: no history) and the previous-step increments
+  int hist_slot = -1;
+  double guess_accept = 1.0;  // keep a guess whose residual is below guess_accept x the residual without it
+  std::unique_ptr<svgpu::GuessWork> guess;
   // mixed solves of systems with empty rows (the FSI equation): zero the increment's
   // entries of empty rows after flexible cycles (zero_null_rows_kernel)
   bool zero_null_rows = false;
@@ -324,9 +353,23 @@ int to_host(svgpu_ctx* ctx, std::vector<T>& dst, const T* src, size_t n) {
 
 bool misaligned_device(const void* p);
 // GNN helpers used by the solver (gnn.cpp)
-int gnn_apply_device(svgpu_ctx* ctx, const float* r32, const double* r64, const double* scale, float* out32,
-                     double* out64, const int* flags);
-int gnn_store_pair(svgpu_ctx* ctx, const double* r, const double* x);
+// scale: the device scalars {s_r, 1/s_p, s_o} of this evaluation (gnn_scales)
+int gnn_apply_device(svgpu_ctx* ctx, const float* r32, const double* r64, const float* p32, const double* scale,
+                     float* out32, double* out64, const int* flags);
+// Stores (r, p, x) in FP32 in the ring of training pairs; p (the prior) may be null.
+int gnn_store_pair(svgpu_ctx* ctx, const double* r, const float* p, const double* x);
+
+#ifdef __CUDACC__
+// Sum over nparts CTA partials part[c * stride + d] by one full warp: lane l adds
+// c = l, l + 32, ... in order, then a fixed shuffle tree (deterministic; every lane
+// returns the sum).  Call with all 32 lanes of warp 0.
+__device__ __forceinline__ double warp_sum_parts(const double* part, int nparts, int stride, int d) {
+  double v = 0.0;
+  for (int c = threadIdx.x & 31; c < nparts; c += 32) v += part[(long)c * stride + d];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+#endif
 
 inline int grid_for(long n, int block, int cap = 152 * 16) {
   long g = (n + block - 1) / block;
@@ -511,16 +554,32 @@ void launch_f32_to_f64(cudaStream_t s, long n, const float* a, double* b);
 int gnn_param_count();
 size_t gnn_part_floats(int sm_count);
 void gnn_forward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
-                 const double* r64, const float* stat, const double* sc, const __nv_bfloat16* P,
+                 const double* r64, const float* p32, const float* stat, const double* sc, const __nv_bfloat16* P,
                  __nv_bfloat16* const* h, __nv_bfloat16* const* msave, uint64_t* mask, float* out32,
                  double* out64, float* raw, int sm_count, const int* flags);
 void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
-                  const float* stat, const double* sc, const __nv_bfloat16* P, __nv_bfloat16* const* h,
-                  __nv_bfloat16* const* msave, const uint64_t* mask, const float* raw, const float* tgt,
-                  float* dA, float* dB, float* dC, float* part, double* lossbuf, float* grad, int sm_count);
+                  const float* p32, const float* stat, const double* sc, const __nv_bfloat16* P,
+                  __nv_bfloat16* const* h, __nv_bfloat16* const* msave, const uint64_t* mask, const float* raw,
+                  const float* tgt, float* dA, float* dB, float* dC, float* part, double* lossbuf, float* grad,
+                  int sm_count);
+void gnn_loss(cudaStream_t st, int nNo, const float* raw, const float* tgt, const float* p32, const double* sc,
+              double* lossbuf, int sm_count);
 void gnn_adam(cudaStream_t st, float lr, int step, const float* g, float* p, float* m, float* v, __nv_bfloat16* pb);
 void gnn_to_bf16(cudaStream_t st, const float* p, __nv_bfloat16* pb);
-void gnn_scale(cudaStream_t st, const double* nrm2, long n, double* sc);
+void gnn_scales(cudaStream_t st, long n, const float* a32, const double* a64, const float* p32, double* part,
+                double* sc, int sm_count);
+
+// ---- k_guess.cu ----------------------------------------------------------------
+// Minimal-residual initial guess from one or two directions (the previous step's
+// increment g and the network's correction d): dots, coefficients, update.
+constexpr int kGuessMaxDots = 4;
+void launch_guess_dots(cudaStream_t s, long n, int nd, const double* const* a, const double* const* b, double* part,
+                       int sm_count);
+void launch_guess_coef1(cudaStream_t s, int sm_count, const double* part, double* coef);
+void launch_guess_coef2(cudaStream_t s, int sm_count, const double* part, double* coef);
+void launch_guess_apply(cudaStream_t s, long n, const double* coef, const double* g, const double* d,
+                        const double* w1, const double* w2, const double* r, double* X, double* r0);
+void launch_scale_f32(cudaStream_t s, long n, const double* coef, const float* g, float* p);
 void gnn_f64_to_f32(cudaStream_t st, long n, const double* a, float* b);
 
 }  // namespace svgpu

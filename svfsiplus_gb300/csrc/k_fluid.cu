@@ -15,6 +15,7 @@
 // Scatter: elements arrive grouped by colour (no two elements of a colour share a
 // node), so the read-modify-write of R and Val needs no atomics and is deterministic.
 // The position of block (a,b) is rowPtr[ien[a]] + boff[e][a*4+b] (precomputed).
+#include "dword.h"
 #include "internal.h"
 
 namespace svgpu {
@@ -487,8 +488,9 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
     fluid_p1_kernel<double, double, true, true, false><<<grid, block, 0, s>>>(
         c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr);
   } else {
-    // residual rows in FP64, tangent blocks in FP32
-    fluid_p1_kernel<double, double, true, false, false><<<grid, block, 0, s>>>(
+    // residual rows in double-word FP32 (about 48 bits, accumulated into the FP64 R),
+    // tangent blocks in FP32
+    fluid_p1_kernel<dwf::dw, double, true, false, false><<<grid, block, 0, s>>>(
         c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
     fluid_p1_kernel<float, float, false, true, false><<<grid, block, 0, s>>>(
         c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr);
@@ -499,7 +501,7 @@ void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne,
                            const int* elem_id, const double* x4, const double* Ag, const double* Yg, const double* Bf,
                            const int* rowPtr, double* R, int* errflag) {
   if (ne <= 0) return;
-  fluid_p1_kernel<double, double, true, false, false><<<(ne + 127) / 128, 128, 0, s>>>(
+  fluid_p1_kernel<dwf::dw, double, true, false, false><<<(ne + 127) / 128, 128, 0, s>>>(
       c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
 }
 

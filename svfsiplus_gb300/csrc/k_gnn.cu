@@ -4,19 +4,27 @@
 // The reference has no counterpart; this is new work on top of its FSILS solve.
 //
 // Network (hidden width 64, weights stored in BF16, accumulation in FP32):
-//   input  x_i = [r_i / s (4), static_i (4)]   s = ||r|| / sqrt(n), static = scaled
-//                                               coordinates and wall distance
-//   h0_i   = relu(W0^T x_i + b0)                8 -> 64
+//   input  x_i = [r_i / s_r (4), p_i / s_p (4), static_i (4)]
+//          r: the residual, s_r = ||r|| / sqrt(n); p: an optional prior increment (the
+//          previous time step's increment of the same Newton iteration, scaled by its
+//          minimal-residual coefficient), s_p its rms; static: scaled coordinates and
+//          wall distance.  Without a prior the p channels are zero.
+//   h0_i   = relu(W0^T x_i + b0)                12 -> 64
 //   layer l = 1..3:
 //     m_i  = mean_{j in N(i)} h_j               (N(i): the CSR row of node i, self included)
 //     z_i  = Wl^T [h_i; m_i] + bl               128 -> 64
 //     h_i <- h_i + relu(z_i)
-//   out_i  = Wd^T h3_i + bd                     64 -> 4,  M(r)_i = s * out_i
+//   out_i  = Wd^T h3_i + bd                     64 -> 4
+//   M(r, p) = p + s_o * out,   s_o = s_p with a prior, s_r without
+// The network thus predicts a correction of the prior; the solver uses p and s_o out
+// as two search directions of a minimal-residual initial guess.  Scalars of one
+// evaluation (device array sc): sc[0] = s_r, sc[1] = 1 / s_p (0 without a prior),
+// sc[2] = s_o.
 // Activations h are stored in BF16 (the gathers read 128 bytes per neighbour);
 // gradients and weight-gradient partial sums are FP32.
 //
 // Parameter vector (FP32 master copy, BF16 working copy), offsets in floats:
-//   W0 [8][64] | b0 [64] | W1 [128][64] | b1 [64] | W2 | b2 | W3 | b3 | Wd [64][4] | bd [4]
+//   W0 [12][64] | b0 [64] | W1 [128][64] | b1 [64] | W2 | b2 | W3 | b3 | Wd [64][4] | bd [4]
 #include <cuda_bf16.h>
 
 #include "internal.h"
@@ -26,7 +34,7 @@ namespace svgpu {
 namespace {
 
 constexpr int H = 64;
-constexpr int NIN = 8;
+constexpr int NIN = 12;
 constexpr int OFF_W0 = 0, OFF_B0 = NIN * H;
 constexpr int LAYER = 2 * H * H + H;
 __host__ __device__ constexpr int off_w(int l) { return OFF_B0 + H + (l - 1) * LAYER; }
@@ -39,6 +47,7 @@ __device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162f
 // ---- encoder: one thread per (node, 8 outputs)
 __global__ void __launch_bounds__(256) gnn_encode_kernel(int nNo, const float* __restrict__ in_r,
                                                          const double* __restrict__ in_r64,
+                                                         const float* __restrict__ in_p,
                                                          const float* __restrict__ stat, const double* __restrict__ sc,
                                                          const __nv_bfloat16* __restrict__ P,
                                                          __nv_bfloat16* __restrict__ h0, uint64_t* __restrict__ mask,
@@ -49,11 +58,14 @@ __global__ void __launch_bounds__(256) gnn_encode_kernel(int nNo, const float* _
   const int cg = (int)(t & 7);
   const bool live = i < nNo;  // no early return: the mask is assembled with warp shuffles
   const float inv = (float)(1.0 / sc[0]);
+  const float cp = (float)sc[1];
   float x[NIN];
 #pragma unroll
   for (int k = 0; k < 4; k++) x[k] = live ? (in_r ? in_r[4 * i + k] : (float)in_r64[4 * i + k]) * inv : 0.f;
 #pragma unroll
-  for (int k = 0; k < 4; k++) x[4 + k] = live ? stat[4 * i + k] : 0.f;
+  for (int k = 0; k < 4; k++) x[4 + k] = live && in_p ? in_p[4 * i + k] * cp : 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) x[8 + k] = live ? stat[4 * i + k] : 0.f;
   uint32_t bits = 0;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
@@ -106,9 +118,21 @@ __global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restr
         const __nv_bfloat162 own = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * i)[lane];
         o0 = __low2float(own);
         o1 = __high2float(own);
-        for (int k = b; k < e; k++) {
-          const int j = __ldg(colPtr + k);
-          const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * j)[lane];
+        // eight neighbour rows in flight per warp; the sums keep the row order
+        const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(hin);
+        int k = b;
+        for (; k + 8 <= e; k += 8) {
+          __nv_bfloat162 v[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) v[u] = hv[(long)(H / 2) * __ldg(colPtr + k + u) + lane];
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            s0 += __low2float(v[u]);
+            s1 += __high2float(v[u]);
+          }
+        }
+        for (; k < e; k++) {
+          const __nv_bfloat162 v = hv[(long)(H / 2) * __ldg(colPtr + k) + lane];
           s0 += __low2float(v);
           s1 += __high2float(v);
         }
@@ -169,7 +193,7 @@ __global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restr
   }
 }
 
-// ---- decoder: out_i = s (Wd^T h_i + bd); output FP32 or FP64, optional add
+// ---- decoder: out_i = s_o (Wd^T h_i + bd); output FP32 or FP64
 __global__ void __launch_bounds__(256) gnn_decode_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
                                                          const __nv_bfloat16* __restrict__ P,
                                                          const double* __restrict__ sc, float* __restrict__ out32,
@@ -189,23 +213,30 @@ __global__ void __launch_bounds__(256) gnn_decode_kernel(int nNo, const __nv_bfl
     z = fmaf(__high2float(v), bf(P[OFF_WD + (2 * k + 1) * 4 + c]), z);
   }
   if (raw) raw[4 * i + c] = z;
-  const double s = sc[0];
+  const double s = sc[2];
   if (out32) out32[4 * i + c] = (float)(s * z);
   if (out64) out64[4 * i + c] = s * (double)z;
 }
 
-// ---- loss: per CTA partial of sum |out - t/s|^2 and |t/s|^2; d_out = 2 (out - t/s) / E
+// ---- loss: the target of out is t = (x - p) / s_o; per CTA partial of sum |out - t|^2
+// and E = sum |x / s_o|^2 (the error relative to the increment itself, so that
+// triples whose prior is already close weigh little); d_out = 2 (out - t) / E
+__device__ __forceinline__ float gnn_target(const float* tgt, const float* prior, long k, float inv) {
+  return (prior ? tgt[k] - prior[k] : tgt[k]) * inv;
+}
+
 __global__ void __launch_bounds__(256) gnn_loss_kernel(long n, const float* __restrict__ out,
-                                                       const float* __restrict__ tgt, const double* __restrict__ sc,
-                                                       double* __restrict__ part) {
+                                                       const float* __restrict__ tgt, const float* __restrict__ prior,
+                                                       const double* __restrict__ sc, double* __restrict__ part) {
   __shared__ double r0[8], r1[8];
-  const float inv = (float)(1.0 / sc[0]);
+  const float inv = (float)(1.0 / sc[2]);
   double a = 0.0, b = 0.0;
   for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-    const float tt = tgt[k] * inv;
+    const float tt = gnn_target(tgt, prior, k, inv);
     const float d = out[k] - tt;
+    const float xx = tgt[k] * inv;
     a += (double)d * d;
-    b += (double)tt * tt;
+    b += (double)xx * xx;
   }
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -228,21 +259,20 @@ __global__ void __launch_bounds__(256) gnn_loss_kernel(long n, const float* __re
 }
 
 __global__ void gnn_loss_final_kernel(int nparts, const double* __restrict__ part, double* __restrict__ loss) {
-  if (threadIdx.x != 0) return;
-  double a = 0, b = 0;
-  for (int c = 0; c < nparts; c++) {
-    a += part[2 * c];
-    b += part[2 * c + 1];
+  if (threadIdx.x >= 32 || blockIdx.x != 0) return;
+  const double a = warp_sum_parts(part, nparts, 2, 0), b = warp_sum_parts(part, nparts, 2, 1);
+  if (threadIdx.x == 0) {
+    loss[0] = a / b;  // relative squared error
+    loss[1] = b;
   }
-  loss[0] = a / b;  // relative squared error
-  loss[1] = b;
 }
 
-// d_out = 2 (out - t/s) / E ; decoder backward: dh3 = Wd d_out (FP32), and the
+// d_out = 2 (out - t) / E ; decoder backward: dh3 = Wd d_out (FP32), and the
 // per-CTA partial of dWd = sum_i h_i d_out_i^T, dbd = sum d_out.
 __global__ void __launch_bounds__(128) gnn_decode_bwd_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
                                                              const float* __restrict__ out,
                                                              const float* __restrict__ tgt,
+                                                             const float* __restrict__ prior,
                                                              const double* __restrict__ sc,
                                                              const double* __restrict__ loss,
                                                              const __nv_bfloat16* __restrict__ P,
@@ -250,12 +280,12 @@ __global__ void __launch_bounds__(128) gnn_decode_bwd_kernel(int nNo, const __nv
   __shared__ float g[H * 4 + 4];
   for (int k = threadIdx.x; k < H * 4 + 4; k += blockDim.x) g[k] = 0.f;
   __syncthreads();
-  const float inv = (float)(1.0 / sc[0]);
+  const float inv = (float)(1.0 / sc[2]);
   const float scale = (float)(2.0 / loss[1]);
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nNo; i += (long)gridDim.x * blockDim.x) {
     float d[4];
 #pragma unroll
-    for (int c = 0; c < 4; c++) d[c] = scale * (out[4 * i + c] - tgt[4 * i + c] * inv);
+    for (int c = 0; c < 4; c++) d[c] = scale * (out[4 * i + c] - gnn_target(tgt, prior, 4 * i + c, inv));
     const __nv_bfloat16* hi = h + (long)H * i;
     for (int k = 0; k < H; k++) {
       const float hk = bf(hi[k]);
@@ -371,24 +401,30 @@ __global__ void __launch_bounds__(256) gnn_scatter_bwd_kernel(int nNo, const int
 
 // encoder backward: dz0 = dh0 * relu'; dW0 partial = x^T dz0, db0 = sum dz0
 __global__ void __launch_bounds__(64) gnn_encode_bwd_kernel(int nNo, const float* __restrict__ in_r,
+                                                            const float* __restrict__ in_p,
                                                             const float* __restrict__ stat,
                                                             const double* __restrict__ sc,
                                                             const uint64_t* __restrict__ mask,
                                                             const float* __restrict__ dh, float* __restrict__ gpart) {
-  // thread c (0..63) owns column c of W0 (8 entries) and b0[c]
+  // thread c (0..63) owns column c of W0 (NIN entries) and b0[c]
   const int c = threadIdx.x;
   float g[NIN + 1];
 #pragma unroll
   for (int k = 0; k <= NIN; k++) g[k] = 0.f;
   const float inv = (float)(1.0 / sc[0]);
+  const float cp = (float)sc[1];
   for (long i = blockIdx.x; i < nNo; i += gridDim.x) {
     const uint64_t m = mask[i];
     if (!((m >> c) & 1ull)) continue;
     const float dz = dh[(long)H * i + c];
 #pragma unroll
     for (int k = 0; k < 4; k++) g[k] = fmaf(in_r[4 * i + k] * inv, dz, g[k]);
+    if (in_p) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) g[4 + k] = fmaf(stat[4 * i + k], dz, g[4 + k]);
+      for (int k = 0; k < 4; k++) g[4 + k] = fmaf(in_p[4 * i + k] * cp, dz, g[4 + k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) g[8 + k] = fmaf(stat[4 * i + k], dz, g[8 + k]);
     g[NIN] += dz;
   }
   float* gp = gpart + (long)blockIdx.x * (NIN * H + H);
@@ -430,11 +466,53 @@ __global__ void gnn_to_bf16_kernel(int n, const float* __restrict__ p, __nv_bflo
   if (k < n) pb[k] = __float2bfloat16(p[k]);
 }
 
-__global__ void rms_scale_kernel(const double* __restrict__ nrm2, long n, double* __restrict__ sc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = sqrt(*nrm2 / (double)n);
-    sc[0] = s > 0.0 ? s : 1.0;
+// Per-CTA partial sums of squares of the residual (FP32 or FP64) and of the prior.
+__global__ void __launch_bounds__(256) gnn_sumsq_kernel(long n, const float* __restrict__ a32,
+                                                        const double* __restrict__ a64,
+                                                        const float* __restrict__ p32, double* __restrict__ part) {
+  __shared__ double r0[8], r1[8];
+  double a = 0.0, b = 0.0;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const double v = a32 ? (double)a32[k] : a64[k];
+    a += v * v;
+    if (p32) {
+      const double w = p32[k];
+      b += w * w;
+    }
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r0[threadIdx.x >> 5] = a;
+    r1[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0, s1 = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+      s0 += r0[q];
+      s1 += r1[q];
+    }
+    part[2 * blockIdx.x] = s0;
+    part[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+// sc = {s_r, 1/s_p, s_o} from the partial sums (fixed order): s_r = rms(r) (1 for a
+// zero residual); with a nonzero prior s_o = s_p = rms(p), otherwise sc[1] = 0, s_o = s_r.
+__global__ void gnn_scales_kernel(int nparts, const double* __restrict__ part, long n, double* __restrict__ sc) {
+  if (threadIdx.x >= 32 || blockIdx.x != 0) return;
+  const double a = warp_sum_parts(part, nparts, 2, 0), b = warp_sum_parts(part, nparts, 2, 1);
+  if (threadIdx.x != 0) return;
+  double sr = sqrt(a / (double)n);
+  if (!(sr > 0.0) || !isfinite(sr)) sr = 1.0;
+  const double sp = sqrt(b / (double)n);
+  const bool prior = sp > 0.0 && isfinite(sp);
+  sc[0] = sr;
+  sc[1] = prior ? 1.0 / sp : 0.0;
+  sc[2] = prior ? sp : sr;
 }
 
 __global__ void f64_to_f32_k(long n, const double* __restrict__ a, float* __restrict__ b) {
@@ -446,42 +524,57 @@ __global__ void f64_to_f32_k(long n, const double* __restrict__ a, float* __rest
 
 int gnn_param_count() { return NPARAM; }
 
-// Forward pass.  r: FP32 (r32) or FP64 (r64) input vector (4, nNo); sc: device scale s.
+// Forward pass.  r: FP32 (r32) or FP64 (r64) input vector (4, nNo); p32: the prior
+// (FP32, may be null); sc: the device scalars {s_r, 1/s_p, s_o}.
 // h: 4 activation buffers (BF16, nNo x 64 each); msave/mask may be null (inference).
 void gnn_forward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
-                 const double* r64, const float* stat, const double* sc, const __nv_bfloat16* P,
+                 const double* r64, const float* p32, const float* stat, const double* sc, const __nv_bfloat16* P,
                  __nv_bfloat16* const* h, __nv_bfloat16* const* msave, uint64_t* mask, float* out32,
                  double* out64, float* raw, int sm_count, const int* flags) {
   const long t = 8L * nNo;
-  gnn_encode_kernel<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(nNo, r32, r64, stat, sc, P, h[0], mask, flags);
+  gnn_encode_kernel<<<(unsigned)((t + 255) / 256), 256, 0, st>>>(nNo, r32, r64, p32, stat, sc, P, h[0], mask,
+                                                                  flags);
   const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
-  const int grid = tiles < 8 * sm_count ? tiles : 8 * sm_count;
+  // persistent CTAs: as many as fit on the SMs at once (one wave)
+  static int per_sm = 0;
+  if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gnn_mp_kernel, 128, 0) != cudaSuccess ||
+                      per_sm < 1))
+    per_sm = 4;
+  const int grid = tiles < per_sm * sm_count ? tiles : per_sm * sm_count;
   for (int l = 1; l <= 3; l++)
     gnn_mp_kernel<<<grid, 128, 0, st>>>(nNo, rowPtr, colPtr, h[l - 1], P, l, h[l], msave ? msave[l] : nullptr, mask,
                                         flags);
   gnn_decode_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, st>>>(nNo, h[3], P, sc, out32, out64, raw, flags);
 }
 
-void gnn_scale(cudaStream_t st, const double* nrm2, long n, double* sc) { rms_scale_kernel<<<1, 32, 0, st>>>(nrm2, n, sc); }
+// The scalars of one evaluation from its residual (a32 or a64) and prior p32 (or null);
+// part holds 2 x 2 sm_count doubles.
+void gnn_scales(cudaStream_t st, long n, const float* a32, const double* a64, const float* p32, double* part,
+                double* sc, int sm_count) {
+  const int parts = 2 * sm_count;
+  gnn_sumsq_kernel<<<parts, 256, 0, st>>>(n, a32, a64, p32, part);
+  gnn_scales_kernel<<<1, 32, 0, st>>>(parts, part, n, sc);
+}
 
 void gnn_f64_to_f32(cudaStream_t st, long n, const double* a, float* b) {
   f64_to_f32_k<<<grid_for(n, 256), 256, 0, st>>>(n, a, b);
 }
 
-// Loss + backward + gradient.  raw: decoder outputs (before the scale s) of the
-// forward pass; tgt: FP32 target increments.  grad (NPARAM floats) is written.
+// Loss + backward + gradient.  raw: decoder outputs (before the scale s_o) of the
+// forward pass; tgt: FP32 target increments; p32: the prior of the forward pass (or
+// null).  grad (NPARAM floats) is written.
 // Work buffers: dA, dB, dC (nNo x 64 FP32 each), part (partials), lossbuf (2 doubles).
 void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr, const float* r32,
-                  const float* stat, const double* sc, const __nv_bfloat16* P, __nv_bfloat16* const* h,
+                  const float* p32, const float* stat, const double* sc, const __nv_bfloat16* P, __nv_bfloat16* const* h,
                   __nv_bfloat16* const* msave, const uint64_t* mask, const float* raw, const float* tgt,
                   float* dA, float* dB, float* dC, float* part, double* lossbuf, float* grad, int sm_count) {
   const long n4 = 4L * nNo;
   const int lparts = 2 * sm_count;
-  gnn_loss_kernel<<<lparts, 256, 0, st>>>(n4, raw, tgt, sc, lossbuf + 2);
+  gnn_loss_kernel<<<lparts, 256, 0, st>>>(n4, raw, tgt, p32, sc, lossbuf + 2);
   gnn_loss_final_kernel<<<1, 32, 0, st>>>(lparts, lossbuf + 2, lossbuf);
   // decoder
   const int dparts = 2 * sm_count;
-  gnn_decode_bwd_kernel<<<dparts, 128, 0, st>>>(nNo, h[3], raw, tgt, sc, lossbuf, P, dA, part);
+  gnn_decode_bwd_kernel<<<dparts, 128, 0, st>>>(nNo, h[3], raw, tgt, p32, sc, lossbuf, P, dA, part);
   gnn_reduce_grad_kernel<<<(H * 4 + 4 + 255) / 256, 256, 0, st>>>(dparts, H * 4 + 4, H * 4 + 4, part, grad + OFF_WD);
   // layers 3..1: dA holds the gradient of the layer output
   float* dcur = dA;
@@ -494,9 +587,17 @@ void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr
   }
   // encoder
   const int eparts = 4 * sm_count;
-  gnn_encode_bwd_kernel<<<eparts, 64, 0, st>>>(nNo, r32, stat, sc, mask, dcur, part);
+  gnn_encode_bwd_kernel<<<eparts, 64, 0, st>>>(nNo, r32, p32, stat, sc, mask, dcur, part);
   gnn_reduce_grad_kernel<<<(NIN * H + H + 255) / 256, 256, 0, st>>>(eparts, NIN * H + H, NIN * H + H, part,
                                                                    grad + OFF_W0);
+}
+
+// Loss only (no gradient) of a forward pass: lossbuf[0] = relative squared error.
+void gnn_loss(cudaStream_t st, int nNo, const float* raw, const float* tgt, const float* p32, const double* sc,
+              double* lossbuf, int sm_count) {
+  const int lparts = 2 * sm_count;
+  gnn_loss_kernel<<<lparts, 256, 0, st>>>(4L * nNo, raw, tgt, p32, sc, lossbuf + 2);
+  gnn_loss_final_kernel<<<1, 32, 0, st>>>(lparts, lossbuf + 2, lossbuf);
 }
 
 void gnn_adam(cudaStream_t st, float lr, int step, const float* g, float* p, float* m, float* v, __nv_bfloat16* pb) {

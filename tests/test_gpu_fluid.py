@@ -74,8 +74,9 @@ def test_assembly_is_deterministic(golden):
 
 
 def test_assembly_mixed_precision(golden):
-    """SVGPU_MIXED: FP64 residual rows (within 1e-12 of the reference) and an FP32
-    tangent (within 2e-6 relative)."""
+    """SVGPU_MIXED: residual rows integrated in double-word FP32 arithmetic and
+    accumulated in FP64 (within 1e-12 of the reference) and an FP32 tangent (within
+    2e-6 relative)."""
     g = golden("small")
     m = named_pipe("small")
     ctx = make_ctx(m, g["rowPtr"], g["colPtr"])
