@@ -12,8 +12,9 @@ to 1e-6 of its value at the step's first iteration. There are at most 8 Newton i
 Each linear solve is inexact (relative tolerance 1e-2), as in inexact Newton.
 
 Paths (--path):
-  learned    -- the headline: mixed precision (FP32 tangent/Krylov basis, FP64 residual
-                and defect correction) with FGMRES(50) preconditioned by an aggregation
+  learned    -- the headline: mixed precision (FP32 tangent/Krylov basis, residual rows
+                in double-word FP32 accumulated in FP64, FP64 defect correction) with
+                FGMRES(50) preconditioned by an aggregation
                 multilevel V-cycle, started from the learned initial guess (solver mode
                 4): the minimal-residual combination of the previous time step's
                 increment of the same Newton iteration and the network's correction of
@@ -22,7 +23,7 @@ Paths (--path):
                 is trained online (Adam, lr 1e-3) on the solver's own
                 (residual, prior, increment) triples during the warm-up steps.  The
                 tangent of a step's first Newton iteration serves its later iterations
-                (modified Newton; the FP64 residual is assembled every iteration);
+                (modified Newton; the residual is assembled every iteration);
   history    -- the same initial guess without the network (mode 5);
   multilevel -- the same solver with a zero initial guess (mode 2);
   learned-smoother -- the network as finest-level pre-smoother (mode 3);
@@ -47,7 +48,9 @@ Our arm prints one JSON line:
 
 --impl reference times the reference's CPU path (the oracle port: the reference's
 sources compile only where its tree is present) on a bounded sample per step.
---study MODES prints per-step solver statistics for the listed solver modes.
+--study PATHS prints per-step solver statistics for the listed paths; --long N runs
+--paths for N steps each after the headline's warm-up; --increments N compares the
+Newton increments of consecutive steps; --gnn-only times the network's forward pass.
 """
 from __future__ import annotations
 
@@ -497,7 +500,7 @@ def run_ours(args):
         "metric": METRIC, "value": dev_ms / 1e3 / args.steps, "unit": "s/time step", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if mode < 0 else "f32 tangent/Krylov + f64 residual",
+        "dtype": "f64" if mode < 0 else "f32 tangent/Krylov + double-word f32 residual rows, f64 accumulation",
         "data": "synthetic: procedural 8M-tet pipe, seeded wall perturbation (numpy seed 20261203)",
         "config": {"workload": f"{args.workload}: {mesh.nEl} tets, {nNo} nodes, {colPtr.size} blocks; VMS P1-P1 fluid; "
                                f"Newton to picc r1 <= {NEWTON_TOL:g}*pNorm (max {NEWTON_MAX}); linear rel tol "
@@ -752,6 +755,113 @@ def run_reference(args):
 KRYLOV_ITS_PIPE8M = float((KRYLOV_DIM + 1) * MAX_RESTARTS)
 
 
+def run_long(args):
+    """Several solver paths over many steps from rest, each with the headline's warm-up
+    (and, for the learned path, its online training): per-path mean s per step
+    (CUDA-synchronised host clock around every step), Krylov iterations per step, the
+    first Newton solve's iterations and its initial-guess residual."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    for path in args.paths.split(","):
+        s, mode = make_solver(api, mesh, rowPtr, colPtr, path, 0)
+        api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
+        step, _ = device_stepper(api, s)
+        for k in range(args.warmup):
+            step()
+            if mode in (3, 4):
+                train_online(api, s)
+        if mode in (3, 4):
+            s.ctx.gnn_collect(False)
+            s.ctx.set_solver_mode(mode)
+        its, k0, x0, secs = [], [], [], []
+        for _ in range(args.long):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            q = step()
+            torch.cuda.synchronize()
+            secs.append(time.perf_counter() - t)
+            its.append(sum(r["itr"] for r in q))
+            k0.append(q[0]["itr"])
+            x0.append(round(q[0]["x0_rel"], 3))
+        print(json.dumps({"workload": args.workload, "path": path, "solver_mode": mode, "steps": args.long,
+                          "warmup": args.warmup, "mean_s": float(np.mean(secs)), "krylov_its_total": int(sum(its)),
+                          "krylov_its": its, "first_solve_its": k0, "first_solve_x0_rel": x0,
+                          "guesses_tried_rejected_with_network": s.ctx.guess_stats if mode in (4, 5) else None,
+                          "s": [round(v, 3) for v in secs]}), flush=True)
+        s.ctx.close()
+        torch.cuda.empty_cache()
+
+
+def run_increments(args):
+    """How alike the Newton increments of consecutive steps are: the solver's own
+    (residual, prior, increment) triples of every mixed solve (mode 2, collection on),
+    compared per Newton iteration between consecutive steps: cosine and the relative
+    error of the best multiple, in the increment x and in the residual r = K x."""
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    s, _ = make_solver(api, mesh, rowPtr, colPtr, "multilevel", 0)
+    s.enable_learning(collect=1)
+    counts = []
+    for _ in range(args.increments):
+        counts.append(len(s.step(U_MEAN, U_AMP, U_FREQ)))
+    trip = s.ctx.gnn_pairs()
+    keys = [(n, k) for n, c in enumerate(counts) for k in range(c)][-len(trip):]
+    P = dict(zip(keys, trip))
+
+    def cos(a, b):
+        return float((a * b).sum() / np.sqrt((a * a).sum() * (b * b).sum()))
+    for (n, k), (r, _, x) in P.items():
+        if (n - 1, k) not in P:
+            continue
+        rp, _, xp = P[(n - 1, k)]
+        cx, cr = cos(x, xp), cos(r, rp)
+        print(json.dumps({"workload": args.workload, "step": n + 1, "newton_iter": k + 1, "cos_x": round(cx, 5),
+                          "best_multiple_rel_err_x": round(float(np.sqrt(max(0.0, 1 - cx * cx))), 5),
+                          "cos_r": round(cr, 5), "norm_r": float(np.linalg.norm(r)),
+                          "norm_x": float(np.linalg.norm(x))}), flush=True)
+    s.ctx.close()
+
+
+def run_gnn_time(args):
+    """The network's forward pass (svgpu_gnn_apply with a prior, device arrays) on the
+    workload's graph: CUDA events over repeated calls after two warm-up calls."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(mesh.nNo, rowPtr, colPtr, 0)
+    ctx.gnn_create(api.pipe_node_features(mesh), seed=3)
+    p = ctx.gnn_params()
+    n_dec = 64 * 4 + 4
+    p[-n_dec:] = np.random.default_rng(0).uniform(-0.3, 0.3, n_dec).astype(np.float32)  # a nonzero decoder
+    ctx.gnn_set_params(p)
+    r = torch.randn(4 * mesh.nNo, dtype=torch.float64, device="cuda")
+    pr = torch.randn(4 * mesh.nNo, dtype=torch.float64, device="cuda")
+    z = torch.zeros_like(r)
+    ptr = lambda t: api.C.c_void_p(t.data_ptr())  # noqa: E731
+    for _ in range(2):
+        api.lib().svgpu_gnn_apply(ctx._h, ptr(r), ptr(pr), ptr(z))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        api.lib().svgpu_gnn_apply(ctx._h, ptr(r), ptr(pr), ptr(z))
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": args.workload, "nodes": mesh.nNo, "blocks": int(colPtr.size),
+                      "gnn_apply_ms": e0.elapsed_time(e1) / args.steps, "calls": args.steps}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -778,6 +888,11 @@ def main():
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     ap.add_argument("--reuse-tangent", type=int, default=None,
                     help="1: mixed paths keep the tangent of a step's first Newton iteration (modified Newton)")
+    ap.add_argument("--long", type=int, default=0, help="steps per path of a long run of --paths")
+    ap.add_argument("--paths", default="multilevel,history,learned", help="--long: comma-separated paths")
+    ap.add_argument("--increments", type=int, default=0,
+                    help="steps from rest: compare the Newton increments of consecutive steps")
+    ap.add_argument("--gnn-only", action="store_true", help="time the network's forward pass (--steps calls)")
     args = ap.parse_args()
     global LIN_REL_TOL, REUSE_TANGENT
     if args.lin_rel_tol is not None:
@@ -798,6 +913,12 @@ def main():
         run_config1(args)
     elif args.sweep:
         run_sweep(args)
+    elif args.long:
+        run_long(args)
+    elif args.increments:
+        run_increments(args)
+    elif args.gnn_only:
+        run_gnn_time(args)
     else:
         run_ours(args)
 

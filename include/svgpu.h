@@ -142,7 +142,8 @@ int svgpu_face_create(svgpu_ctx* ctx, int faceId, int nFaEl, const int* fIEN, co
  * VMS tets: adds the element residuals and tangents into R (4,nNo) and Val (16,nnz).
  * Ag, Yg (4,nNo); Bf (3,nNo) or NULL.  R == NULL and Val == NULL assemble into the
  * context's resident system (zeroed first, like ls_alloc, ls.cpp:51).
- * precision SVGPU_FP64 or SVGPU_MIXED (FP32 element integrals and tangent).
+ * precision SVGPU_FP64 or SVGPU_MIXED (FP32 tangent; residual rows integrated in
+ * double-word FP32, about 48 bits, and accumulated in FP64).
  * Returns SVGPU_EJAC for a zero Jacobian. */
 int svgpu_construct_fluid(svgpu_ctx* ctx, const svgpu_fluid_props* props, const double* Ag,
                           const double* Yg, const double* Bf, double* R, double* Val, int precision);
@@ -345,7 +346,7 @@ typedef struct {
   double outletH;            /* Neumann value on it */
   /* SVGPU_MIXED only, no reference counterpart: 1 assembles the tangent (and the
    * diagonal scaling and multilevel set-up) at a step's first Newton iteration and
-   * reuses it for the later ones, which assemble the FP64 residual alone (a modified
+   * reuses it for the later ones, which assemble the residual rows alone (a modified
    * Newton iteration; the residual and the convergence test are unchanged); when an
    * iteration with the kept tangent lowers the preconditioned residual less than
    * tenfold, the next iteration reassembles it.  0: every iteration, as the reference. */
