@@ -68,6 +68,14 @@ int upload_dir(svgpu_ctx* ctx, const svgpu_dirichlet_set* d, DevBuf<int>& nodes,
   return to_device(ctx, A, d->A, 3L * d->n);
 }
 
+// Solver mode of the mesh equation's context: the multilevel FGMRES (mode 2), started
+// from the previous step's increment when the FSI equation uses the history guesses
+// (modes 4 and 5; the mesh context has no network).
+int mesh_mode(const svgpu_ctx* ctx) {
+  if (ctx->learned_mode == 0) return 0;
+  return ctx->learned_mode >= 4 ? 5 : 2;
+}
+
 // The mesh equation's own context for its mixed-precision multilevel solve: the same
 // block pattern, linear-solver faces, multilevel options and solid-node labels as the
 // parent, GMRES settings of the mesh equation, the parent's stream.
@@ -78,7 +86,7 @@ int mesh_context(svgpu_ctx* ctx, const svgpu_fsi_opts* opts, FsiWork& w) {
     if ((rc = svgpu_ls_create(m, SVGPU_LS_GMRES, opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
                               opts->dimKry[1])))
       return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
-    m->learned_mode = ctx->learned_mode == 0 ? 0 : 2;
+    m->learned_mode = mesh_mode(ctx);
     return SVGPU_OK;
   }
   svgpu_ctx* m = nullptr;
@@ -98,7 +106,7 @@ int mesh_context(svgpu_ctx* ctx, const svgpu_fsi_opts* opts, FsiWork& w) {
   if ((rc = svgpu_ls_create(m, SVGPU_LS_GMRES, opts->relTol[1], opts->absTol[1], opts->lsMaxItr[1],
                             opts->dimKry[1])))
     return set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + m->err);
-  m->learned_mode = ctx->learned_mode == 0 ? 0 : 2;
+  m->learned_mode = mesh_mode(ctx);
   m->ml_omega = ctx->ml_omega;
   m->ml_coarse_sweeps = ctx->ml_coarse_sweeps;
   m->ml_coarsest = ctx->ml_coarsest;

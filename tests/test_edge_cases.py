@@ -156,3 +156,23 @@ def test_fsi_step_without_domains_is_refused():
                      (np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3))), z, z, z, z.copy(), z.copy(), z.copy(),
                      [0.0, 0.0], [0.0, 0.0])
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_history_and_guess_options_checked():
+    """The history slot and the guess threshold are range-checked; a cleared history
+    gives no initial guess (x0_rel 0) and the solve still converges."""
+    m = named_pipe("tiny")
+    ctx, rowPtr, colPtr = _ctx(m, 0)
+    ctx.fsils_ls_create(api.LS_TYPE_GMRES, 1e-8, 1e-17, 10, 20)
+    with pytest.raises(RuntimeError, match="history_slot"):
+        ctx.history_slot(16)
+    with pytest.raises(RuntimeError, match="history_slot"):
+        ctx.history_slot(-2)
+    assert api.lib().svgpu_guess_options(ctx._h, api.C.c_double(0.0)) != api.SVGPU_OK
+    assert api.lib().svgpu_guess_options(ctx._h, api.C.c_double(1.5)) != api.SVGPU_OK
+    assert api.lib().svgpu_guess_options(ctx._h, api.C.c_double(0.5)) == api.SVGPU_OK
+    ctx.history_slot(0)
+    ctx.history_clear()
+    assert ctx.guess_stats == (0, 0, 0)
+    ctx.close()

@@ -180,10 +180,13 @@ def test_gpu_fsi_steps_mixed_multilevel(golden):
 
 
 @pytest.mark.gpu
-def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden):
+@pytest.mark.parametrize("mode", [2, 5])
+def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden, mode):
     """The mixed path with the mesh equation solved by the multilevel FGMRES as well (its
     dof-3 system padded to 4x4 blocks in a solver context of its own): per-field
-    relative L2 within 1e-6 of the reference's fields after every step."""
+    relative L2 within 1e-6 of the reference's fields after every step.  Mode 5 starts
+    both equations' solves from the previous step's increment of the same Newton
+    iteration (kept only where it lowers the FP64 residual)."""
     from svfsiplus_gb300 import api
     g = golden("fsi_run_small")
     ps = _run_params(g)
@@ -193,7 +196,7 @@ def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden):
     s = api.PipeFsiSolver(m, p, newton=(3, 3, 1e-11), mesh_newton=(3, 3, 1e-11),
                           gmres=(ps["ls_rel_tol"], ps["ls_abs_tol"], ps["ls_max_itr"], ps["ls_krylov_dim"]),
                           precision=api.SVGPU_MIXED, mesh_gmres=(1e-10, 1e-17, 100, 50))
-    s.ctx.set_solver_mode(2)
+    s.ctx.set_solver_mode(mode)
     solid = np.zeros(m.nNo, bool)
     solid[s.solid_nodes] = True
     for step in (1, 2, 3):
