@@ -14,6 +14,7 @@
  */
 #ifndef SVGPU_H
 #define SVGPU_H
+#include <stddef.h>
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -70,6 +71,11 @@ const char* svgpu_last_error(const svgpu_ctx* ctx);
 long long svgpu_kernel_launches(const svgpu_ctx* ctx);
 /* Use a caller-owned cudaStream_t (passed as void*) instead of the context's own. */
 int svgpu_set_stream(svgpu_ctx* ctx, void* stream);
+/* Page-locked host memory for the host arrays a caller passes (the state of a time
+ * step): copies from and to it run at the link's rate instead of through staging
+ * buffers.  No context needed; free with svgpu_host_free. */
+int svgpu_host_alloc(size_t bytes, void** p);
+int svgpu_host_free(void* p);
 
 /* ---- CSR pattern ------------------------------------------------------------------ */
 /* Replaces lhsa (solver/lhsa.cpp:153-380, without the undefNeu remap): the block

@@ -484,6 +484,33 @@ def _restart_error(path, stamp):
     return f"read_restart: file too short: {path}"
 
 
+class _PinnedHolder:
+    """Owns one page-locked host allocation (svgpu_host_alloc) and frees it."""
+
+    def __init__(self, nbytes):
+        self.p = C.c_void_p()
+        if lib().svgpu_host_alloc(C.c_size_t(nbytes), C.byref(self.p)) != SVGPU_OK:
+            raise RuntimeError(f"svgpu_host_alloc: {nbytes} bytes of page-locked memory not available")
+
+    def __del__(self):
+        if self.p:
+            lib().svgpu_host_free(self.p)
+            self.p = C.c_void_p()
+
+
+def pinned_zeros(shape, dtype=np.float64):
+    """A zeroed numpy array in page-locked host memory: the host state of a time step
+    then moves to and from the GPU without staging copies."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    h = _PinnedHolder(nbytes)
+    buf = (C.c_char * max(nbytes, 1)).from_address(h.p.value)
+    buf._holder = h  # the allocation lives as long as the array's buffer
+    a = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+    a[...] = 0
+    return a
+
+
 def csr_pattern(nNo: int, ien: np.ndarray):
     """lhsa (lhsa.cpp:153): rowPtr/colPtr of the element cliques, sorted columns
     (native svgpu_lhsa)."""
@@ -572,7 +599,7 @@ class PipeFluidSolver:
         self.dir_nodes, self.dir_prof = dirichlet_nodes(mesh)
         self.ctx.set_dirichlet(self.dir_nodes)
         self.opts = NewtonOpts(newton_min, newton_max, newton_tol, precision, FACE_OUTLET, 0.0, int(reuse_tangent))
-        z = lambda: np.zeros((nNo, 4))  # noqa: E731
+        z = lambda: pinned_zeros((nNo, 4))  # noqa: E731
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.norms = [0.0, 0.0]
         self.time = 0.0
@@ -691,7 +718,7 @@ class PipeFsiSolver:
         inl = np.searchsorted(self.dirF, F["inlet"].gN)
         self.profF[inl] = mesh.inlet_profile
         self.dirM = np.union1d(F["inlet"].gN, F["outlet"].gN).astype(np.int32)
-        z = lambda: np.zeros((nNo, 7))  # noqa: E731
+        z = lambda: pinned_zeros((nNo, 7))  # noqa: E731
         self.Ao, self.Yo, self.Do, self.An, self.Yn, self.Dn = z(), z(), z(), z(), z(), z()
         self.iNorm, self.pNorm = [0.0, 0.0], [0.0, 0.0]
         self.time = 0.0

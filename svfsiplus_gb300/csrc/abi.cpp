@@ -1019,6 +1019,17 @@ const char* svgpu_last_error(const svgpu_ctx* ctx) { return ctx ? ctx->err.c_str
 
 long long svgpu_kernel_launches(const svgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int svgpu_host_alloc(size_t bytes, void** p) {
+  if (!p) return SVGPU_EINVAL;
+  *p = nullptr;
+  return cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocDefault) == cudaSuccess ? SVGPU_OK : SVGPU_ECUDA;
+}
+
+int svgpu_host_free(void* p) {
+  if (!p) return SVGPU_OK;
+  return cudaFreeHost(p) == cudaSuccess ? SVGPU_OK : SVGPU_ECUDA;
+}
+
 int svgpu_set_stream(svgpu_ctx* ctx, void* stream) {
   if (!ctx) return SVGPU_EINVAL;
   cudaStreamSynchronize(ctx->stream);

@@ -176,3 +176,20 @@ def test_history_and_guess_options_checked():
     ctx.history_clear()
     assert ctx.guess_stats == (0, 0, 0)
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_pinned_host_arrays():
+    """Page-locked host arrays (svgpu_host_alloc) start at zero, keep their data, and
+    are freed with their last view."""
+    import gc
+    a = api.pinned_zeros((1000, 4))
+    assert a.shape == (1000, 4) and not a.any()
+    a[:] = 3.0
+    v = a[10:20]
+    del a
+    gc.collect()
+    assert (v == 3.0).all()
+    del v
+    gc.collect()
+    assert api.lib().svgpu_host_free(None) == api.SVGPU_OK
