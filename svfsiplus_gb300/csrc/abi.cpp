@@ -913,7 +913,34 @@ FluidConsts fluid_consts(const svgpu_fluid_props* p) {
   c.am = p->am;
   c.af = p->af;
   c.gam = p->gam;
+  // the double-word residual's constants, split on the host (hi = v rounded to float)
+  const double v[FDW_COUNT] = {c.rho, c.mu, c.kd, c.f0, c.f1, c.f2, c.af * c.gam * c.dt,
+                               c.am / (c.af * c.gam * c.dt), 4.0 / (c.dt * c.dt), 1.0 / 24.0};
+  for (int k = 0; k < FDW_COUNT; k++) {
+    c.dwh[k] = (float)v[k];
+    c.dwl[k] = (float)(v[k] - (double)c.dwh[k]);
+  }
   return c;
+}
+
+// Double-word copies of the node data for the mixed residual, its accumulator zeroed.
+int prepare_dw(svgpu_ctx* ctx, const double* Ag, const double* Yg, DwState& d) {
+  MeshData& m = *ctx->mesh;
+  const long n4 = 4L * ctx->nNo;
+  if (m.x4w.n != (size_t)n4) {
+    SVGPU_CUDA(ctx, m.x4w.resize(n4));
+    launch_to_dw(ctx->stream, n4, m.x4.p, m.x4w.p);
+    ctx->launches++;
+  }
+  SVGPU_CUDA(ctx, ctx->Agw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Ygw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Rw.resize(n4));
+  launch_to_dw(ctx->stream, n4, Ag, ctx->Agw.p);
+  launch_to_dw(ctx->stream, n4, Yg, ctx->Ygw.p);
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Rw.p, 0, n4 * sizeof(float2), ctx->stream));
+  ctx->launches += 2;
+  d = DwState{m.x4w.p, ctx->Agw.p, ctx->Ygw.p, ctx->Rw.p};
+  return SVGPU_OK;
 }
 
 int check_errflag(svgpu_ctx* ctx) {
@@ -930,10 +957,17 @@ int assemble_fluid_device(svgpu_ctx* ctx, const svgpu_fluid_props* props, const 
                           const double* Bf, double* R, double* Val64, float* Val32, int precision) {
   MeshData& m = *ctx->mesh;
   FluidConsts c = fluid_consts(props);
+  DwState dws{nullptr, nullptr, nullptr, nullptr};
+  int rc;
+  if (precision != SVGPU_FP64 && (rc = prepare_dw(ctx, Ag, Yg, dws))) return rc;
   for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
     launch_fluid_assembly(ctx->stream, precision, c, m.color_start[k], m.color_start[k + 1] - m.color_start[k],
                           m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, Ag, Yg, Bf, ctx->rowPtr.p, R, Val64, Val32,
-                          ctx->errflag.p);
+                          ctx->errflag.p, &dws);
+    ctx->launches += precision == SVGPU_FP64 ? 1 : 2;
+  }
+  if (precision != SVGPU_FP64) {  // R += the double-word rows
+    launch_add_dw(ctx->stream, 4L * ctx->nNo, dws.R, R);
     ctx->launches++;
   }
   return SVGPU_OK;
@@ -1724,12 +1758,15 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
       MeshData& m = *ctx->mesh;
       const FluidConsts fc = fluid_consts(props);
+      DwState dws;
+      if ((rc = prepare_dw(ctx, ctx->Ag.p, ctx->Yg.p, dws))) return rc;
       for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
         launch_fluid_residual(ctx->stream, fc, m.color_start[k], m.color_start[k + 1] - m.color_start[k], m.ien.p,
-                              m.boff.p, m.elem_id.p, m.x4.p, ctx->Ag.p, ctx->Yg.p, nullptr, ctx->rowPtr.p, ctx->R.p,
-                              ctx->errflag.p);
+                              m.boff.p, m.elem_id.p, nullptr, ctx->errflag.p, dws);
         ctx->launches++;
       }
+      launch_add_dw(ctx->stream, 4L * ctx->nNo, dws.R, ctx->R.p);
+      ctx->launches++;
       if ((rc = check_errflag(ctx))) return rc;
     } else if ((rc = svgpu_construct_fluid(ctx, props, ctx->Ag.p, ctx->Yg.p, nullptr, nullptr, nullptr,
                                            opts->precision))) {

@@ -101,6 +101,7 @@ struct MeshData {
   DevBuf<int> ien;       // (4, nEl), elements permuted into colour order
   DevBuf<int> elem_id;   // original element id of each permuted element
   DevBuf<double> x4;     // (4, nNo): x, y, z, 0 -- 32-byte aligned node records
+  DevBuf<float2> x4w;    // the same as double words (the mixed residual)
   DevBuf<uint8_t> boff;  // (nEl, 16) offset of block (a,b) within row ien[a]
   std::vector<int> color_start;  // nColors + 1
   // per colour: fluid elements [color_start[k], split_fluid[k]), solid elements
@@ -285,6 +286,7 @@ struct svgpu_ctx {
   svgpu::DevBuf<float> Val32;
   bool resident_mixed = false;  // the resident tangent is Val32
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
+  svgpu::DevBuf<float2> Agw, Ygw, Rw;  // double-word copies for the mixed residual
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
   svgpu::PhaseTimer phases;
@@ -486,22 +488,38 @@ void launch_start_vector32(cudaStream_t s, long n, const double* r, const double
                            int* flags);
 
 // ---- k_fluid.cu ----------------------------------------------------------------
+// Constants of the fluid integrand; dwh/dwl hold the double-word (hi + lo float)
+// split of those the double-word residual kernel uses (filled by fluid_consts).
+enum FluidDw { FDW_RHO, FDW_MU, FDW_KD, FDW_F0, FDW_F1, FDW_F2, FDW_T1C, FDW_AMD, FDW_KT, FDW_W24, FDW_COUNT };
 struct FluidConsts {
   double rho, mu, f0, f1, f2, kd, beta_bf, dt, am, af, gam;
+  float dwh[FDW_COUNT], dwl[FDW_COUNT];
 };
+// Node data of the double-word residual kernel, (hi, lo) float pairs in the layout of
+// the FP64 arrays: coordinates x4 (4, nNo), Ag, Yg (4, nNo), and its residual R
+// (4, nNo), accumulated over the colours and then added to the FP64 R.
+struct DwState {
+  const float2* x4;
+  const float2* Ag;
+  const float2* Yg;
+  float2* R;
+};
+void launch_to_dw(cudaStream_t s, long n, const double* a, float2* b);
+void launch_add_dw(cudaStream_t s, long n, const float2* a, double* b);
 // FP64 fluid elements of the FSI equation (ALE: state arrays with ld rows per node)
 void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
                                const uint8_t* boff, const int* elem_id, const double* x4, int ld, const double* Ag,
                                const double* Yg, const double* Dg, const double* Bf, const int* rowPtr, double* R,
                                double* Val64, int* errflag);
+// precision SVGPU_MIXED: residual rows in double-word arithmetic into dws.R (dws must
+// be set), tangent in FP32 into Val32
 void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, int e0, int ne,
                            const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
                            const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,
-                           double* R, double* Val64, float* Val32, int* errflag);
-// FP64 residual rows only (the mixed path's Newton iterations that keep the tangent)
+                           double* R, double* Val64, float* Val32, int* errflag, const DwState* dws);
+// double-word residual rows only into dws.R (the mixed path's Newton iterations that keep the tangent)
 void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
-                           const int* elem_id, const double* x4, const double* Ag, const double* Yg, const double* Bf,
-                           const int* rowPtr, double* R, int* errflag);
+                           const int* elem_id, const double* Bf, int* errflag, const DwState& dws);
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
                          const int* fien, const int* inner, const uint8_t* boff, const double* x4,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32);

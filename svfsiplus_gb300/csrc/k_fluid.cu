@@ -15,6 +15,8 @@
 // Scatter: elements arrive grouped by colour (no two elements of a colour share a
 // node), so the read-modify-write of R and Val needs no atomics and is deterministic.
 // The position of block (a,b) is rowPtr[ien[a]] + boff[e][a*4+b] (precomputed).
+#include <type_traits>
+
 #include "dword.h"
 #include "internal.h"
 
@@ -22,12 +24,28 @@ namespace svgpu {
 
 namespace {
 
+template <typename T>
+constexpr bool kIsDw = std::is_same<T, dwf::dw>::value;
+
+// A constant of the integrand in the arithmetic type: the double-word split prepared
+// on the host for T = dw (no FP64 operation in the kernel), a conversion otherwise.
+template <typename T>
+__device__ __forceinline__ T cst(const FluidConsts& c, int k, double v) {
+  if constexpr (kIsDw<T>)
+    return dwf::dw(c.dwh[k], c.dwl[k]);
+  else
+    return (T)v;
+}
+
+// A double-word value from a (hi, lo) pair
+__device__ __forceinline__ dwf::dw dwv(float h, float l) { return dwf::dw(h, l); }
+
 // utils::is_zero(v, 0) (utils.cpp:170-189): |v| / max(|v|, eps) < 10 eps.  With eps =
 // 2^-52 the division is an exact power-of-two scaling, so the test is exactly
 // |v| < 10 * 2^-104, which needs no FP64 division (and no FP64 at all for T = float).
 template <typename T>
 __device__ __forceinline__ bool is_zero_ref(T v) {
-  return fabs(v) < (T)4.930380657631324e-31;  // 10 * 2^-104, exact in float and double
+  return fabs(v) < (T)4.930380657631324e-31f;  // 10 * 2^-104 = 5 * 2^-103, exact in float
 }
 
 template <typename T>
@@ -36,20 +54,31 @@ struct Tet4Quad {
   T SN;       // sum_g N_g(a): the same for every a
 };
 
+// a double's value as T; for T = dw the split of a compile-time constant (folded)
+template <typename T>
+__device__ __forceinline__ T from_const(double v) {
+  if constexpr (kIsDw<T>) {
+    const float h = (float)v;
+    return dwf::dw(h, (float)(v - (double)h));
+  } else {
+    return (T)v;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void tet4_quad(Tet4Quad<T>& q) {
   // nn_elem_gip.h:501-515 with qmTET4 = (5 + 3 sqrt 5)/20 (ComMod.h:1011)
-  const double s = (5.0 + 3.0 * 2.23606797749978969640917366873) / 20.0;
-  const double t = (1.0 - s) / 3.0;
-  const double xi[4][3] = {{s, t, t}, {t, s, t}, {t, t, s}, {t, t, t}};
+  constexpr double s = (5.0 + 3.0 * 2.23606797749978969640917366873) / 20.0;
+  constexpr double t = (1.0 - s) / 3.0;
+  constexpr double xi[4][3] = {{s, t, t}, {t, s, t}, {t, t, s}, {t, t, t}};
 #pragma unroll
   for (int g = 0; g < 4; g++) {
-    q.N[g][0] = (T)xi[g][0];
-    q.N[g][1] = (T)xi[g][1];
-    q.N[g][2] = (T)xi[g][2];
-    q.N[g][3] = (T)(1.0 - xi[g][0] - xi[g][1] - xi[g][2]);
+    q.N[g][0] = from_const<T>(xi[g][0]);
+    q.N[g][1] = from_const<T>(xi[g][1]);
+    q.N[g][2] = from_const<T>(xi[g][2]);
+    q.N[g][3] = from_const<T>(1.0 - xi[g][0] - xi[g][1] - xi[g][2]);
   }
-  q.SN = (T)(s + 3.0 * t);
+  q.SN = from_const<T>(s + 3.0 * t);
 }
 
 template <typename TV>
@@ -100,7 +129,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
                                                        const int* __restrict__ rowPtr,
                                                        double* __restrict__ R, TV* __restrict__ Val,
                                                        int* __restrict__ errflag, int ld,
-                                                       const double* __restrict__ Dg) {
+                                                       const double* __restrict__ Dg, DwState dws) {
   const int le = blockIdx.x * blockDim.x + threadIdx.x;
   if (le >= ne) return;
   const int e = e0 + le;
@@ -112,7 +141,26 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
   T xl[4][3], al[4][3], yl[4][4];
   T ym[ALE ? 4 : 1][3];  // mesh velocity
 #pragma unroll
-  for (int a = 0; a < 4; a++) {
+  for (int a = 0; a < 4 && kIsDw<T>; a++) {
+    // double words straight from their (hi, lo) copies: no FP64 operation
+    const float4* xw = reinterpret_cast<const float4*>(dws.x4 + 4L * nd[a]);
+    const float4* aw = reinterpret_cast<const float4*>(dws.Ag + 4L * nd[a]);
+    const float4* yw = reinterpret_cast<const float4*>(dws.Yg + 4L * nd[a]);
+    const float4 x01 = xw[0], x23 = xw[1], a01 = aw[0], a23 = aw[1], y01 = yw[0], y23 = yw[1];
+    if constexpr (kIsDw<T>) {
+      xl[a][0] = dwv(x01.x, x01.y); xl[a][1] = dwv(x01.z, x01.w); xl[a][2] = dwv(x23.x, x23.y);
+      al[a][0] = dwv(a01.x, a01.y); al[a][1] = dwv(a01.z, a01.w); al[a][2] = dwv(a23.x, a23.y);
+      if (Bf) {
+        al[a][0] = al[a][0] - (T)Bf[3L * nd[a]];
+        al[a][1] = al[a][1] - (T)Bf[3L * nd[a] + 1];
+        al[a][2] = al[a][2] - (T)Bf[3L * nd[a] + 2];
+      }
+      yl[a][0] = dwv(y01.x, y01.y); yl[a][1] = dwv(y01.z, y01.w);
+      yl[a][2] = dwv(y23.x, y23.y); yl[a][3] = dwv(y23.z, y23.w);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4 && !kIsDw<T>; a++) {
     const double2 x01 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a]);
     const double2 x23 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a] + 2);
     double b0 = 0.0, b1 = 0.0, b2 = 0.0;
@@ -175,13 +223,13 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
     Nx[k][3] = -(xiX[0][k] + xiX[1][k] + xiX[2][k]);
   }
 
-  const T rho = (T)c.rho, mu = (T)c.mu, kd = (T)c.kd;
-  const T T1c = (T)(c.af * c.gam * c.dt);
-  const T amd = (T)(c.am / (c.af * c.gam * c.dt));
-  const T w = Jac * (T)(1.0 / 24.0);
+  const T rho = cst<T>(c, FDW_RHO, c.rho), mu = cst<T>(c, FDW_MU, c.mu), kd = cst<T>(c, FDW_KD, c.kd);
+  const T T1c = cst<T>(c, FDW_T1C, c.af * c.gam * c.dt);
+  const T amd = cst<T>(c, FDW_AMD, c.am / (c.af * c.gam * c.dt));
+  const T w = Jac * cst<T>(c, FDW_W24, 1.0 / 24.0);
   const T wl = w * T1c;
   // tauM pieces that do not depend on the Gauss point (fluid.cpp:1924-1941)
-  const T kT = (T)(4.0 / (c.dt * c.dt)) + (kd * mu / rho) * (kd * mu / rho);
+  const T kT = cst<T>(c, FDW_KT, 4.0 / (c.dt * c.dt)) + (kd * mu / rho) * (kd * mu / rho);
   T kS = 0;
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -210,7 +258,8 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
   for (int g = 0; g < 4; g++) {
     const T* N = q.N[g];
     // kinematics at the Gauss point (fluid.cpp:1745-1790)
-    T ud[3] = {(T)-c.f0, (T)-c.f1, (T)-c.f2}, u[3] = {0, 0, 0}, ux[3][3], p = 0, px[3] = {0, 0, 0};
+    T ud[3] = {-cst<T>(c, FDW_F0, c.f0), -cst<T>(c, FDW_F1, c.f1), -cst<T>(c, FDW_F2, c.f2)}, u[3] = {0, 0, 0},
+      ux[3][3], p = 0, px[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < 3; k++) ux[k][0] = ux[k][1] = ux[k][2] = 0;
 #pragma unroll
@@ -252,7 +301,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
     for (int i = 0; i < 3; i++)
 #pragma unroll
       for (int j = 0; j < 3; j++) tauB += up[i] * up[j] * K[i][j];
-    if (is_zero_ref(tauB)) tauB = (T)2.220446049250313e-16;
+    if (is_zero_ref(tauB)) tauB = (T)2.220446049250313e-16f;  // 2^-52, exact in float
     tauB = rho / sqrt(tauB);
     const T ua[3] = {u[0] + up[0], u[1] + up[1], u[2] + up[2]};
     const T pa = p - tauC * divU;
@@ -304,7 +353,22 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 
   // residual rows (lR, fluid.cpp:2038-2040, 1658-1660)
 #pragma unroll
-  for (int a = 0; a < 4 && WR; a++) {
+  for (int a = 0; a < 4 && WR && kIsDw<T>; a++) {
+    if constexpr (kIsDw<T>) {  // double-word rows into dws.R (colour order: no conflicts)
+      float4* Ra = reinterpret_cast<float4*>(dws.R + 4L * nd[a]);
+      const T r0 = w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]);
+      const T r1 = w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]);
+      const T r2 = w * (RV[a][2] + Nx[0][a] * RM[0][2] + Nx[1][a] * RM[1][2] + Nx[2][a] * RM[2][2]);
+      const T r3 = w * RC[a];
+      float4 v01 = Ra[0], v23 = Ra[1];
+      const T s0 = dwv(v01.x, v01.y) + r0, s1 = dwv(v01.z, v01.w) + r1;
+      const T s2 = dwv(v23.x, v23.y) + r2, s3 = dwv(v23.z, v23.w) + r3;
+      Ra[0] = make_float4(s0.hi, s0.lo, s1.hi, s1.lo);
+      Ra[1] = make_float4(s2.hi, s2.lo, s3.hi, s3.lo);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4 && WR && !kIsDw<T>; a++) {
     double* Ra = R + 4L * nd[a];
     double r0 = (double)(w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]));
     double r1 = (double)(w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]));
@@ -480,29 +544,54 @@ __global__ void f64_to_f32_kernel(long n, const double* __restrict__ a, float* _
 void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, int e0, int ne,
                            const int* ien, const uint8_t* boff, const int* elem_id, const double* x4,
                            const double* Ag, const double* Yg, const double* Bf, const int* rowPtr,
-                           double* R, double* Val64, float* Val32, int* errflag) {
+                           double* R, double* Val64, float* Val32, int* errflag, const DwState* dws) {
   if (ne <= 0) return;
   const int block = 128;
   const int grid = (ne + block - 1) / block;
+  const DwState none{nullptr, nullptr, nullptr, nullptr};
   if (precision == SVGPU_FP64) {
     fluid_p1_kernel<double, double, true, true, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr);
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr, none);
   } else {
-    // residual rows in double-word FP32 (about 48 bits, accumulated into the FP64 R),
-    // tangent blocks in FP32
+    // residual rows in double-word FP32 (about 48 bits) into dws->R, tangent blocks in FP32
     fluid_p1_kernel<dwf::dw, double, true, false, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr, *dws);
     fluid_p1_kernel<float, float, false, true, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr);
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr, none);
   }
 }
 
 void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
-                           const int* elem_id, const double* x4, const double* Ag, const double* Yg, const double* Bf,
-                           const int* rowPtr, double* R, int* errflag) {
+                           const int* elem_id, const double* Bf, int* errflag, const DwState& dws) {
   if (ne <= 0) return;
   fluid_p1_kernel<dwf::dw, double, true, false, false><<<(ne + 127) / 128, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr);
+      c, e0, ne, ien, boff, elem_id, nullptr, nullptr, nullptr, Bf, nullptr, nullptr, nullptr, errflag, 4, nullptr,
+      dws);
+}
+
+namespace {
+__global__ void to_dw_kernel(long n, const double* __restrict__ a, float2* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = a[i];
+    const float h = __double2float_rn(v);
+    b[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
+__global__ void add_dw_kernel(long n, const float2* __restrict__ a, double* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const float2 v = a[i];
+    b[i] += (double)v.x + (double)v.y;
+  }
+}
+}  // namespace
+
+void launch_to_dw(cudaStream_t s, long n, const double* a, float2* b) {
+  to_dw_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, b);
+}
+
+void launch_add_dw(cudaStream_t s, long n, const float2* a, double* b) {
+  add_dw_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, a, b);
 }
 
 void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
@@ -511,7 +600,8 @@ void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int
                                double* Val64, int* errflag) {
   if (ne <= 0) return;
   fluid_p1_kernel<double, double, true, true, true><<<(ne + 127) / 128, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, ld, Dg);
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, ld, Dg,
+      DwState{nullptr, nullptr, nullptr, nullptr});
 }
 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
