@@ -519,6 +519,7 @@ def run_ours(args):
         "e2e": {"value": e2e_s / args.steps, "unit": "s/time step", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "krylov_iters": [q["itr"] for st in e2e_stats for q in st]},
         "gpu_launches": launches,
+        "gpu_launches_before_timed": launches0,
         "roofline": roof,
         "clocks": clk.summary(),
         "setup_s": setup_s,
@@ -835,7 +836,8 @@ def run_increments(args):
 
 def run_gnn_time(args):
     """The network's forward pass (svgpu_gnn_apply with a prior, device arrays) on the
-    workload's graph: CUDA events over repeated calls after two warm-up calls."""
+    workload's graph: CUDA events over repeated calls after two warm-up calls; then the
+    time of one training step (svgpu_gnn_train, host clock around synchronised calls)."""
     import torch
     from svfsiplus_gb300 import api
     from svfsiplus_gb300.mesh import named_pipe
@@ -861,8 +863,17 @@ def run_gnn_time(args):
         api.lib().svgpu_gnn_apply(ctx._h, ptr(r), ptr(pr), ptr(z))
     e1.record()
     torch.cuda.synchronize()
+    apply_ms = e0.elapsed_time(e1) / args.steps
+    # one Adam step (forward with saved activations, loss, backward, update) on a stored triple
+    x = r.cpu().numpy().reshape(-1, 4)
+    ctx.gnn_add_pair(x, 0.9 * x + 0.1, pr.cpu().numpy().reshape(-1, 4))
+    ctx.gnn_train(2, 1e-4)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    ctx.gnn_train(args.steps, 1e-4)
+    train_ms = (time.perf_counter() - t) * 1e3 / args.steps
     print(json.dumps({"workload": args.workload, "nodes": mesh.nNo, "blocks": int(colPtr.size),
-                      "gnn_apply_ms": e0.elapsed_time(e1) / args.steps, "calls": args.steps}), flush=True)
+                      "gnn_apply_ms": apply_ms, "gnn_train_step_ms": train_ms, "calls": args.steps}), flush=True)
     ctx.close()
 
 

@@ -268,8 +268,11 @@ __global__ void gnn_loss_final_kernel(int nparts, const double* __restrict__ par
 }
 
 // d_out = 2 (out - t) / E ; decoder backward: dh3 = Wd d_out (FP32), and the
-// per-CTA partial of dWd = sum_i h_i d_out_i^T, dbd = sum d_out.
-__global__ void __launch_bounds__(128) gnn_decode_bwd_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
+// per-CTA partial of dWd = sum_i h_i d_out_i^T, dbd = sum d_out.  Tiles of 32 nodes:
+// the tile's d_out (32 x 4) and h (32 x 64) in shared memory; thread (k, c) keeps its
+// entry of dWd in a register over all of its CTA's tiles (no atomics).
+constexpr int DB_NODES = 32;
+__global__ void __launch_bounds__(256) gnn_decode_bwd_kernel(int nNo, const __nv_bfloat16* __restrict__ h,
                                                              const float* __restrict__ out,
                                                              const float* __restrict__ tgt,
                                                              const float* __restrict__ prior,
@@ -277,31 +280,47 @@ __global__ void __launch_bounds__(128) gnn_decode_bwd_kernel(int nNo, const __nv
                                                              const double* __restrict__ loss,
                                                              const __nv_bfloat16* __restrict__ P,
                                                              float* __restrict__ dh, float* __restrict__ gpart) {
-  __shared__ float g[H * 4 + 4];
-  for (int k = threadIdx.x; k < H * 4 + 4; k += blockDim.x) g[k] = 0.f;
-  __syncthreads();
+  __shared__ float D[DB_NODES][4];
+  __shared__ float Hs[DB_NODES][H + 1];
+  __shared__ float Wd[H][4];
+  const int t = threadIdx.x, kk = t >> 2, cc = t & 3;  // 256 threads = 64 x 4 entries of dWd
+  Wd[kk][cc] = bf(P[OFF_WD + kk * 4 + cc]);
   const float inv = (float)(1.0 / sc[2]);
   const float scale = (float)(2.0 / loss[1]);
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nNo; i += (long)gridDim.x * blockDim.x) {
-    float d[4];
-#pragma unroll
-    for (int c = 0; c < 4; c++) d[c] = scale * (out[4 * i + c] - gnn_target(tgt, prior, 4 * i + c, inv));
-    const __nv_bfloat16* hi = h + (long)H * i;
-    for (int k = 0; k < H; k++) {
-      const float hk = bf(hi[k]);
-      float acc = 0.f;
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        acc = fmaf(bf(P[OFF_WD + k * 4 + c]), d[c], acc);
-        atomicAdd(&g[k * 4 + c], hk * d[c]);
-      }
-      dh[(long)H * i + k] = acc;
+  float g = 0.f, gb = 0.f;
+  const int tiles = (nNo + DB_NODES - 1) / DB_NODES;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long i0 = (long)tile * DB_NODES;
+    __syncthreads();
+    if (t < DB_NODES * 4) {
+      const int q = t >> 2, c = t & 3;
+      const long i = i0 + q;
+      D[q][c] = i < nNo ? scale * (out[4 * i + c] - gnn_target(tgt, prior, 4 * i + c, inv)) : 0.f;
     }
+    for (int idx = t; idx < DB_NODES * H; idx += blockDim.x) {
+      const int q = idx / H, k = idx % H;
+      const long i = i0 + q;
+      Hs[q][k] = i < nNo ? bf(h[H * i + k]) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int q = 0; q < DB_NODES; q++) g = fmaf(Hs[q][kk], D[q][cc], g);
+    if (kk == 0)
+      for (int q = 0; q < DB_NODES; q++) gb += D[q][cc];
+    for (int idx = t; idx < DB_NODES * H; idx += blockDim.x) {
+      const int q = idx / H, k = idx % H;
+      const long i = i0 + q;
+      if (i < nNo) {
+        float acc = 0.f;
 #pragma unroll
-    for (int c = 0; c < 4; c++) atomicAdd(&g[H * 4 + c], d[c]);
+        for (int c = 0; c < 4; c++) acc = fmaf(Wd[k][c], D[q][c], acc);
+        dh[H * i + k] = acc;
+      }
+    }
   }
-  __syncthreads();
-  for (int k = threadIdx.x; k < H * 4 + 4; k += blockDim.x) gpart[(long)blockIdx.x * (H * 4 + 4) + k] = g[k];
+  float* gp = gpart + (long)blockIdx.x * (H * 4 + 4);
+  gp[kk * 4 + cc] = g;
+  if (kk == 0) gp[H * 4 + cc] = gb;
 }
 
 // ---- message-passing layer backward, dense part.  dh (FP32, gradient of the
@@ -316,7 +335,7 @@ __global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __r
                                                          float* __restrict__ dms, float* __restrict__ gpart) {
   __shared__ float X[MP_NODES][2 * H + 1];
   __shared__ float DZ[MP_NODES][H + 1];
-  __shared__ float W[2 * H][H];
+  __shared__ float W[2 * H][H + 1];  // padded: the 8 rows one warp reads at a time sit in 8 banks
   const __nv_bfloat16* Wg = P + off_w(layer);
   for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) W[k / H][k % H] = bf(Wg[k]);
   // each thread owns 64 entries of the 128 x 64 weight gradient (+ bias share)
@@ -343,13 +362,13 @@ __global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __r
       DZ[q][f] = dz;
     }
     __syncthreads();
-    // d[h;m] = W dz: thread -> node q = t / 8, features (t % 8) * 16 .. +15
+    // d[h;m] = W dz: thread -> node q = t / 8, features r = 8 j + t % 8, j = 0..15
     {
       const int q = threadIdx.x >> 3, part = threadIdx.x & 7;
       const int i = node0 + q;
       if (i < nNo) {
         const float invdeg = 1.f / (float)(rowPtr[i + 1] - rowPtr[i]);
-        for (int r = part * 16; r < part * 16 + 16; r++) {
+        for (int r = part; r < 2 * H; r += 8) {
           float acc = 0.f;
 #pragma unroll 8
           for (int c = 0; c < H; c++) acc = fmaf(W[r][c], DZ[q][c], acc);
@@ -399,21 +418,23 @@ __global__ void __launch_bounds__(256) gnn_scatter_bwd_kernel(int nNo, const int
   reinterpret_cast<float2*>(dprev + (long)H * j)[lane] = acc;
 }
 
-// encoder backward: dz0 = dh0 * relu'; dW0 partial = x^T dz0, db0 = sum dz0
-__global__ void __launch_bounds__(64) gnn_encode_bwd_kernel(int nNo, const float* __restrict__ in_r,
-                                                            const float* __restrict__ in_p,
-                                                            const float* __restrict__ stat,
-                                                            const double* __restrict__ sc,
-                                                            const uint64_t* __restrict__ mask,
-                                                            const float* __restrict__ dh, float* __restrict__ gpart) {
-  // thread c (0..63) owns column c of W0 (NIN entries) and b0[c]
-  const int c = threadIdx.x;
+// encoder backward: dz0 = dh0 * relu'; dW0 partial = x^T dz0, db0 = sum dz0.
+// 256 threads: four node groups x 64 columns; thread (group, c) owns column c of W0
+// (NIN entries) and b0[c] for its group's nodes; the groups are summed in a fixed order.
+__global__ void __launch_bounds__(256) gnn_encode_bwd_kernel(int nNo, const float* __restrict__ in_r,
+                                                             const float* __restrict__ in_p,
+                                                             const float* __restrict__ stat,
+                                                             const double* __restrict__ sc,
+                                                             const uint64_t* __restrict__ mask,
+                                                             const float* __restrict__ dh, float* __restrict__ gpart) {
+  __shared__ float red[4][NIN + 1][H];
+  const int c = threadIdx.x & (H - 1), grp = threadIdx.x >> 6;
   float g[NIN + 1];
 #pragma unroll
   for (int k = 0; k <= NIN; k++) g[k] = 0.f;
   const float inv = (float)(1.0 / sc[0]);
   const float cp = (float)sc[1];
-  for (long i = blockIdx.x; i < nNo; i += gridDim.x) {
+  for (long i = (long)blockIdx.x * 4 + grp; i < nNo; i += (long)gridDim.x * 4) {
     const uint64_t m = mask[i];
     if (!((m >> c) & 1ull)) continue;
     const float dz = dh[(long)H * i + c];
@@ -427,10 +448,17 @@ __global__ void __launch_bounds__(64) gnn_encode_bwd_kernel(int nNo, const float
     for (int k = 0; k < 4; k++) g[8 + k] = fmaf(stat[4 * i + k], dz, g[8 + k]);
     g[NIN] += dz;
   }
-  float* gp = gpart + (long)blockIdx.x * (NIN * H + H);
 #pragma unroll
-  for (int k = 0; k < NIN; k++) gp[k * H + c] = g[k];
-  gp[NIN * H + c] = g[NIN];
+  for (int k = 0; k <= NIN; k++) red[grp][k][c] = g[k];
+  __syncthreads();
+  if (grp == 0) {
+    float* gp = gpart + (long)blockIdx.x * (NIN * H + H);
+#pragma unroll
+    for (int k = 0; k <= NIN; k++) {
+      const float v = ((red[0][k][c] + red[1][k][c]) + red[2][k][c]) + red[3][k][c];
+      gp[k * H + c] = v;  // k = NIN: the bias b0[c]
+    }
+  }
 }
 
 // grad[off + k] = sum over parts of part[p * stride + k] (fixed order)
@@ -574,12 +602,12 @@ void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr
   gnn_loss_final_kernel<<<1, 32, 0, st>>>(lparts, lossbuf + 2, lossbuf);
   // decoder
   const int dparts = 2 * sm_count;
-  gnn_decode_bwd_kernel<<<dparts, 128, 0, st>>>(nNo, h[3], raw, tgt, p32, sc, lossbuf, P, dA, part);
+  gnn_decode_bwd_kernel<<<dparts, 256, 0, st>>>(nNo, h[3], raw, tgt, p32, sc, lossbuf, P, dA, part);
   gnn_reduce_grad_kernel<<<(H * 4 + 4 + 255) / 256, 256, 0, st>>>(dparts, H * 4 + 4, H * 4 + 4, part, grad + OFF_WD);
   // layers 3..1: dA holds the gradient of the layer output
   float* dcur = dA;
   float* dtmp = dB;
-  const int mparts = 2 * sm_count;
+  const int mparts = 4 * sm_count;
   for (int l = 3; l >= 1; l--) {
     gnn_mp_bwd_kernel<<<mparts, 128, 0, st>>>(nNo, rowPtr, h[l - 1], msave[l], mask, l, P, dcur, dtmp, dC, part);
     gnn_reduce_grad_kernel<<<(LAYER + 255) / 256, 256, 0, st>>>(mparts, LAYER, LAYER, part, grad + off_w(l));
@@ -587,7 +615,7 @@ void gnn_backward(cudaStream_t st, int nNo, const int* rowPtr, const int* colPtr
   }
   // encoder
   const int eparts = 4 * sm_count;
-  gnn_encode_bwd_kernel<<<eparts, 64, 0, st>>>(nNo, r32, p32, stat, sc, mask, dcur, part);
+  gnn_encode_bwd_kernel<<<eparts, 256, 0, st>>>(nNo, r32, p32, stat, sc, mask, dcur, part);
   gnn_reduce_grad_kernel<<<(NIN * H + H + 255) / 256, 256, 0, st>>>(eparts, NIN * H + H, NIN * H + H, part,
                                                                    grad + OFF_W0);
 }
@@ -609,7 +637,7 @@ void gnn_to_bf16(cudaStream_t st, const float* p, __nv_bfloat16* pb) {
 }
 
 size_t gnn_part_floats(int sm_count) {
-  size_t a = (size_t)2 * sm_count * LAYER;
+  size_t a = (size_t)4 * sm_count * LAYER;
   size_t b = (size_t)4 * sm_count * (NIN * H + H);
   size_t c = (size_t)2 * sm_count * (H * 4 + 4);
   return std::max(a, std::max(b, c));
