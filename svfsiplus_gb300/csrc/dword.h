@@ -8,12 +8,16 @@
 //   TwoSum (Knuth, TAOCP vol. 2, 4.2.2): s + e = a + b exactly;
 //   FastTwoSum (Dekker 1971, |a| >= |b|): the same with three operations;
 //   TwoProd with a fused multiply-add: p + e = a * b exactly.
-// Addition follows "AccurateDWPlusDW" and multiplication "DWTimesDW3" of Joldes,
+// Addition follows "SloppyDWPlusDW" and multiplication "DWTimesDW3" of Joldes,
 // Muller and Popescu, "Tight and rigorous error bounds for basic building blocks of
-// double-word arithmetic", ACM TOMS 44(2), 2017 (relative errors below 3 u^2 and
-// 4 u^2, u = 2^-24).  Division and square root take an FP32 first approximation and
-// one correction from the double-word remainder (Newton's method), which leaves a
-// relative error of a few u^2.
+// double-word arithmetic", ACM TOMS 44(2), 2017 (u = 2^-24).  The sloppy sum is exact
+// in its high parts (TwoSum) and rounds only the low-order terms, so its error is
+// below about 3 u^2 (|x| + |y|): relative to the operands, not to the (possibly
+// cancelled) sum, which is the accuracy an assembled residual needs (its terms cancel
+// between elements anyway).  Its relative error is below 3 u^2 when x and y have the
+// same sign.  The multiplication's relative error is below 4 u^2.  Division and square
+// root take an FP32 first approximation and one correction from the double-word
+// remainder (Newton's method), which leaves a relative error of a few u^2.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,14 +50,11 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
 }
 
 __device__ __forceinline__ dw operator+(const dw& x, const dw& y) {
-  float sh, sl, th, tl, vh, vl;
+  float sh, sl;
   two_sum(x.hi, y.hi, sh, sl);
-  two_sum(x.lo, y.lo, th, tl);
-  sl = __fadd_rn(sl, th);
-  fast_two_sum(sh, sl, vh, vl);
-  vl = __fadd_rn(vl, tl);
+  const float w = __fadd_rn(sl, __fadd_rn(x.lo, y.lo));
   dw z;
-  fast_two_sum(vh, vl, z.hi, z.lo);
+  fast_two_sum(sh, w, z.hi, z.lo);
   return z;
 }
 
