@@ -107,6 +107,7 @@ int ensure_krylov(svgpu_ctx* ctx, long n, int sD) {
   SVGPU_CUDA(ctx, kw.Wc.resize(n));
   SVGPU_CUDA(ctx, kw.mask.resize(n));
   SVGPU_CUDA(ctx, kw.tmp.resize(n));
+  SVGPU_CUDA(ctx, kw.xw.resize(n));
   SVGPU_CUDA(ctx, kw.hess.resize((size_t)(sD + 1) * sD));
   SVGPU_CUDA(ctx, kw.givens.resize(5 * (size_t)sD + 3));
   SVGPU_CUDA(ctx, kw.partial.resize((size_t)multidot_ctas(n, ctx->sm_count) * (sD + 2) + 16));
@@ -573,7 +574,7 @@ int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& 
   int rc = SVGPU_OK;
   phase_mark(ctx, PH_GUESS);
   launch_f32_to_f64(s, n, gw.hist[slot].p, gw.g.p);
-  launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.g.p, gw.w1.p);
+  launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.g.p, gw.w1.p, kw.xw.p);
   add_coupled(ctx, 4, gw.g.p, gw.w1.p, nullptr);
   {
     const double* a[2] = {Rs, gw.w1.p};
@@ -581,7 +582,7 @@ int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& 
     launch_guess_dots(s, n, 2, a, b, gw.part.p, ctx->sm_count);
   }
   launch_guess_coef1(s, ctx->sm_count, gw.part.p, gw.coef.p);
-  ctx->launches += 4;
+  ctx->launches += 5;
   if (ctx->gnn && (net || collect)) {
     SVGPU_CUDA(ctx, gw.prior.resize(n));
     launch_scale_f32(s, n, gw.coef.p, gw.hist[slot].p, gw.prior.p);
@@ -624,13 +625,13 @@ int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& 
     gnn_scales(s, n, nullptr, Rs, gw.prior.p, g.nrmp.p, g.scal.p, ctx->sm_count);
     ctx->launches += 2;
     if ((rc = gnn_apply_device(ctx, nullptr, Rs, gw.prior.p, g.scal.p, nullptr, gw.d.p, nullptr))) return rc;
-    launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.d.p, gw.w2.p);
+    launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.d.p, gw.w2.p, kw.xw.p);
     add_coupled(ctx, 4, gw.d.p, gw.w2.p, nullptr);
     const double* a[3] = {Rs, gw.w1.p, gw.w2.p};
     const double* b[3] = {gw.w2.p, gw.w2.p, gw.w2.p};
     launch_guess_dots(s, n, 3, a, b, gw.part.p, ctx->sm_count);
     launch_guess_coef2(s, ctx->sm_count, gw.part.p, gw.coef.p);
-    ctx->launches += 3;
+    ctx->launches += 4;
     d = gw.d.p;
     w2 = gw.w2.p;
   }
@@ -703,10 +704,10 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   for (int l = 0; l < ctx->mItr; l++) {
     phase_mark(ctx, PH_RESTART);
     if (l > 0) {
-      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p, kw.xw.p);
     add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
       launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
-      ctx->launches += 2;
+      ctx->launches += 3;
       nrm = device_norm(ctx, n, kw.r64.p, rc);
       if (rc) return rc;
       if (learned && !(nrm < before)) {
@@ -746,10 +747,10 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     st->itr += std::min(flags[1], sD - 1) + 1;
     if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
     if (l + 1 == ctx->mItr) {  // final true residual
-      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p);
+      launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p, kw.xw.p);
     add_coupled(ctx, 4, kw.X.p, kw.tmp.p, nullptr);
       launch_sub(ctx->stream, n, Rs, kw.tmp.p, kw.r64.p);
-      ctx->launches += 2;
+      ctx->launches += 3;
       nrm = device_norm(ctx, n, kw.r64.p, rc);
       if (rc) return rc;
       st->fNorm = nrm;

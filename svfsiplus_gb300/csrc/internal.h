@@ -120,6 +120,7 @@ struct KrylovWork {
   DevBuf<float> V32;       // FP32 basis of the mixed-precision path
   DevBuf<float> zbasis;    // flexible-GMRES directions Z (sD x n), FP32
   DevBuf<double> X, Wc, mask, tmp, r64, rbak, rsave;
+  DevBuf<float2> xw;       // double-word copy of a vector for the FP32 x FP64 products
   DevBuf<double> hess;     // (sD+1, sD) column-major, + c, s, err, y
   DevBuf<double> givens;   // c[sD], s[sD], err[sD+1], y[sD]
   DevBuf<double> partial;  // per-CTA partial dot products
@@ -459,8 +460,10 @@ void launch_diag_w32(cudaStream_t s, int nNo, const int* diagPtr, const float* V
 void launch_scale_val32(cudaStream_t s, long nnz, const int* blkRow, const int* colPtr, const double* W, float* Val);
 void launch_spmv4_f32(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
                       const float* x, float* y, const int* flags);
+// y = K x, FP32 matrix, FP64 vectors: with a scratch xw (4 nNo float2) in double-word
+// FP32 arithmetic (two launches), without it with FP64 accumulation
 void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
-                          const double* x, double* y);
+                          const double* x, double* y, float2* xw = nullptr);
 int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
                       int sm_count, const int* flags);
 void launch_cgs_update32(cudaStream_t s, long n, int i, float* V, long ldv, const double* hcol, const int* flags);

@@ -9,6 +9,7 @@
 // Every kernel that belongs to an Arnoldi iteration takes the solver's flag word and
 // returns at once when flags[0] (converged) or flags[2] (breakdown) is set, so that a
 // whole restart cycle can be launched as one CUDA graph and stop early on the device.
+#include "dword.h"
 #include "internal.h"
 
 namespace svgpu {
@@ -573,6 +574,47 @@ __global__ void __launch_bounds__(256) spmv4_f32_f64_kernel(int nNo, const int* 
   y[4 * row + r] = acc;
 }
 
+// y = K x with the FP32 matrix and x given as double words (hi, lo floats): every term
+// K_ij x_j is formed exactly in its high part (fused multiply-add) and summed in
+// double-word arithmetic on the FP32 pipes, y written in FP64.  Same accuracy class as
+// FP64 accumulation (errors below a few 2^-48 of sum |K_ij x_j|) without FP64 operations
+// in the loop (GB300's FP64 rate made the FP64 version the slowest product of a step).
+__global__ void __launch_bounds__(256) spmv4_f32_dw_kernel(int nNo, const int* __restrict__ rowPtr,
+                                                           const int* __restrict__ colPtr,
+                                                           const float* __restrict__ Val,
+                                                           const float4* __restrict__ xw, double* __restrict__ y) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long row = t >> 2;
+  const int r = (int)(t & 3);
+  if (row >= nNo) return;
+  const int s = rowPtr[row], e = rowPtr[row + 1];
+  dwf::dw acc(0.f, 0.f);
+  auto term = [&](float v, float xh, float xl) {
+    const float p = __fmul_rn(v, xh);
+    const float q = __fmaf_rn(v, xl, __fmaf_rn(v, xh, -p));  // exact error of v xh, plus v xl
+    acc = acc + dwf::dw(p, q);
+  };
+  for (int k = s; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
+    const float4 x01 = xw[2L * col], x23 = xw[2L * col + 1];  // (x0h, x0l, x1h, x1l), (x2h, ...)
+    term(v.x, x01.x, x01.y);
+    term(v.y, x01.z, x01.w);
+    term(v.z, x23.x, x23.y);
+    term(v.w, x23.z, x23.w);
+  }
+  y[4 * row + r] = (double)acc.hi + (double)acc.lo;
+}
+
+// x -> (hi, lo) float pairs
+__global__ void split_dw_kernel(long n, const double* __restrict__ a, float2* __restrict__ b) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = a[i];
+    const float h = __double2float_rn(v);
+    b[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
 // Partial <V_j, w> over FP32 vectors: FP32 products summed per thread, FP64 across
 // threads and CTAs.
 template <int JB>
@@ -773,8 +815,14 @@ void launch_spmv4_f32(cudaStream_t s, int nNo, const int* rowPtr, const int* col
 }
 
 void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
-                          const double* x, double* y) {
-  spmv4_f32_f64_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y);
+                          const double* x, double* y, float2* xw) {
+  const unsigned grid = (unsigned)((4L * nNo + 255) / 256);
+  if (!xw) {
+    spmv4_f32_f64_kernel<<<grid, 256, 0, s>>>(nNo, rowPtr, colPtr, Val, x, y);
+    return;
+  }
+  split_dw_kernel<<<grid_for(4L * nNo, 256), 256, 0, s>>>(4L * nNo, x, xw);
+  spmv4_f32_dw_kernel<<<grid, 256, 0, s>>>(nNo, rowPtr, colPtr, Val, reinterpret_cast<const float4*>(xw), y);
 }
 
 int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
