@@ -193,9 +193,8 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, 
       amg_spmv_res_h(s, A.n, rp, cp, st.val0h.p, x, b, A.r.p, fl);
       ctx->launches += 2;
     } else {
-      amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);
-      amg_residual(s, 4L * A.n, b, A.r.p, A.r.p, fl);
-      ctx->launches += 3;
+      amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl, b);  // r = b - A x in one pass
+      ctx->launches += 2;
     }
   }
   if (marks) phase_mark(ctx, PH_VC_TRANSFER);

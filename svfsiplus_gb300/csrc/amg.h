@@ -71,7 +71,6 @@ void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h);
 // r = b - A x with an FP16 block matrix
 void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
                     const float* b, float* r, const int* flags);
-void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags);
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags);
 void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x, const int* flags);
@@ -92,7 +91,8 @@ int amg_numeric(svgpu_ctx* ctx, const float* Val0);
 // z = M b on level 0 (FP32 vectors of 4 nNo); enqueued on ctx->stream, capturable;
 // every kernel is skipped once flags (the cycle's flag word, may be null) says stop
 void amg_vcycle(svgpu_ctx* ctx, const float* b, float* z, const int* flags);
+// y = A x, or y = b - A x when b is given
 void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y,
-              const int* flags);
+              const int* flags, const float* b = nullptr);
 
 }  // namespace svgpu

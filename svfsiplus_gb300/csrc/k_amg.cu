@@ -155,12 +155,6 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   *reinterpret_cast<float2*>(r + 4 * row + 2 * q) = make_float2(bb.x - a0, bb.y - a1);
 }
 
-// r = b - Ax; r may be the same array as Ax
-__global__ void residual_kernel(long n4, const float* __restrict__ b, const float* Ax, float* r, const int* flags) {
-  if (stopped(flags)) return;
-  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (long)gridDim.x * blockDim.x)
-    r[k] = b[k] - Ax[k];
-}
 
 __global__ void restrict_kernel(int nc, const int* __restrict__ aggPtr, const int* __restrict__ aggList,
                                 const float* __restrict__ r, float* __restrict__ bc, const int* flags) {
@@ -183,10 +177,11 @@ __global__ void prolong_kernel(int n, const int* __restrict__ agg, const float* 
   x[t] += xc[4L * agg[i] + (t & 3)];
 }
 
+// y = A x, or with b given y = b - A x (the residual fused into the product)
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict__ rowPtr,
                                                    const int* __restrict__ colPtr, const float* __restrict__ val,
                                                    const float* __restrict__ x, float* __restrict__ y,
-                                                   const int* flags) {
+                                                   const int* flags, const float* __restrict__ b) {
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
@@ -221,7 +216,7 @@ __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict_
     acc = fmaf(v.z, xv.z, acc);
     acc = fmaf(v.w, xv.w, acc);
   }
-  y[4 * row + r] = acc;
+  y[4 * row + r] = b ? b[4 * row + r] - acc : acc;
 }
 
 // A P block b, entry e: FP16 of the sum of entry e over the listed fine blocks
@@ -327,9 +322,6 @@ void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr,
       n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, b, r, flags);
 }
 
-void amg_residual(cudaStream_t s, long n4, const float* b, const float* Ax, float* r, const int* flags) {
-  residual_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, b, Ax, r, flags);
-}
 
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags) {
@@ -341,8 +333,8 @@ void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, flo
 }
 
 void amg_spmv(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const float* val, const float* x, float* y,
-              const int* flags) {
-  spmv_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, rowPtr, colPtr, val, x, y, flags);
+              const int* flags, const float* b) {
+  spmv_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, rowPtr, colPtr, val, x, y, flags, b);
 }
 
 }  // namespace svgpu
