@@ -656,8 +656,9 @@ int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& 
 }
 
 // Restarted GMRES with FP32 Arnoldi cycles inside an FP64 defect-correction loop:
-// every restart starts from the residual Rs - K X recomputed with FP64 arithmetic and
-// X accumulates in FP64; the test for convergence uses that FP64 residual.  Same
+// every restart starts from the residual Rs - K X recomputed in FP64 (the product K X
+// summed in double-word FP32 arithmetic, about 48 bits, written in FP64) and X
+// accumulates in FP64; the test for convergence uses that residual.  Same
 // restart structure, tolerances and statistics as gmres_v (gmres.cpp:450-629).
 int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xout, svgpu_ls_stats* st) {
   KrylovWork& kw = ctx->kw;
