@@ -336,7 +336,7 @@ def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newt
 def train_online(api, s):
     """Adam steps on the triples stored so far (none after the first step: it has no
     history); returns (mean loss before, after) over the stored triples or None."""
-    if api.lib().svgpu_gnn_pair_count(s.ctx._h) == 0:
+    if s.ctx.gnn_pair_count() == 0:
         return None
     e0 = s.ctx.gnn_eval()
     s.ctx.gnn_train(TRAIN_ITERS, TRAIN_LR)

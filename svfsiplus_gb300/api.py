@@ -307,11 +307,15 @@ class Context:
         self._check(lib().svgpu_gnn_eval(self._h, C.byref(loss)), "gnn_eval")
         return loss.value
 
+    def gnn_pair_count(self):
+        """How many (residual, prior, increment) triples are stored."""
+        return int(lib().svgpu_gnn_pair_count(self._h))
+
     def gnn_pairs(self):
         """The stored (residual, prior, increment) triples of the scaled system, oldest
         first; the prior is zero where a triple has none."""
         out = []
-        for k in range(lib().svgpu_gnn_pair_count(self._h)):
+        for k in range(self.gnn_pair_count()):
             r, p, x = (np.zeros((self.nNo, 4)) for _ in range(3))
             self._check(lib().svgpu_gnn_get_pair(self._h, k, _ptr(r), _ptr(p), _ptr(x)), "gnn_get_pair")
             out.append((r, p, x))
