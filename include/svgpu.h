@@ -110,22 +110,24 @@ int svgpu_ls_create(svgpu_ctx* ctx, int lsType, double relTol, double absTol, in
 int svgpu_fsils_solve(svgpu_ctx* ctx, int dof, double* Ri, double* Val, int prec,
                       const int* incL, const double* res, svgpu_ls_stats* stats);
 
-/* Allocation-free dot product of two device vectors U, V of dof*nNo entries.  It has
- * no counterpart in the reference: it is the same reduction the solver's Gram-Schmidt
- * and norms use (the value fsils_nc_dot_v, dot.cpp:134-171, computes), for callers
- * that cannot allocate device memory -- code recording a CUDA graph, where cudaMalloc
- * is not permitted during stream capture, or code whose device memory belongs to
- * another allocator or a fixed budget.  It calls no cudaMalloc/cudaFree: its per-CTA
- * partial sums live in a file-scope __device__ array of 4097 doubles (32 KB), held by
- * every GPU that loads the library until the process exits.  Limit: dof*nNo <=
- * 16,777,216 entries, else SVGPU_ETOOBIG.  U and V must be device pointers (else
- * SVGPU_EINVAL); *result may be a device or a host pointer (a host result is copied
- * back and the stream synchronised).  The work runs on `stream` (a cudaStream_t, NULL
- * for the legacy default stream) of the calling thread's current device.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the array and each
- * call overwrites the partial sums it reads, so nothing needs clearing between calls;
- * calls whose kernels overlap on the GPU (unordered streams) race on it. */
+/* Allocation-free dot product of two device vectors U, V of dof*nNo entries, summed
+ * in FP64.  It has no counterpart in the reference.  It is for callers that must not
+ * call cudaMalloc where they need the dot: a host program whose device memory is all
+ * owned by another allocator or held to a fixed budget (a framework's caching
+ * allocator, an embedded solver sharing the GPU), where one more allocation could fail
+ * or fragment that pool.  It calls no cudaMalloc/cudaFree: its per-CTA partial sums
+ * live in a file-scope __device__ array of 4097 doubles (32 KB), held by every GPU that
+ * loads the library until the process exits.  Limit: dof*nNo <= 16,777,216 entries,
+ * else SVGPU_ETOOBIG.  U and V must be device pointers of the current device (else
+ * SVGPU_EINVAL); *result may be a device pointer of the current device or a host
+ * pointer (a host result is copied back and the stream synchronised).  The work runs
+ * on `stream` (a cudaStream_t, NULL for the legacy default stream) of the calling
+ * thread's current device.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and caches it; make that first call before any stream
+ * capture, and do not call this entry point on a device after cudaDeviceReset.  All
+ * calls share the array and each call overwrites the partial sums it reads, so nothing
+ * needs clearing between calls; calls whose kernels overlap on the GPU (unordered
+ * streams) race on it. */
 int svgpu_fsils_dot_noalloc(int dof, int nNo, const double* U, const double* V, double* result,
                             void* stream);
 
@@ -302,8 +304,10 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
  * needed fewer Krylov iterations on average than those without: each is tried twice,
  * then the better one is kept and the other retried every eighth visit); 5 as 2 with
  * the minimal-residual multiple of g alone (no network).
- * Initial guesses and flexible cycles that do not lower the FP64 residual are rejected
- * (plain cycles finish the solve). */
+ * Initial guesses and flexible cycles that do not lower the FP64 residual, or whose
+ * Arnoldi step breaks down (a zero or non-finite preconditioned vector), are rejected:
+ * the solve goes on with the method without the learned part (mode 3: the plain
+ * V-cycle; then, and in the other modes, plain FP32 GMRES cycles). */
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
 /* History of modes 4 and 5: the slot (0..15) whose previous increment the next mixed
  * solves use and replace; svgpu_fluid_step and svgpu_fsi_step set it to the Newton
@@ -347,7 +351,11 @@ int svgpu_phase_times(svgpu_ctx* ctx, double* ms, long long* intervals, int n);
 typedef struct {
   int minItr, maxItr;        /* eqType minItr / maxItr */
   double tol;                /* eqType tol */
-  int precision;             /* SVGPU_FP64 or SVGPU_MIXED */
+  /* SVGPU_FP64: FP64 residual and tangent, solved by the reference's GMRES + diagonal
+   * preconditioner (solver mode 0) or, with a flexible solver mode (1-5, no reference
+   * counterpart), on an FP32 copy of the FP64 tangent inside the FP64 defect
+   * correction; SVGPU_MIXED: double-word FP32 residual rows and an FP32 tangent */
+  int precision;
   int outletFace;            /* face id of the traction-free outlet, -1 for none */
   double outletH;            /* Neumann value on it */
   /* SVGPU_MIXED only, no reference counterpart: 1 assembles the tangent (and the
@@ -373,6 +381,14 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                      const double* Ao, const double* Yo, const double* Do,
                      double* An, double* Yn, double* Dn,
                      double* iNorm, double* pNorm, svgpu_ls_stats* stats);
+
+/* Device time of the last svgpu_fluid_step / svgpu_fsi_step in milliseconds: CUDA
+ * events on the context's stream, the first recorded once the step's inputs are
+ * enqueued to the device, the second before its outputs are copied back.  The host
+ * copies of the inputs and outputs are outside this interval; everything the step
+ * computes is inside it.  No counterpart in the reference (its callD, gmres.cpp:624,
+ * times one solve).  SVGPU_ESTATE if no step has completed since the last failure. */
+int svgpu_step_device_ms(const svgpu_ctx* ctx, double* ms);
 
 /* ---- coupled ALE FSI time step (solver/main.cpp:292-762 with the FSI and mesh
  * equations coupled, as in the reference's fsi/pipe_3d case) ----------------------- */

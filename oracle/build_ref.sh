@@ -8,6 +8,10 @@ HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${1:-/root/reference}"
 SRC="$REF/Code/Source"
 OUT="$HERE/_ref"
+if [ ! -d "$SRC" ]; then
+  echo "no reference tree at $REF: oracle/_ref not built"
+  exit 0
+fi
 mkdir -p "$OUT/obj"
 INC="-I$HERE/refstub -I$SRC/solver -I$SRC/liner_solver -I$REF/Code/ThirdParty/tinyxml/simvascular_tinyxml -I$REF/Code/ThirdParty/eigen/include/eigen3"
 FLAGS="-std=c++17 -O3 -w -include cstring -include stdexcept -include limits"

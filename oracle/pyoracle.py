@@ -16,12 +16,17 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle (gcc, -ffp-contract=off so results match across hosts)."""
+    """Compile the oracle (gcc, -ffp-contract=off so results match across hosts), with
+    OpenMP for the threaded CPU baseline where the compiler has it (one thread, the
+    default, is the reference's sequential order either way)."""
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     src = os.path.join(HERE, "svoracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-shared",
-                        "-o", LIB_PATH, src, "-lm"], check=True)
+    hdr = os.path.join(HERE, "svoracle.h")
+    newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
+        base = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"]
+        if subprocess.run(base[:1] + ["-fopenmp"] + base[1:], capture_output=True).returncode != 0:
+            subprocess.run(base, check=True)
     return LIB_PATH
 
 
@@ -79,7 +84,7 @@ def construct_mesh(E, nu, rho, dt, rho_inf, x, ien, A, D, Do, rowPtr, colPtr):
 class LS(C.Structure):
     _fields_ = [("sD", C.c_int), ("mItr", C.c_int), ("relTol", C.c_double), ("absTol", C.c_double),
                 ("iNorm", C.c_double), ("fNorm", C.c_double), ("dB", C.c_double),
-                ("itr", C.c_int), ("suc", C.c_int)]
+                ("itr", C.c_int), ("suc", C.c_int), ("t_precond", C.c_double), ("t_krylov", C.c_double)]
 
 
 class FluidProblem(C.Structure):
@@ -120,6 +125,37 @@ def fluid_params(rho=1.06, mu=0.04, dt=1e-3, rho_inf=0.5, backflow_beta=0.2, k_i
     lib().or_genalpha_first_order(C.c_double(rho_inf), C.byref(am), C.byref(af), C.byref(gam), C.byref(beta))
     return FluidParams(rho, mu, f[0], f[1], f[2], k_inv_darcy, backflow_beta, dt,
                        am.value, af.value, gam.value, beta.value)
+
+
+def set_threads(n: int) -> int:
+    """Host threads of the oracle's loops (n < 1: every processor); returns the count in
+    use.  1 is the reference's sequential order, bit for bit."""
+    return int(lib().or_set_threads(int(n)))
+
+
+def color_elements(nNo: int, ien: np.ndarray):
+    """Greedy element colouring: (perm, color_start) for construct_fluid_coloured."""
+    ien = np.ascontiguousarray(ien, dtype=np.int32)
+    perm = np.zeros(ien.shape[0], dtype=np.int32)
+    start = np.zeros(129, dtype=np.int32)
+    nc = lib().or_color_elements(int(nNo), int(ien.shape[0]), _p(ien), _p(perm), _p(start))
+    if nc < 0:
+        raise RuntimeError("more than 128 element colours")
+    return perm, start[:nc + 1].copy()
+
+
+def construct_fluid_coloured(P, x, ien, Ag, Yg, rowPtr, colPtr, perm, color_start, R=None, Val=None):
+    """construct_fluid over the elements colour by colour, threads inside a colour."""
+    nNo = x.shape[0]
+    R = np.zeros((nNo, 4)) if R is None else R
+    Val = np.zeros((colPtr.size, 16)) if Val is None else Val
+    x, ien, Ag, Yg = (np.ascontiguousarray(a) for a in (x, ien, Ag, Yg))
+    rc = lib().or_construct_fluid_coloured(C.byref(P), nNo, ien.shape[0], _p(ien), _p(x), _p(Ag), _p(Yg),
+                                           _p(rowPtr), _p(colPtr), _p(R), _p(Val), _p(perm), _p(color_start),
+                                           int(color_start.size - 1))
+    if rc != 0:
+        raise RuntimeError(f"zero Jacobian in element {-1 - rc}")
+    return R, Val
 
 
 def lhsa(nNo: int, ien: np.ndarray):
@@ -181,7 +217,7 @@ def fsils_solve_gmres(rowPtr, colPtr, Val, R, dirMask, sD=50, mItr=100, relTol=1
     nNo = rowPtr.size - 1
     Val = np.array(Val, dtype=np.float64, order="C", copy=True)
     R = np.array(R, dtype=np.float64, order="C", copy=True)
-    ls = LS(sD, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0)
+    ls = LS(sD, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0, 0.0, 0.0)
     mask = None if dirMask is None else _p(np.ascontiguousarray(dirMask, dtype=np.float64))
     lib().or_fsils_solve_gmres(nNo, dof, _p(rowPtr), _p(colPtr), _p(Val), _p(R), mask, C.byref(ls))
     return R, Val, ls
@@ -192,7 +228,7 @@ def fsils_solve_cg(rowPtr, colPtr, Val, R, dirMask, mItr=1000, relTol=1e-2, absT
     nNo = rowPtr.size - 1
     Val = np.array(Val, dtype=np.float64, order="C", copy=True)
     R = np.array(R, dtype=np.float64, order="C", copy=True)
-    ls = LS(0, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0)
+    ls = LS(0, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0, 0.0, 0.0)
     mask = None if dirMask is None else _p(np.ascontiguousarray(dirMask, dtype=np.float64))
     lib().or_fsils_solve_cg(nNo, dof, _p(rowPtr), _p(colPtr), _p(Val), _p(R), mask, C.byref(ls))
     return R, Val, ls
@@ -220,7 +256,7 @@ class FluidRun:
                                _p(self.colPtr).value, self.colPtr.size, self.dir_nodes.size,
                                _p(self.dir_nodes).value, _p(self.dirMask).value,
                                newton_min, newton_max, newton_tol)
-        self.ls = LS(sD, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0)
+        self.ls = LS(sD, mItr, relTol, absTol, 0.0, 0.0, 0.0, 0, 0, 0.0, 0.0)
         self.ns = NewtonState(0.0, 0.0, 0.0, 0.0)
         self.newton_max = newton_max
         z = lambda: np.zeros((nNo, 4))  # noqa: E731

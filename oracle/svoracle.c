@@ -1,7 +1,16 @@
 /* CPU oracle of the fluid Newton-step hot path -- TEST INFRASTRUCTURE ONLY.
  * See svoracle.h.  Compiled with -ffp-contract=off so that results do not depend on
  * whether the host has fused multiply-add; the reference harness it is pinned against
- * is compiled the same way. */
+ * is compiled the same way.
+ *
+ * Host threads (or_set_threads, OpenMP): with one thread (the default) every function
+ * runs the reference's sequential operation order and is bit-exact with it.  With
+ * more threads, the timed CPU baseline's stand-in for the reference's multi-rank run:
+ * block rows of the SpMV, element-wise vector updates and the diagonal scaling are
+ * split over threads without changing any result; dot products sum fixed per-thread
+ * chunks, then the chunk sums in order (deterministic for a given thread count, not
+ * bitwise the reference's); the element loop runs colour by colour
+ * (or_construct_fluid_coloured), elements of one colour sharing no node. */
 #include "svoracle.h"
 
 #include <float.h>
@@ -9,6 +18,23 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 1;
+
+int or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n < 1) n = omp_get_num_procs();
+  g_threads = n;
+#else
+  (void)n;
+  g_threads = 1;
+#endif
+  return g_threads;
+}
+#define PAR_FOR _Pragma("omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)")
 
 /* utils::is_zero(value, 0) (utils.cpp:170-189): true when |value| < 10 eps^2 */
 static int is_zero(double v) {
@@ -375,6 +401,75 @@ int or_construct_fluid(const or_fluid_params* P, int nNo, int nEl, const int* ie
   return 0;
 }
 
+/* Greedy element colouring for the threaded element loop: no two elements of a colour
+ * share a node.  perm (nEl) lists the elements colour by colour, in mesh order inside a
+ * colour; color_start (up to 129 entries) their offsets.  Returns the colour count, or
+ * -1 when an element would need more than 128 colours. */
+int or_color_elements(int nNo, int nEl, const int* ien, int* perm, int* color_start) {
+  unsigned long long* used = (unsigned long long*)calloc((size_t)nNo * 2, sizeof(unsigned long long));
+  unsigned char* col = (unsigned char*)malloc((size_t)(nEl > 0 ? nEl : 1));
+  int count[128] = {0}, ncol = 0;
+  for (int e = 0; e < nEl; e++) {
+    unsigned long long m0 = 0, m1 = 0;
+    for (int a = 0; a < 4; a++) {
+      m0 |= used[2 * (long)ien[4 * e + a]];
+      m1 |= used[2 * (long)ien[4 * e + a] + 1];
+    }
+    int c = -1;
+    for (int b = 0; b < 128 && c < 0; b++)
+      if (!((b < 64 ? m0 >> b : m1 >> (b - 64)) & 1ULL)) c = b;
+    if (c < 0) { free(used); free(col); return -1; }
+    for (int a = 0; a < 4; a++) used[2 * (long)ien[4 * e + a] + (c >= 64)] |= 1ULL << (c & 63);
+    col[e] = (unsigned char)c;
+    count[c]++;
+    if (c + 1 > ncol) ncol = c + 1;
+  }
+  color_start[0] = 0;
+  for (int c = 0; c < ncol; c++) color_start[c + 1] = color_start[c] + count[c];
+  int fill[128];
+  for (int c = 0; c < ncol; c++) fill[c] = color_start[c];
+  for (int e = 0; e < nEl; e++) perm[fill[col[e]]++] = e;
+  free(used);
+  free(col);
+  return ncol;
+}
+
+/* construct_fluid + do_assem over the elements colour by colour, the elements of a
+ * colour split over the host threads (they share no node, so no two threads add into
+ * the same R entry or Val block).  Returns -1 - e for a zero Jacobian in element e. */
+int or_construct_fluid_coloured(const or_fluid_params* P, int nNo, int nEl, const int* ien,
+                                const double* x, const double* Ag, const double* Yg,
+                                const int* rowPtr, const int* colPtr, double* R, double* Val,
+                                const int* perm, const int* color_start, int ncolors) {
+  (void)nNo;
+  (void)nEl;
+  int bad = 0;
+  for (int c = 0; c < ncolors; c++) {
+    PAR_FOR
+    for (int q = color_start[c]; q < color_start[c + 1]; q++) {
+      const int e = perm[q];
+      double xl[12], al[16], yl[16], bfl[12] = {0}, lR[16], lK[256];
+      const int* ptr = ien + 4 * e;
+      for (int a = 0; a < 4; a++) {
+        const int Ac = ptr[a];
+        for (int i = 0; i < 3; i++) xl[3 * a + i] = x[3 * Ac + i];
+        for (int i = 0; i < 4; i++) {
+          al[4 * a + i] = Ag[4 * Ac + i];
+          yl[4 * a + i] = Yg[4 * Ac + i];
+        }
+      }
+      if (or_fluid_element(P, xl, al, yl, bfl, lR, lK) != 0) {
+#pragma omp atomic write
+        bad = -1 - e;
+        continue;
+      }
+      do_assem4(4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    }
+    if (bad) return bad;
+  }
+  return 0;
+}
+
 void or_neu_backflow(const or_fluid_params* P, int nFa, const int* fien, const int* gE,
                      const int* ien, const double* x, const double* Yg, double h,
                      const int* rowPtr, const int* colPtr, double* R, double* Val) {
@@ -447,6 +542,7 @@ void or_spar_mul(int nNo, int dof, const int* rowPtr, const int* colPtr, const d
                  const double* U, double* KU) {
   /* spar_mul.cpp:191-258: KU(l,i) = sum_j sum_k K(l*dof+k, j) U(k, col j) */
   const int d2 = dof * dof;
+  PAR_FOR
   for (int i = 0; i < nNo; i++) {
     for (int l = 0; l < dof; l++) KU[dof * i + l] = 0.0;
     for (int j = rowPtr[i]; j < rowPtr[i + 1]; j++) {
@@ -462,14 +558,66 @@ void or_spar_mul(int nNo, int dof, const int* rowPtr, const int* colPtr, const d
 
 static double dotv(long n, const double* u, const double* v) {
   /* fsils_nc_dot_v (dot.cpp:134-171): one running sum over nodes, dofs inside */
+  if (g_threads > 1) {
+    double part[256];
+    const int T = g_threads < 256 ? g_threads : 256;
+#pragma omp parallel num_threads(T)
+    {
+#ifdef _OPENMP
+      const int t = omp_get_thread_num();
+#else
+      const int t = 0;
+#endif
+      const long b = n * t / T, e = n * (t + 1) / T;
+      double r = 0.0;
+      for (long i = b; i < e; i++) r = r + u[i] * v[i];
+      part[t] = r;
+    }
+    double r = 0.0;
+    for (int t = 0; t < T; t++) r = r + part[t];
+    return r;
+  }
   double r = 0.0;
   for (long i = 0; i < n; i++) r = r + u[i] * v[i];
   return r;
 }
 
+/* out[j] = dotv(n, U + n j, v) for j < m: with threads, one pass over the chunks (the
+ * same chunk sums, combined in the same order, as m calls of dotv) */
+static void multidotv(long n, const double* U, int m, const double* v, double* out) {
+  if (g_threads <= 1) {
+    for (int j = 0; j < m; j++) out[j] = dotv(n, U + n * j, v);
+    return;
+  }
+  const int T = g_threads < 256 ? g_threads : 256;
+  double* part = (double*)malloc(sizeof(double) * (size_t)T * (size_t)m);
+#pragma omp parallel num_threads(T)
+  {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num();
+#else
+    const int t = 0;
+#endif
+    const long b = n * t / T, e = n * (t + 1) / T;
+    for (int j = 0; j < m; j++) {
+      const double* u = U + n * j;
+      double r = 0.0;
+      for (long i = b; i < e; i++) r = r + u[i] * v[i];
+      part[(long)t * m + j] = r;
+    }
+  }
+  for (int j = 0; j < m; j++) {
+    double r = 0.0;
+    for (int t = 0; t < T; t++) r = r + part[(long)t * m + j];
+    out[j] = r;
+  }
+  free(part);
+}
+
 double or_dot(long n, const double* u, const double* v) { return dotv(n, u, v); }
 
 void or_axpy(long n, double r, double* U, const double* V) {
+  PAR_FOR
   for (long k = 0; k < n; k++) U[k] = U[k] + r * V[k];
 }
 
@@ -489,11 +637,13 @@ static double* precond_diag_apply(int nNo, int dof, const int* rowPtr, const int
   for (long i = 0; i < n; i++) if (W[i] == 0.0) W[i] = 1.0;
   for (long i = 0; i < n; i++) W[i] = 1.0 / sqrt(fabs(W[i]));
   if (dirMask) for (long i = 0; i < n; i++) W[i] = W[i] * dirMask[i];
+  PAR_FOR
   for (int a = 0; a < nNo; a++) /* pre_mul (precond.cpp:549-624) */
     for (int k = rowPtr[a]; k < rowPtr[a + 1]; k++)
       for (int r = 0; r < dof; r++)
         for (int c = 0; c < dof; c++) Val[(long)d2 * k + r * dof + c] = Val[(long)d2 * k + r * dof + c] * W[dof * a + r];
   for (long i = 0; i < n; i++) R[i] = W[i] * R[i];
+  PAR_FOR
   for (int a = 0; a < nNo; a++) /* pos_mul (precond.cpp:46-111) */
     for (int k = rowPtr[a]; k < rowPtr[a + 1]; k++) {
       int col = colPtr[k];
@@ -506,7 +656,10 @@ static double* precond_diag_apply(int nNo, int dof, const int* rowPtr, const int
 void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr,
                           double* Val, double* R, const double* dirMask, or_ls* ls) {
   const long n = (long)nNo * dof;
+  const double t0 = now_s();
   double* W = precond_diag_apply(nNo, dof, rowPtr, colPtr, Val, R, dirMask);
+  const double t1 = now_s();
+  ls->t_precond = t1 - t0;
 
   /* gmres_v (gmres.cpp:450-629) */
   const int sD = ls->sD;
@@ -532,8 +685,10 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
       ls->dB = ls->fNorm;
       ls->itr = ls->itr + 1;
       or_spar_mul(nNo, dof, rowPtr, colPtr, Val, X, u);
+      PAR_FOR
       for (long k = 0; k < n; k++) u[k] = R[k] - u[k];
       err[0] = sqrt(dotv(n, u, u));
+      PAR_FOR
       for (long k = 0; k < n; k++) u[k] = u[k] / err[0];
       for (int i = 0; i < sD; i++) {
         ls->itr = ls->itr + 1;
@@ -541,15 +696,18 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
         double* ui = u + n * i;
         double* ui1 = u + n * (i + 1);
         or_spar_mul(nNo, dof, rowPtr, colPtr, Val, ui, ui1);
-        for (int j = 0; j <= i + 1; j++) H(j, i) = dotv(n, u + n * j, ui1);
-        for (int j = 0; j <= i; j++) {
-          const double r = -H(j, i);
-          const double* uj = u + n * j;
-          for (long k = 0; k < n; k++) ui1[k] = ui1[k] + r * uj[k];
-          H(i + 1, i) = H(i + 1, i) - H(j, i) * H(j, i);
+        multidotv(n, u, i + 2, ui1, &H(0, i));
+        /* ui1 -= sum_j H(j,i) u_j, each entry updated in j order (omp_sum_v) */
+        PAR_FOR
+        for (long k = 0; k < n; k++) {
+          double a = ui1[k];
+          for (int j = 0; j <= i; j++) a = a + (-H(j, i)) * u[n * j + k];
+          ui1[k] = a;
         }
+        for (int j = 0; j <= i; j++) H(i + 1, i) = H(i + 1, i) - H(j, i) * H(j, i);
         H(i + 1, i) = sqrt(fabs(H(i + 1, i)));
         const double rinv = 1.0 / H(i + 1, i);
+        PAR_FOR
         for (long k = 0; k < n; k++) ui1[k] = rinv * ui1[k];
         for (int j = 0; j <= i - 1; j++) {
           double tmp = c[j] * H(j, i) + s[j] * H(j + 1, i);
@@ -571,9 +729,11 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
         for (int k = j + 1; k <= last_i; k++) y[j] = y[j] - H(j, k) * y[k];
         y[j] = y[j] / H(j, j);
       }
-      for (int j = 0; j <= last_i; j++) {
-        const double* uj = u + n * j;
-        for (long k = 0; k < n; k++) X[k] = X[k] + y[j] * uj[k];
+      PAR_FOR
+      for (long k = 0; k < n; k++) {
+        double a = X[k];
+        for (int j = 0; j <= last_i; j++) a = a + y[j] * u[n * j + k];
+        X[k] = a;
       }
       ls->fNorm = fabs(err[last_i + 1]);
       if (ls->suc) break;
@@ -584,6 +744,7 @@ void or_fsils_solve_gmres(int nNo, int dof, const int* rowPtr, const int* colPtr
 #undef H
   /* solve.cpp:184-186: R <- Wc * R */
   for (long i = 0; i < n; i++) R[i] = W[i] * R[i];
+  ls->t_krylov = now_s() - t1;
   free(W); free(h); free(X); free(u); free(y); free(c); free(s); free(err);
 }
 

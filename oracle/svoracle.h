@@ -27,6 +27,24 @@ typedef struct {
   double dt, am, af, gam, beta;   /* time step and generalised-alpha constants */
 } or_fluid_params;
 
+/* Host threads of the functions below (OpenMP; n < 1: every processor).  Returns the
+ * count in use: 1 (the default, and always where OpenMP is absent) keeps the
+ * reference's sequential operation order bit for bit.  More threads are for the timed
+ * CPU baseline only: results then agree with the sequential ones to rounding. */
+int or_set_threads(int n);
+
+/* Greedy element colouring (no two elements of a colour share a node) for the
+ * threaded element loop: perm (nEl), color_start (up to 129 ints); returns the colour
+ * count or -1 above 128 colours. */
+int or_color_elements(int nNo, int nEl, const int* ien, int* perm, int* color_start);
+
+/* or_construct_fluid (without body force) over the elements colour by colour, each
+ * colour's elements split over the host threads. */
+int or_construct_fluid_coloured(const or_fluid_params* p, int nNo, int nEl, const int* ien,
+                                const double* x, const double* Ag, const double* Yg,
+                                const int* rowPtr, const int* colPtr, double* R, double* Val,
+                                const int* perm, const int* color_start, int ncolors);
+
 /* generalised-alpha constants of a first-order equation (initialize.cpp:426-465) */
 void or_genalpha_first_order(double rho_inf, double* am, double* af, double* gam, double* beta);
 
@@ -98,6 +116,7 @@ typedef struct {
   /* outputs, the reference's FSILS_subLsType fields (fils_struct.hpp:211-257) */
   double iNorm, fNorm, dB;
   int itr, suc;
+  double t_precond, t_krylov;  /* seconds: precond_diag, the Krylov iterations */
 } or_ls;
 
 /* fsils_solve (solve.cpp:50-193) for GMRES + FSILS diagonal preconditioning with

@@ -392,6 +392,13 @@ class Context:
         return [stats[i].as_dict() for i in range(it)]
 
 
+    def step_device_ms(self):
+        """Device milliseconds of the last fluid/FSI time step, between its inputs'
+        arrival on the device and the copy-back of its outputs (svgpu_step_device_ms)."""
+        ms = C.c_double()
+        self._check(lib().svgpu_step_device_ms(self._h, C.byref(ms)), "step_device_ms")
+        return ms.value
+
     def fsi_step(self, props, opts, dir_fsi, dir_mesh, Ao, Yo, Do, An, Yn, Dn, iNorm, pNorm):
         """svgpu_fsi_step: one coupled FSI + mesh-motion time step.  dir_* are
         (nodes, Y, A) triples; iNorm/pNorm are 2-element lists carried across steps.

@@ -19,6 +19,21 @@ int set_err(svgpu_ctx* ctx, int status, const std::string& msg) {
   return status;
 }
 
+int step_time_mark(svgpu_ctx* ctx, int which) {
+  if (!ctx->step_ev[which]) SVGPU_CUDA(ctx, cudaEventCreate(&ctx->step_ev[which]));
+  SVGPU_CUDA(ctx, cudaEventRecord(ctx->step_ev[which], ctx->stream));
+  return SVGPU_OK;
+}
+
+void step_time_read(svgpu_ctx* ctx) {
+  float ms = -1.f;
+  if (!ctx->step_ev[0] || !ctx->step_ev[1] || cudaEventElapsedTime(&ms, ctx->step_ev[0], ctx->step_ev[1]) != cudaSuccess) {
+    cudaGetLastError();
+    ms = -1.f;
+  }
+  ctx->last_step_ms = ms;
+}
+
 int cuda_fail(svgpu_ctx* ctx, cudaError_t e, const char* what) {
   return set_err(ctx, SVGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -425,17 +440,20 @@ void enqueue_cycle32(svgpu_ctx* ctx, const float* Val32) {
 // Flexible cycle with the learned right preconditioner: z_i = M(u_i) (the network on
 // the unit-norm basis vector without a prior, scale 1/sqrt(n)), u_{i+1} = K z_i, then the same
 // Gram-Schmidt and Givens steps; the solution is updated from the z_i (FGMRES).
-void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
+// kind 2: the network as the preconditioner (mode 1); kind 3: the multilevel V-cycle;
+// kind 4: the V-cycle with the network as finest-level pre-smoother (mode 3).
+void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32, int kind) {
   KrylovWork& kw = ctx->kw;
   const long n = (long)kw.n;
   const int sD = kw.sD;
   double* hraw = kw.givens.p + 4 * sD + 1;
+  if (ctx->amg) ctx->amg->gnn_smoother = kind == 4 && ctx->gnn;
   for (int i = 0; i < sD; i++) {
     float* ui = kw.V32.p + (long)i * n;
     float* ui1 = kw.V32.p + (long)(i + 1) * n;
     float* zi = kw.zbasis.p + (long)i * n;
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_PRECOND);
-    if (ctx->learned_mode == 1)
+    if (kind == 2)
       gnn_apply_device(ctx, ui, nullptr, nullptr, ctx->gnn->scal.p + 8, zi, nullptr, kw.flags.p);
     else
       amg_vcycle(ctx, ui, zi, kw.flags.p);
@@ -455,7 +473,7 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32) {
 int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
   if (!ctx->use_graphs) {
     if (kind >= 2)
-      enqueue_cycle_flex(ctx, Val32);
+      enqueue_cycle_flex(ctx, Val32, kind);
     else
       enqueue_cycle32(ctx, Val32);
     SVGPU_CUDA(ctx, cudaGetLastError());
@@ -478,7 +496,7 @@ int run_cycle_kind(svgpu_ctx* ctx, const float* Val32, int kind) {
     cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
       if (kind >= 2)
-        enqueue_cycle_flex(ctx, Val32);
+        enqueue_cycle_flex(ctx, Val32, kind);
       else
         enqueue_cycle32(ctx, Val32);
       ce = cudaStreamEndCapture(ctx->stream, &graph);
@@ -666,9 +684,11 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
   const int sD = kw.sD;
   int rc = SVGPU_OK;
   const int mode = ctx->learned_mode;
-  bool learned = mode != 0;  // flexible cycles
-  // modes 4 and 5 run the cycles of mode 2 (multilevel V-cycle); only their initial guess differs
-  const int cycle_kind = 1 + (mode >= 4 ? 2 : mode);
+  // cycle kind (run_cycle_kind): 1 plain FP32 GMRES, 2 the network as preconditioner
+  // (mode 1), 3 the multilevel V-cycle (modes 2, 4, 5: 4 and 5 differ only in their
+  // initial guess), 4 the V-cycle with the network as pre-smoother (mode 3)
+  int cycle_kind = 1 + (mode >= 4 ? 2 : mode);
+  bool learned = mode != 0;  // flexible cycles (kinds 2-4)
   if (!kw.V32.p || kw.V32.n != (size_t)n * (sD + 1)) SVGPU_CUDA(ctx, kw.V32.resize((size_t)n * (sD + 1)));
   st->suc = 0;
   double nrm = device_norm(ctx, n, Rs, rc);
@@ -712,10 +732,12 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
       nrm = device_norm(ctx, n, kw.r64.p, rc);
       if (rc) return rc;
       if (learned && !(nrm < before)) {
-        // the learned cycle did not lower the true FP64 residual: undo it and finish
-        // the solve with plain GMRES cycles
+        // the flexible cycle did not lower the true FP64 residual: undo it and go on
+        // with the method without the learned part (mode 3: the plain V-cycle), or,
+        // after a V-cycle, with plain GMRES cycles
         ctx->learned_rejects++;
-        learned = false;
+        cycle_kind = cycle_kind == 4 ? 3 : 1;
+        learned = cycle_kind >= 2;
         SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.X.p, kw.mask.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, kw.rbak.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
                                         ctx->stream));
@@ -746,6 +768,20 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
     SVGPU_CUDA(ctx, cudaMemcpyAsync(flags, kw.flags.p, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
     SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     st->itr += std::min(flags[1], sD - 1) + 1;
+    if (flags[2] && learned) {
+      // a flexible cycle broke down (a preconditioned vector was zero or not finite, e.g.
+      // an untrained network's zero output): reject it like a cycle that did not lower
+      // the FP64 residual, and go on without its preconditioner
+      ctx->learned_rejects++;
+      cycle_kind = cycle_kind == 4 ? 3 : 1;
+      learned = cycle_kind >= 2;
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.X.p, kw.mask.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, kw.rbak.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+      nrm = before;
+      st->fNorm = nrm;
+      continue;
+    }
     if (flags[2]) return set_err(ctx, SVGPU_ENAN, "GMRES breakdown (zero or non-finite Arnoldi norm)");
     if (l + 1 == ctx->mItr) {  // final true residual
       launch_spmv4_f32_f64(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, kw.X.p, kw.tmp.p, kw.xw.p);
@@ -1042,6 +1078,8 @@ int svgpu_destroy(svgpu_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   graphs().erase(ctx);
   cg_release(ctx);
+  for (cudaEvent_t e : ctx->step_ev)
+    if (e) cudaEventDestroy(e);
   cudaStream_t s = ctx->stream;
   cudaStream_t cs = ctx->capture_stream;
   bool own = ctx->own_stream;
@@ -1052,6 +1090,12 @@ int svgpu_destroy(svgpu_ctx* ctx) {
 }
 
 const char* svgpu_last_error(const svgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int svgpu_step_device_ms(const svgpu_ctx* ctx, double* ms) {
+  if (!ctx || !ms) return SVGPU_EINVAL;
+  *ms = ctx->last_step_ms;
+  return ctx->last_step_ms >= 0.0 ? SVGPU_OK : SVGPU_ESTATE;
+}
 
 long long svgpu_kernel_launches(const svgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
@@ -1733,6 +1777,8 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     if ((rc = to_device(ctx, ctx->dirY, dirY, 3L * ctx->nDir))) return rc;
     if ((rc = to_device(ctx, ctx->dirA, dirA, 3L * ctx->nDir))) return rc;
   }
+  ctx->last_step_ms = -1.0;
+  if ((rc = step_time_mark(ctx, 0))) return rc;
   // picp (pic.cpp:591-767) and the strong Dirichlet values (set_bc_dir)
   launch_pic_predict(ctx->stream, n4, (props->gam - 1.0) / props->gam, ctx->Ao.p, ctx->Yo.p, ctx->Do.p, ctx->An.p,
                      ctx->Yn.p, ctx->Dn.p);
@@ -1784,9 +1830,17 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     }
     svgpu_ls_stats st;
     std::memset(&st, 0, sizeof(st));
-    if (opts->precision == SVGPU_FP64) {
+    if (opts->precision == SVGPU_FP64 && ctx->learned_mode == 0) {
       rc = solve_device(ctx, 4, ctx->R.p, ctx->Val.p, SVGPU_PREC_FSILS, incL.data(), &st, res.data());
     } else {
+      if (opts->precision == SVGPU_FP64) {
+        // FP64 residual and tangent with a flexible solver mode: the solve runs on an
+        // FP32 copy of the FP64 tangent inside the FP64 defect correction, so the
+        // Newton iteration converges to the FP64 residual's solution
+        SVGPU_CUDA(ctx, ctx->Val32.resize((size_t)ctx->nnz * 16));
+        gnn_f64_to_f32(ctx->stream, (long)ctx->nnz * 16, ctx->Val.p, ctx->Val32.p);
+        ctx->launches++;
+      }
       // the Newton iteration is the history slot of the solve (initial guesses of modes 4, 5)
       const int slot0 = ctx->hist_slot;
       ctx->hist_slot = itr - 1 < kHistSlots ? itr - 1 : -1;
@@ -1815,10 +1869,12 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     prev_iN = iN;
   }
   if (rcr) ctx->rcr->xo = ctx->rcr->xn;  // cplBC.xo = cplBC.xn at the end of the step (main.cpp:758)
+  if ((rc = step_time_mark(ctx, 1))) return rc;
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, ctx->An.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, ctx->Yn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, ctx->Dn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  step_time_read(ctx);
   phase_mark(ctx, PH_COUNT);
   return itr;
 }

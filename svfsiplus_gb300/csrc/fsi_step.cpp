@@ -186,6 +186,8 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     c.ini[q][2] = 1.0 - af[q];
     c.ini[q][3] = af[q];
   }
+  ctx->last_step_ms = -1.0;
+  if ((rc = step_time_mark(ctx, 0))) return rc;
   // picp and the strong Dirichlet values (set_bc_dir, set_bc.cpp:794-1004)
   phase_mark(ctx, PH_OTHER);
   launch_fsi_predict(ctx->stream, nNo, c, w.Ao.p, w.Yo.p, w.Do.p, w.An.p, w.Yn.p, w.Dn.p);
@@ -313,10 +315,12 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     cEq = (cEq + 1) % 2;
   }
   if (rc) return rc;
+  if ((rc = step_time_mark(ctx, 1))) return rc;
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, w.An.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, w.Yn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Dn, w.Dn.p, n7 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  step_time_read(ctx);
   phase_mark(ctx, PH_COUNT);
   return total;
 }

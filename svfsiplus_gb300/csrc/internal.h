@@ -321,9 +321,19 @@ struct svgpu_ctx {
   bool zero_null_rows = false;
   // host staging
   svgpu::DevBuf<double> stage1, stage2;
+  // device time of the last time step (svgpu_step_device_ms): events recorded after the
+  // step's inputs reached the device and before its outputs are copied back
+  cudaEvent_t step_ev[2] = {nullptr, nullptr};
+  double last_step_ms = -1.0;
 };
 
 namespace svgpu {
+
+// Step timing (svgpu_step_device_ms): mark the start of a time step's device work (its
+// inputs enqueued) and its end (before its outputs are copied back); step_time_read
+// stores the elapsed milliseconds once the stream has been synchronised.
+int step_time_mark(svgpu_ctx* ctx, int which);
+void step_time_read(svgpu_ctx* ctx);
 
 // Records a CUDA error into the context and returns SVGPU_ECUDA.
 int cuda_fail(svgpu_ctx* ctx, cudaError_t e, const char* what);

@@ -3,10 +3,10 @@
 // partial sums in a file-scope device array instead of memory the caller or the
 // library allocates.
 //
-// Who needs it: code that cannot call cudaMalloc at the point where it needs a dot
-// product -- a caller recording a CUDA graph (allocation is not allowed while a stream
-// is being captured), or a caller whose device memory is all owned by another
-// allocator or a fixed budget (a framework's caching allocator, an embedded solver).
+// Who needs it: callers that must not call cudaMalloc where they need a dot product --
+// a host program whose device memory is all owned by another allocator or held to a
+// fixed budget (a framework's caching allocator, an embedded solver sharing the GPU),
+// where an extra allocation could fail or fragment that pool.
 //
 // Limits and sharing:
 //   * the scratch array holds SVGPU_NOALLOC_MAX_PARTS partial sums (32 KB); each CTA
@@ -17,7 +17,10 @@
 //     call's contents; each call overwrites every partial it reads, so nothing has to
 //     start at zero;
 //   * calls whose kernels overlap on the GPU (different streams, no ordering) race on
-//     the array: order them on one stream or with events.
+//     the array: order them on one stream or with events;
+//   * the array's device address is looked up once per device and cached; it is not
+//     valid any more after cudaDeviceReset, so a process that resets a device must not
+//     call this entry point on it again.
 #include <mutex>
 
 #include "internal.h"
@@ -84,6 +87,26 @@ int scratch_for_device(int dev, double** out) {
   return SVGPU_OK;
 }
 
+// Device (or managed) memory of device `dev`; host memory and another GPU's memory are
+// not: the kernels run on the current device and would fault on a peer's address.
+bool on_device(const void* p, int dev) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
+}
+
+// A launch whose configuration the runtime rejects is reported by the launch call's own
+// return value, so an error left pending by the caller's earlier work is neither
+// reported here nor cleared.
+template <typename... Args>
+cudaError_t launch(void (*k)(Args...), int grid, int block, cudaStream_t s, Args... args) {
+  void* argv[] = {static_cast<void*>(&args)...};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k), dim3(grid), dim3(block), argv, 0, s);
+}
+
 }  // namespace
 }  // namespace svgpu
 
@@ -93,19 +116,27 @@ extern "C" int svgpu_fsils_dot_noalloc(int dof, int nNo, const double* U, const 
   if (dof <= 0 || nNo <= 0 || !U || !V || !result) return SVGPU_EINVAL;
   const long n = (long)dof * nNo;
   if (n > (long)SVGPU_NOALLOC_MAX_PARTS * SVGPU_NOALLOC_CHUNK) return SVGPU_ETOOBIG;
-  if (!is_device_ptr(U) || !is_device_ptr(V)) return SVGPU_EINVAL;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return SVGPU_ECUDA;
+  if (!on_device(U, dev) || !on_device(V, dev)) return SVGPU_EINVAL;
+  // a result in device memory must be this device's; anything else is host memory
+  cudaPointerAttributes rat;
+  bool dres = false;
+  if (cudaPointerGetAttributes(&rat, result) == cudaSuccess) {
+    dres = rat.type == cudaMemoryTypeDevice || rat.type == cudaMemoryTypeManaged;
+    if (dres && rat.device != dev) return SVGPU_EINVAL;
+  } else {
+    cudaGetLastError();
+  }
   double* part = nullptr;
   int rc = scratch_for_device(dev, &part);
   if (rc != SVGPU_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nparts = (int)((n + SVGPU_NOALLOC_CHUNK - 1) / SVGPU_NOALLOC_CHUNK);
-  noalloc_dot_partial_kernel<<<nparts, 256, 0, s>>>(n, U, V, part);
-  const bool dres = is_device_ptr(result);
+  if (launch(noalloc_dot_partial_kernel, nparts, 256, s, n, U, V, part) != cudaSuccess) return SVGPU_ECUDA;
   double* dst = dres ? result : part + SVGPU_NOALLOC_MAX_PARTS;
-  noalloc_dot_final_kernel<<<1, 256, 0, s>>>(nparts, part, dst);
-  if (cudaGetLastError() != cudaSuccess) return SVGPU_ECUDA;
+  if (launch(noalloc_dot_final_kernel, 1, 256, s, nparts, (const double*)part, dst) != cudaSuccess)
+    return SVGPU_ECUDA;
   if (!dres) {
     if (cudaMemcpyAsync(result, dst, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SVGPU_ECUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return SVGPU_ECUDA;

@@ -20,7 +20,6 @@ void rcr_integrate(double Rp, double C, double Rd, double Pd, double dt, double 
   const int nTS = 100;
   const double dtt = dt / static_cast<double>(nTS);
   double X = xo;
-  double Q3 = Qn;
   for (int n = 0; n < nTS; n++) {
     double Qrk[4];
     for (int i = 0; i < 4; i++) {
@@ -39,9 +38,7 @@ void rcr_integrate(double Rp, double C, double Rd, double Pd, double dt, double 
     f[3] = (Qrk[3] - (Xrk - Pd) / Rd) / C;
     const double r = dtt / 8.0;
     X = X + r * (f[0] + 3.0 * (f[1] + f[2]) + f[3]);
-    Q3 = Qrk[3];
   }
-  (void)Q3;
   *xn = X;
   *y = X + Qn * Rp;
 }

@@ -51,6 +51,10 @@ CASES = {
     # resistance term in every GMRES product (add_bc_mul.cpp:53)
     "small_rcr": dict(mesh="small", n_steps=3, dump_step=2, dump_iter=2, u_amp=5.0, rcr=1, rcr_Rp=121.0,
                       rcr_C=1.5e-5, rcr_Rd=1212.0, rcr_Pd=0.0, rcr_Xo=0.0),
+    # the same outlet with a steady inflow: the case tests/test_solver_xml.py writes as
+    # solver.xml + .vtu/.vtp files and runs through FluidCase
+    "small_rcr_steady": dict(mesh="small", n_steps=2, dump_step=2, dump_iter=2, rcr=1, rcr_Rp=121.0,
+                             rcr_C=1.5e-5, rcr_Rd=1212.0, rcr_Pd=0.0, rcr_Xo=0.0),
 }
 
 

@@ -8,8 +8,10 @@
   raw; zlib-compressed or not), and a mesh written as the reference's inputs
   (GlobalNodeID / GlobalElementID, 1-based) loads back into the same faces;
 * the parabolic profile of bc_ini on the straight pipe equals 1 - r^2/R^2;
-* (GPU) a case run from an XML file and .vtu/.vtp meshes gives the same fields as the
-  same case set up through the Python API.
+* (GPU) a case run from an XML file and .vtu/.vtp meshes gives the reference's fields:
+  with the RCR outlet against the compiled reference's own run of the same case
+  (tests/golden/ref_small_rcr_steady.npz), with a traction-free outlet against the
+  oracle's time loop (oracle/pyoracle.FluidRun) on the same mesh and settings.
 """
 import os
 
@@ -68,12 +70,23 @@ CASE_XML = """<?xml version="1.0" encoding="UTF-8" ?>
 """
 
 
-def _write_case(d):
+TRACTION_FREE_OUTLET = """   <Add_BC name="outlet" >
+      <Type> Neu </Type> <Time_dependence> Steady </Time_dependence> <Value> 0.0 </Value>
+   </Add_BC>
+</Add_equation>"""
+
+
+def _write_case(d, traction_free=False):
     m = named_pipe("small")
     vtkio.write_mesh_files(os.path.join(d, "mesh"), m)
     p = os.path.join(d, "solver.xml")
+    xml = CASE_XML
+    if traction_free:
+        a = xml.index('   <Add_BC name="outlet" >')
+        b = xml.index("</Add_equation>") + len("</Add_equation>")
+        xml = xml[:a] + TRACTION_FREE_OUTLET + xml[b:]
     with open(p, "w") as fh:
-        fh.write(CASE_XML)
+        fh.write(xml)
     return m, p
 
 
@@ -139,22 +152,46 @@ def test_parabolic_profile_is_the_pipe_profile():
     assert np.allclose(nV, [0.0, 0.0, -1.0], atol=1e-12)
 
 
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 @pytest.mark.gpu
-def test_gpu_xml_case_matches_api_case(tmp_path):
+def test_gpu_xml_case_matches_reference(tmp_path, golden):
     """The XML case (inlet -10 along the outward normal with the parabolic profile, no-slip
-    wall, RCR outlet) through FluidCase against PipeFluidSolver with u_mean = 10."""
+    wall, RCR outlet) through FluidCase against the compiled reference's run of the same
+    case (ref_small_rcr_steady): fields after each of 2 steps within 1e-8, the tolerance
+    of the reference's RCR steps through the API (test_rcr.py)."""
+    g = golden("small_rcr_steady")
+    ps = eval(str(g["params"]))
+    assert ps["u_amp"] == 0.0 and ps["rcr_Rp"] == 121.0 and ps["n_steps"] == 2
     m, p = _write_case(str(tmp_path))
     case = sx.FluidCase(p)
-    direct = api.PipeFluidSolver(m, sD=50, mItr=100, relTol=1e-8, absTol=1e-17, newton_min=3, newton_max=3,
-                                 newton_tol=1e-11, rcr=dict(Rp=121.0, C=1.5e-5, Rd=1212.0, Pd=0.0, Xo=0.0))
-    for _ in range(2):
+    for step in (1, 2):
         case.step()
-        direct.step(10.0, 0.0, 1.0)
-        e = float(np.linalg.norm(case.Yn - direct.Yn) / np.linalg.norm(direct.Yn))
-        print("XML case vs API case:", e)
-        assert e <= 1e-12
+        ev, ea = _rel(case.Yn, g[f"Yn_{step}"]), _rel(case.An, g[f"An_{step}"])
+        print("XML case vs reference, step", step, "Yn", ev, "An", ea)
+        assert ev <= 1e-8 and ea <= 1e-8
     case.run(1, vtu_prefix=str(tmp_path / "result"), save_every=1)
     d = vtkio.read_vtk(str(tmp_path / "result_003.vtu"))
     assert np.array_equal(d["point_data"]["Pressure"], case.Yn[:, 3])
     case.ctx.close()
-    direct.ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_xml_traction_free_case_matches_oracle(tmp_path):
+    """The same XML case with a traction-free outlet against the oracle's time loop
+    (the reference's Newton loop restated in C) on the same mesh and settings: fields
+    after each of 2 steps within 1e-8."""
+    from oracle import pyoracle as po
+    m, p = _write_case(str(tmp_path), traction_free=True)
+    case = sx.FluidCase(p)
+    run = po.FluidRun(m, po.fluid_params(), sD=50, mItr=100, relTol=1e-8, absTol=1e-17, newton_min=3,
+                      newton_max=3, newton_tol=1e-11)
+    for step in (1, 2):
+        case.step()
+        run.step(10.0, 0.0, 1.0)
+        ev, ea = _rel(case.Yn, run.Yn), _rel(case.An, run.An)
+        print("XML case vs oracle, step", step, "Yn", ev, "An", ea)
+        assert ev <= 1e-8 and ea <= 1e-8
+    case.ctx.close()

@@ -1,6 +1,6 @@
-"""svgpu_fsils_dot_noalloc: the dot product for callers that cannot allocate device
-memory (code recording a CUDA graph, or code whose device memory belongs to another
-allocator).  Called through the C ABI, its result is checked against the existing
+"""svgpu_fsils_dot_noalloc: the dot product for callers that must not allocate device
+memory (a host program whose device memory belongs to another allocator or a fixed
+budget).  Called through the C ABI, its result is checked against the existing
 entry point that computes the same reduction with allocated scratch: fsils_solve
 without preconditioning reports iNorm = ||R|| (RI.iNorm, gmres.cpp:481-483).
 Tolerance 1e-12 relative, as the FP64 parity tests use; two calls in a row."""
