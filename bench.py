@@ -7,8 +7,9 @@ mean plus a 5 cm/s sine at 1 Hz), generalised-alpha rho_inf = 0.5, dt = 1e-3.
 
 A "step" is one time step of the reference's Newton loop (main.cpp:371-617). Newton
 iterations run until the reference's own test in picc (pic.cpp:239-281) holds:
-r1 <= tol * pNorm with tol = 1e-6. That is, the preconditioned residual norm has fallen
-to 1e-6 of its value at the step's first iteration. There are at most 8 Newton iterations.
+r1 <= tol or r1 <= tol * pNorm with tol = 1e-8 (tighter than the metric's 1e-6, so that
+the fields stay within 1e-6 of the FP64 solution of the same steps). There are at most
+8 Newton iterations.
 Each linear solve is inexact (relative tolerance 1e-2), as in inexact Newton.
 
 Paths (--path):
@@ -69,7 +70,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "s/time step + Krylov iters, learned-precond vs plain GPU, 1 GB300, res<=1e-6"
 WORKLOAD = "pipe8m"
-NEWTON_TOL = 1e-6
+# Newton tolerance of picc's test (r1 <= tol or r1 <= tol pNorm, pic.cpp:239-281).  The
+# metric asks for res <= 1e-6; 1e-8 is used because at 1e-6 the pressure drifts from the
+# FP64 solution of the same steps by up to 3e-5 over 20 steps (the Newton tolerance, not
+# the mixed precision: FP64 assembly drifts alike), at 1e-8 by at most 2e-7.
+NEWTON_TOL = 1e-8
 NEWTON_MAX = 8
 LIN_REL_TOL = 1e-2
 KRYLOV_DIM = 50
@@ -78,6 +83,7 @@ KRYLOV_DIM = 50
 # it every iteration as the reference does (the plain path always does)
 REUSE_TANGENT = True
 MAX_RESTARTS = 40
+PREDICTOR = 1  # mixed paths: 1 extrapolating Newton predictor, 0 picp
 PATH_MODES = {"learned": 4, "history": 5, "multilevel": 2, "learned-smoother": 3, "mixed": 0, "plain": -1}
 TRAIN_ITERS, TRAIN_LR = 100, 1e-3  # Adam steps after every warm-up step that stored triples
 U_MEAN, U_AMP, U_FREQ = 10.0, 5.0, 1.0
@@ -378,6 +384,10 @@ def make_solver(api, mesh, rowPtr, colPtr, path, device=0, newton_tol=None, newt
         s.enable_learning()
     if mode >= 0:
         s.ctx.set_solver_mode(mode if mode not in (3, 4) else 2)
+        # the mixed paths start each step's Newton iteration from the velocity
+        # extrapolated from the last two steps (svgpu_set_predictor); the plain path
+        # keeps the reference's picp
+        s.ctx.set_predictor(PREDICTOR)
     return s, mode
 
 
@@ -640,6 +650,7 @@ def run_ours(args):
         "path": args.path, "solver_mode": mode,
         "tangent": "kept from the step's first Newton iteration" if (REUSE_TANGENT and mode >= 0)
         else "reassembled every Newton iteration",
+        "predictor": "velocity extrapolated from the last two steps" if (PREDICTOR and mode >= 0) else "picp",
         "timing": "value: device time of each timed step between its inputs' arrival and its outputs' copy-back "
                   "(CUDA events on the library's stream), summed over the steps; e2e: host clock around the same "
                   "C-ABI calls, host arrays copied in and out",

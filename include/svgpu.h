@@ -382,6 +382,17 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
                      double* An, double* Yn, double* Dn,
                      double* iNorm, double* pNorm, svgpu_ls_stats* stats);
 
+/* Newton predictor of svgpu_fluid_step (no reference counterpart).  0 (the default):
+ * picp (pic.cpp:591-767), An = Ao (gam - 1) / gam, Yn = Yo.  1: the velocity rows'
+ * acceleration extrapolated linearly from the last two steps, An = 2 Ao - Aoo, with the
+ * velocity the generalised-alpha update makes consistent with it,
+ * Yn = Yo + dt ((1 - gam) Ao + gam An); the pressure row keeps picp's prediction (its
+ * rate is too noisy to extrapolate); Aoo is the Ao of the context's previous
+ * svgpu_fluid_step call, so the calls must be consecutive time steps (the first call
+ * after this one uses picp).  The predictor only moves the Newton iteration's start:
+ * the converged step is the same. */
+int svgpu_set_predictor(svgpu_ctx* ctx, int kind);
+
 /* Device time of the last svgpu_fluid_step / svgpu_fsi_step in milliseconds: CUDA
  * events on the context's stream, the first recorded once the step's inputs are
  * enqueued to the device, the second before its outputs are copied back.  The host

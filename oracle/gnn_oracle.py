@@ -5,8 +5,9 @@ A numpy restatement of the message-passing network the GPU kernels implement
 gradients.  Inputs per node: the residual r / s_r, the prior p / s_p (zero without a
 prior) and 4 static features; the output out is the correction scaled by s_o
 (s_p with a prior, s_r without): M(r, p) = p + s_o * out.  It reproduces the GPU's storage precisions: weights rounded to BF16,
-activations h stored in BF16, the neighbour mean m used in FP32 by the forward pass and
-stored in BF16 for the weight gradient; arithmetic is FP64 here (FP32 on the GPU).
+activations h stored in BF16, the neighbour mean m rounded to BF16 before the dense
+layer (the GPU multiplies BF16 tiles on the tensor cores) and for the weight gradient;
+arithmetic is FP64 here (FP32 accumulation on the GPU).
 """
 from __future__ import annotations
 
@@ -82,9 +83,10 @@ def forward(p, rowPtr, colPtr, r, stat, prior=None):
     ms = [None]
     for l in range(3):
         m, _ = _mean_gather(rowPtr, colPtr, h[-1])
-        z = np.concatenate([h[-1], m], axis=1) @ Ws[l] + bs[l]
+        mb = bf16(m)  # the neighbour mean enters the dense layer (tensor cores) in BF16
+        z = np.concatenate([h[-1], mb], axis=1) @ Ws[l] + bs[l]
         masks.append(z > 0)
-        ms.append(bf16(m))
+        ms.append(mb)
         h.append(bf16(h[-1] + np.maximum(z, 0.0)))
     out = h[3] @ Wd + bd
     return out, so, dict(x=x, h=h, ms=ms, masks=masks)

@@ -392,6 +392,10 @@ class Context:
         return [stats[i].as_dict() for i in range(it)]
 
 
+    def set_predictor(self, kind):
+        """svgpu_set_predictor: 0 picp, 1 the acceleration extrapolated from the last two steps."""
+        self._check(lib().svgpu_set_predictor(self._h, int(kind)), "set_predictor")
+
     def step_device_ms(self):
         """Device milliseconds of the last fluid/FSI time step, between its inputs'
         arrival on the device and the copy-back of its outputs (svgpu_step_device_ms)."""

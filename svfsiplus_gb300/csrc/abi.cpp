@@ -601,9 +601,35 @@ int history_guess(svgpu_ctx* ctx, const float* Val32, const double* Rs, double& 
   }
   launch_guess_coef1(s, ctx->sm_count, gw.part.p, gw.coef.p);
   ctx->launches += 5;
+  // From the second Newton iteration of a step on, the previous iteration's increment
+  // of this step (history slot - 1, replaced by that solve) is a second direction: the
+  // prior g becomes the minimal-residual combination of the two (a modified Newton
+  // iteration's increments of one step are nearly parallel, where the previous step's
+  // increment of the same iteration is a weak predictor).
+  const bool two = slot >= 1 && gw.valid[slot - 1] && gw.hist[slot - 1].n == (size_t)n;
+  if (two) {
+    SVGPU_CUDA(ctx, gw.g2.resize(n));
+    SVGPU_CUDA(ctx, gw.wg2.resize(n));
+    launch_f32_to_f64(s, n, gw.hist[slot - 1].p, gw.g2.p);
+    launch_spmv4_f32_f64(s, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, gw.g2.p, gw.wg2.p, kw.xw.p);
+    add_coupled(ctx, 4, gw.g2.p, gw.wg2.p, nullptr);
+    const double* a[3] = {Rs, gw.w1.p, gw.wg2.p};
+    const double* b[3] = {gw.wg2.p, gw.wg2.p, gw.wg2.p};
+    launch_guess_dots(s, n, 3, a, b, gw.part.p, ctx->sm_count);
+    launch_guess_coef2(s, ctx->sm_count, gw.part.p, gw.coef.p);
+    launch_guess_combine(s, n, gw.coef.p, gw.g.p, gw.g2.p, gw.w1.p, gw.wg2.p);
+    const double* a1[2] = {Rs, gw.w1.p};
+    const double* b1[2] = {gw.w1.p, gw.w1.p};
+    launch_guess_dots(s, n, 2, a1, b1, gw.part.p, ctx->sm_count);
+    launch_guess_coef1(s, ctx->sm_count, gw.part.p, gw.coef.p);
+    ctx->launches += 7;
+  }
   if (ctx->gnn && (net || collect)) {
     SVGPU_CUDA(ctx, gw.prior.resize(n));
-    launch_scale_f32(s, n, gw.coef.p, gw.hist[slot].p, gw.prior.p);
+    if (two)
+      launch_scale_f64_f32(s, n, gw.coef.p, gw.g.p, gw.prior.p);
+    else
+      launch_scale_f32(s, n, gw.coef.p, gw.hist[slot].p, gw.prior.p);
     ctx->launches++;
     gw.prior_valid = true;
   }
@@ -1090,6 +1116,14 @@ int svgpu_destroy(svgpu_ctx* ctx) {
 }
 
 const char* svgpu_last_error(const svgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int svgpu_set_predictor(svgpu_ctx* ctx, int kind) {
+  if (!ctx) return SVGPU_EINVAL;
+  if (kind < 0 || kind > 1) return set_err(ctx, SVGPU_EINVAL, "set_predictor: kind must be 0 or 1");
+  ctx->predictor = kind;
+  ctx->aprev_valid = false;
+  return SVGPU_OK;
+}
 
 int svgpu_step_device_ms(const svgpu_ctx* ctx, double* ms) {
   if (!ctx || !ms) return SVGPU_EINVAL;
@@ -1779,9 +1813,14 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
   }
   ctx->last_step_ms = -1.0;
   if ((rc = step_time_mark(ctx, 0))) return rc;
-  // picp (pic.cpp:591-767) and the strong Dirichlet values (set_bc_dir)
-  launch_pic_predict(ctx->stream, n4, (props->gam - 1.0) / props->gam, ctx->Ao.p, ctx->Yo.p, ctx->Do.p, ctx->An.p,
-                     ctx->Yn.p, ctx->Dn.p);
+  // picp (pic.cpp:591-767), or the extrapolating predictor, and the strong Dirichlet
+  // values (set_bc_dir)
+  if (ctx->predictor == 1 && ctx->aprev_valid && ctx->Aprev.n == (size_t)n4)
+    launch_pic_predict_extrap(ctx->stream, n4, props->dt, props->gam, ctx->Ao.p, ctx->Aprev.p, ctx->Yo.p, ctx->Do.p,
+                              ctx->An.p, ctx->Yn.p, ctx->Dn.p);
+  else
+    launch_pic_predict(ctx->stream, n4, (props->gam - 1.0) / props->gam, ctx->Ao.p, ctx->Yo.p, ctx->Do.p, ctx->An.p,
+                       ctx->Yn.p, ctx->Dn.p);
   launch_set_dirichlet(ctx->stream, ctx->nDir, ctx->dirNodes.p, ctx->dirY.p, ctx->dirA.p, ctx->An.p, ctx->Yn.p);
   ctx->launches += 2;
   std::vector<int> incL(ctx->nFaces, 1);
@@ -1869,6 +1908,12 @@ int svgpu_fluid_step(svgpu_ctx* ctx, const svgpu_fluid_props* props, const svgpu
     prev_iN = iN;
   }
   if (rcr) ctx->rcr->xo = ctx->rcr->xn;  // cplBC.xo = cplBC.xn at the end of the step (main.cpp:758)
+  if (ctx->predictor == 1) {  // this step's Ao is the next step's Aoo
+    SVGPU_CUDA(ctx, ctx->Aprev.resize(n4));
+    SVGPU_CUDA(ctx, cudaMemcpyAsync(ctx->Aprev.p, ctx->Ao.p, n4 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    ctx->stream));
+    ctx->aprev_valid = true;
+  }
   if ((rc = step_time_mark(ctx, 1))) return rc;
   SVGPU_CUDA(ctx, cudaMemcpyAsync(An, ctx->An.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));
   SVGPU_CUDA(ctx, cudaMemcpyAsync(Yn, ctx->Yn.p, n4 * sizeof(double), cudaMemcpyDefault, ctx->stream));

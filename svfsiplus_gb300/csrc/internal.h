@@ -210,6 +210,7 @@ struct GuessWork {
   DevBuf<float> hist[kHistSlots];
   bool valid[kHistSlots] = {};
   DevBuf<double> g, w1, d, w2;  // FP64 directions and their products
+  DevBuf<double> g2, wg2;       // the current step's previous increment and its product
   DevBuf<float> prior;          // alpha g in FP32 (the network's prior)
   DevBuf<double> part, coef;    // dot partials; coef = {a1, a2, r.w1, w1.w1, ...}
   bool prior_valid = false;     // prior holds the prior of the current solve
@@ -325,6 +326,11 @@ struct svgpu_ctx {
   // step's inputs reached the device and before its outputs are copied back
   cudaEvent_t step_ev[2] = {nullptr, nullptr};
   double last_step_ms = -1.0;
+  // Newton predictor of svgpu_fluid_step (svgpu_set_predictor): 0 picp, 1 the
+  // acceleration extrapolated from the last two steps (Aprev: the previous step's Ao)
+  int predictor = 0;
+  svgpu::DevBuf<double> Aprev;
+  bool aprev_valid = false;
 };
 
 namespace svgpu {
@@ -570,6 +576,8 @@ void launch_mesh_correct(cudaStream_t s, int nNo, double c0, double c1, const do
 void launch_pad_mesh_system(cudaStream_t s, int nNo, long nnz, const int* blkRow, const int* colPtr,
                             const double* Val9, const double* R3, float* Val16, double* R4);
 void launch_unpad_vec(cudaStream_t s, int nNo, const double* R4, double* R3);
+void launch_pic_predict_extrap(cudaStream_t s, long n4, double dt, double gam, const double* Ao, const double* Aoo,
+                               const double* Yo, const double* Do, double* An, double* Yn, double* Dn);
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn);
 void launch_set_dirichlet(cudaStream_t s, int nDir, const int* nodes, const double* dirY,
@@ -611,6 +619,11 @@ void launch_guess_coef2(cudaStream_t s, int sm_count, const double* part, double
 void launch_guess_apply(cudaStream_t s, long n, const double* coef, const double* g, const double* d,
                         const double* w1, const double* w2, const double* r, double* X, double* r0);
 void launch_scale_f32(cudaStream_t s, long n, const double* coef, const float* g, float* p);
+// g = coef[0] g + coef[1] g2 and w = coef[0] w + coef[1] w2 (in place)
+void launch_guess_combine(cudaStream_t s, long n, const double* coef, double* g, const double* g2, double* w,
+                          const double* w2);
+// p = coef[0] g in FP32
+void launch_scale_f64_f32(cudaStream_t s, long n, const double* coef, const double* g, float* p);
 void gnn_f64_to_f32(cudaStream_t st, long n, const double* a, float* b);
 
 }  // namespace svgpu

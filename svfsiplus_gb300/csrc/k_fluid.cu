@@ -499,6 +499,29 @@ __global__ void pic_predict_kernel(long n4, double coef, const double* __restric
   }
 }
 
+// Extrapolating predictor (no reference counterpart): the fluid acceleration
+// extrapolated linearly from the last two steps, An = 2 Ao - Aoo, and the velocity that
+// the generalised-alpha update makes consistent with it,
+// Yn = Yo + dt ((1 - gam) Ao + gam An) (the relation picc keeps, pic.cpp:156-166); the
+// pressure row (every fourth entry) keeps picp's prediction, and Dn = Do as in picp.
+__global__ void pic_predict_extrap_kernel(long n4, double dt, double gam, const double* __restrict__ Ao,
+                                          const double* __restrict__ Aoo, const double* __restrict__ Yo,
+                                          const double* __restrict__ Do, double* __restrict__ An,
+                                          double* __restrict__ Yn, double* __restrict__ Dn) {
+  const double coef = (gam - 1.0) / gam;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long)gridDim.x * blockDim.x) {
+    if ((i & 3) == 3) {
+      An[i] = Ao[i] * coef;
+      Yn[i] = Yo[i];
+    } else {
+      const double a = 2.0 * Ao[i] - Aoo[i];
+      An[i] = a;
+      Yn[i] = Yo[i] + dt * ((1.0 - gam) * Ao[i] + gam * a);
+    }
+    Dn[i] = Do[i];
+  }
+}
+
 __global__ void set_dirichlet_kernel(int nDir, const int* __restrict__ nodes, const double* __restrict__ dirY,
                                      const double* __restrict__ dirA, double* __restrict__ An, double* __restrict__ Yn) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -623,6 +646,11 @@ void launch_neu_backflow_ale(cudaStream_t s, const FluidConsts& c, double h, int
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
   neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, ld, Yg, Do, rowPtr, R, Val64);
+}
+
+void launch_pic_predict_extrap(cudaStream_t s, long n4, double dt, double gam, const double* Ao, const double* Aoo,
+                               const double* Yo, const double* Do, double* An, double* Yn, double* Dn) {
+  pic_predict_extrap_kernel<<<grid_for(n4, 256), 256, 0, s>>>(n4, dt, gam, Ao, Aoo, Yo, Do, An, Yn, Dn);
 }
 
 void launch_pic_predict(cudaStream_t s, long n4, double coef, const double* Ao, const double* Yo,

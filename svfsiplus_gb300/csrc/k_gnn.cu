@@ -86,10 +86,25 @@ __global__ void __launch_bounds__(256) gnn_encode_kernel(int nNo, const float* _
 }
 
 // ---- message-passing layer: gather mean + dense 128 -> 64 + relu + residual.
-// Persistent CTAs of 128 threads keep the layer's weights in shared memory and walk
-// tiles of 16 nodes: the 4 warps gather (lanes over features, 128-byte rows), then
-// every thread computes 2 nodes x 4 outputs from the shared tile.
+// Persistent CTAs of 128 threads keep the layer's weights (BF16, transposed so that a
+// column's k run is contiguous) in shared memory and walk tiles of 16 nodes: the 4
+// warps gather (lanes over features, 128-byte rows) the node's own row and the mean
+// of its neighbours' rows into a 16 x 128 BF16 tile; then the tile times the 128 x 64
+// weights runs on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
+// accumulation): warp w computes output columns 16w..16w+15 as two 16 x 8 tiles over
+// 8 k-steps.
 constexpr int MP_NODES = 16;
+constexpr int MP_LD = 2 * H + 8;  // BF16 row stride of the shared tiles: 272 bytes, conflict-free fragments
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 __global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restrict__ rowPtr,
                                                      const int* __restrict__ colPtr,
                                                      const __nv_bfloat16* __restrict__ hin,
@@ -98,26 +113,26 @@ __global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restr
                                                      __nv_bfloat16* __restrict__ msave, uint64_t* __restrict__ mask,
                                                      const int* flags) {
   if (flags && (flags[0] != 0 || flags[2] != 0)) return;
-  __shared__ float A[MP_NODES][2 * H + 1];
-  __shared__ __align__(16) float W[2 * H][H];
+  __shared__ __align__(16) __nv_bfloat16 As[MP_NODES][MP_LD];  // [h_i ; mean_j h_j] per node
+  __shared__ __align__(16) __nv_bfloat16 Wt[H][MP_LD];         // Wt[n][k] = W[k][n]
   __shared__ float B[H];
+  __shared__ uint16_t smask[MP_NODES][4];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const __nv_bfloat16* Wg = P + off_w(layer);
-  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) W[k / H][k % H] = bf(Wg[k]);
+  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) Wt[k % H][k / H] = Wg[k];
   for (int k = threadIdx.x; k < H; k += blockDim.x) B[k] = bf(P[off_b(layer) + k]);
   const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
-  const int ng = threadIdx.x >> 4, cgp = threadIdx.x & 15;
+  const int g = lane >> 2, tq = lane & 3;  // fragment row group and thread-in-quad
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int node0 = tile * MP_NODES;
     __syncthreads();
     for (int q = warp; q < MP_NODES; q += 4) {
       const int i = node0 + q;
-      float s0 = 0.f, s1 = 0.f, o0 = 0.f, o1 = 0.f;
+      __nv_bfloat162 own = __floats2bfloat162_rn(0.f, 0.f), mean = own;
       if (i < nNo) {
         const int b = rowPtr[i], e = rowPtr[i + 1];
-        const __nv_bfloat162 own = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * i)[lane];
-        o0 = __low2float(own);
-        o1 = __high2float(own);
+        own = reinterpret_cast<const __nv_bfloat162*>(hin + (long)H * i)[lane];
+        float s0 = 0.f, s1 = 0.f;
         // eight neighbour rows in flight per warp; the sums keep the row order
         const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(hin);
         int k = b;
@@ -137,57 +152,65 @@ __global__ void __launch_bounds__(128) gnn_mp_kernel(int nNo, const int* __restr
           s1 += __high2float(v);
         }
         const float inv = 1.f / (float)(e - b);
-        s0 *= inv;
-        s1 *= inv;
-        if (msave) reinterpret_cast<__nv_bfloat162*>(msave + (long)H * i)[lane] = __floats2bfloat162_rn(s0, s1);
+        mean = __floats2bfloat162_rn(s0 * inv, s1 * inv);
+        if (msave) reinterpret_cast<__nv_bfloat162*>(msave + (long)H * i)[lane] = mean;
       }
-      A[q][2 * lane] = o0;
-      A[q][2 * lane + 1] = o1;
-      A[q][H + 2 * lane] = s0;
-      A[q][H + 2 * lane + 1] = s1;
+      reinterpret_cast<__nv_bfloat162*>(&As[q][0])[lane] = own;
+      reinterpret_cast<__nv_bfloat162*>(&As[q][H])[lane] = mean;
     }
     __syncthreads();
-    float acc[2][4];
+    // z (16 x 16 per warp) = As (16 x 128) x W[:, 16w .. 16w+15]
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
-    for (int a = 0; a < 2; a++)
+    for (int k0 = 0; k0 < 2 * H; k0 += 16) {
+      const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&As[g][k0 + 2 * tq]);
+      const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&As[g + 8][k0 + 2 * tq]);
+      const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&As[g][k0 + 8 + 2 * tq]);
+      const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&As[g + 8][k0 + 8 + 2 * tq]);
 #pragma unroll
-      for (int c = 0; c < 4; c++) acc[a][c] = B[cgp * 4 + c];
-#pragma unroll 8
-    for (int k = 0; k < 2 * H; k++) {
-      const float4 w = *reinterpret_cast<const float4*>(&W[k][cgp * 4]);
-#pragma unroll
-      for (int a = 0; a < 2; a++) {
-        const float x = A[ng * 2 + a][k];
-        acc[a][0] = fmaf(x, w.x, acc[a][0]);
-        acc[a][1] = fmaf(x, w.y, acc[a][1]);
-        acc[a][2] = fmaf(x, w.z, acc[a][2]);
-        acc[a][3] = fmaf(x, w.w, acc[a][3]);
+      for (int j = 0; j < 2; j++) {
+        const int n = 16 * warp + 8 * j + g;
+        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&Wt[n][k0 + 2 * tq]);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&Wt[n][k0 + 8 + 2 * tq]);
+        mma_bf16_16816(acc[j], a0, a1, a2, a3, b0, b1);
       }
     }
+    // epilogue: rows g and g + 8, columns 16w + 8j + 2tq + {0, 1}
+    uint32_t bits[2] = {0u, 0u};
 #pragma unroll
-    for (int a = 0; a < 2; a++) {
-      const int q = ng * 2 + a;
+    for (int hrow = 0; hrow < 2; hrow++) {
+      const int q = g + 8 * hrow;
       const int i = node0 + q;
-      uint32_t bits = 0;
-      float o[4];
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const float z = acc[a][c];
-        if (z > 0.f) bits |= 1u << c;
-        o[c] = A[q][cgp * 4 + c] + (z > 0.f ? z : 0.f);
+      for (int j = 0; j < 2; j++) {
+        const int c = 16 * warp + 8 * j + 2 * tq;
+        const float z0 = acc[j][2 * hrow] + B[c], z1 = acc[j][2 * hrow + 1] + B[c + 1];
+        const float2 hh = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&As[q][c]));
+        if (z0 > 0.f) bits[hrow] |= 1u << (8 * j + 2 * tq);
+        if (z1 > 0.f) bits[hrow] |= 1u << (8 * j + 2 * tq + 1);
+        if (i < nNo)
+          *reinterpret_cast<__nv_bfloat162*>(hout + (long)H * i + c) =
+              __floats2bfloat162_rn(hh.x + (z0 > 0.f ? z0 : 0.f), hh.y + (z1 > 0.f ? z1 : 0.f));
       }
-      if (i < nNo) {
-        __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(hout + (long)H * i + cgp * 4);
-        dst[0] = __floats2bfloat162_rn(o[0], o[1]);
-        dst[1] = __floats2bfloat162_rn(o[2], o[3]);
-      }
-      if (mask) {
-        // the 16 threads of a node (a half warp) contribute 4 bits each; every lane
-        // takes part in the shuffles
-        uint64_t word = (uint64_t)bits << (4 * cgp);
+    }
+    if (mask) {
+      // the quad's four lanes hold the 16 columns of rows g and g + 8
 #pragma unroll
-        for (int off = 1; off < 16; off <<= 1) word |= __shfl_xor_sync(0xffffffffu, word, off);
-        if (cgp == 0 && i < nNo) mask[(long)layer * nNo + i] = word;
+      for (int hrow = 0; hrow < 2; hrow++) {
+        bits[hrow] |= __shfl_xor_sync(0xffffffffu, bits[hrow], 1);
+        bits[hrow] |= __shfl_xor_sync(0xffffffffu, bits[hrow], 2);
+      }
+      if (tq == 0) {
+        smask[g][warp] = (uint16_t)bits[0];
+        smask[g + 8][warp] = (uint16_t)bits[1];
+      }
+      __syncthreads();
+      if (threadIdx.x < MP_NODES && node0 + (int)threadIdx.x < nNo) {
+        const int q = threadIdx.x;
+        uint64_t word = 0;
+#pragma unroll
+        for (int w = 0; w < 4; w++) word |= (uint64_t)smask[q][w] << (16 * w);
+        mask[(long)layer * nNo + node0 + q] = word;
       }
     }
   }
@@ -326,6 +349,14 @@ __global__ void __launch_bounds__(256) gnn_decode_bwd_kernel(int nNo, const __nv
 // ---- message-passing layer backward, dense part.  dh (FP32, gradient of the
 // layer output) -> dz = dh * relu'(z); d[h;m] = W dz; dhd = dh + d[h]; dms = d[m] / deg.
 // Weight gradient partial per CTA: [h; m]^T dz (128 x 64) and sum dz (64).
+// Both products run on the tensor cores (mma.sync m16n8k16, FP32 accumulation): the
+// layer input [h; m] and W are BF16 values already, and dz is split into two BF16
+// parts (dz = hi + lo, |lo| <= 2^-9 |dz|) whose products are summed, so the result
+// keeps about 16 bits of dz.  Per tile of 16 nodes warp w computes d[h;m] for input
+// features 32w..32w+31 and accumulates weight-gradient rows 32w..32w+31 over the
+// CTA's tiles in registers (no atomics).
+constexpr int BW_LDT = MP_NODES + 8;  // BF16 row stride of the node-minor tiles: 48 bytes
+
 __global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __restrict__ rowPtr,
                                                          const __nv_bfloat16* __restrict__ hin,
                                                          const __nv_bfloat16* __restrict__ msave,
@@ -333,15 +364,21 @@ __global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __r
                                                          const __nv_bfloat16* __restrict__ P,
                                                          const float* __restrict__ dh, float* __restrict__ dhd,
                                                          float* __restrict__ dms, float* __restrict__ gpart) {
-  __shared__ float X[MP_NODES][2 * H + 1];
-  __shared__ float DZ[MP_NODES][H + 1];
-  __shared__ float W[2 * H][H + 1];  // padded: the 8 rows one warp reads at a time sit in 8 banks
+  __shared__ __align__(16) __nv_bfloat16 Wr[2 * H][H + 8];           // W[r][c]
+  __shared__ __align__(16) __nv_bfloat16 XT[2 * H][BW_LDT];          // [h; m]^T: XT[r][q]
+  __shared__ __align__(16) __nv_bfloat16 DZ[2][MP_NODES][H + 8];     // dz hi / lo: [q][c]
+  __shared__ __align__(16) __nv_bfloat16 DZT[2][H][BW_LDT];          // dz^T hi / lo: [c][q]
   const __nv_bfloat16* Wg = P + off_w(layer);
-  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) W[k / H][k % H] = bf(Wg[k]);
-  // each thread owns 64 entries of the 128 x 64 weight gradient (+ bias share)
-  float gacc[64];
+  for (int k = threadIdx.x; k < 2 * H * H; k += blockDim.x) Wr[k / H][k % H] = Wg[k];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tq = lane & 3;
+  float gacc[2][8][4];
 #pragma unroll
-  for (int q = 0; q < 64; q++) gacc[q] = 0.f;
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) gacc[mt][nt][e] = 0.f;
   float gb = 0.f;
   const int tiles = (nNo + MP_NODES - 1) / MP_NODES;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -350,51 +387,98 @@ __global__ void __launch_bounds__(128) gnn_mp_bwd_kernel(int nNo, const int* __r
     for (int k = threadIdx.x; k < MP_NODES * H; k += blockDim.x) {
       const int q = k / H, f = k % H;
       const int i = node0 + q;
-      float x0 = 0.f, x1 = 0.f, dz = 0.f;
+      __nv_bfloat16 x0 = __float2bfloat16(0.f), x1 = x0;
+      float dz = 0.f;
       if (i < nNo) {
-        x0 = bf(hin[(long)H * i + f]);
-        x1 = bf(msave[(long)H * i + f]);
+        x0 = hin[(long)H * i + f];
+        x1 = msave[(long)H * i + f];
         const uint64_t m = mask[(long)layer * nNo + i];
         dz = ((m >> f) & 1ull) ? dh[(long)H * i + f] : 0.f;
       }
-      X[q][f] = x0;
-      X[q][H + f] = x1;
-      DZ[q][f] = dz;
+      const __nv_bfloat16 hi = __float2bfloat16(dz);
+      const __nv_bfloat16 lo = __float2bfloat16(dz - __bfloat162float(hi));
+      XT[f][q] = x0;
+      XT[H + f][q] = x1;
+      DZ[0][q][f] = hi;
+      DZ[1][q][f] = lo;
+      DZT[0][f][q] = hi;
+      DZT[1][f][q] = lo;
     }
     __syncthreads();
-    // d[h;m] = W dz: thread -> node q = t / 8, features r = 8 j + t % 8, j = 0..15
+    // d[h;m] (16 x 128) = dz (16 x 64) W^T: warp w -> columns r = 32w .. 32w + 31
     {
-      const int q = threadIdx.x >> 3, part = threadIdx.x & 7;
-      const int i = node0 + q;
-      if (i < nNo) {
+      float acc[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+        for (int e = 0; e < 4; e++) acc[nt][e] = 0.f;
+#pragma unroll
+      for (int k0 = 0; k0 < H; k0 += 16) {
+#pragma unroll
+        for (int part = 0; part < 2; part++) {
+          const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&DZ[part][g][k0 + 2 * tq]);
+          const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&DZ[part][g + 8][k0 + 2 * tq]);
+          const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&DZ[part][g][k0 + 8 + 2 * tq]);
+          const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&DZ[part][g + 8][k0 + 8 + 2 * tq]);
+#pragma unroll
+          for (int nt = 0; nt < 4; nt++) {
+            const int r = 32 * warp + 8 * nt + g;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&Wr[r][k0 + 2 * tq]);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&Wr[r][k0 + 8 + 2 * tq]);
+            mma_bf16_16816(acc[nt], a0, a1, a2, a3, b0, b1);
+          }
+        }
+      }
+#pragma unroll
+      for (int hrow = 0; hrow < 2; hrow++) {
+        const int q = g + 8 * hrow;
+        const int i = node0 + q;
+        if (i >= nNo) continue;
         const float invdeg = 1.f / (float)(rowPtr[i + 1] - rowPtr[i]);
-        for (int r = part; r < 2 * H; r += 8) {
-          float acc = 0.f;
-#pragma unroll 8
-          for (int c = 0; c < H; c++) acc = fmaf(W[r][c], DZ[q][c], acc);
-          if (r < H)
-            dhd[(long)H * i + r] = dh[(long)H * i + r] + acc;
-          else
-            dms[(long)H * i + (r - H)] = acc * invdeg;
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+          const int r = 32 * warp + 8 * nt + 2 * tq;
+          const float v0 = acc[nt][2 * hrow], v1 = acc[nt][2 * hrow + 1];
+          if (r < H) {
+            const float2 d = *reinterpret_cast<const float2*>(dh + (long)H * i + r);
+            *reinterpret_cast<float2*>(dhd + (long)H * i + r) = make_float2(d.x + v0, d.y + v1);
+          } else {
+            *reinterpret_cast<float2*>(dms + (long)H * i + (r - H)) = make_float2(v0 * invdeg, v1 * invdeg);
+          }
         }
       }
     }
-    // weight gradient: thread owns row r = t (0..127), all 64 columns: X[:,r]^T DZ
-    {
-      const int r = threadIdx.x;
-#pragma unroll 4
-      for (int q = 0; q < MP_NODES; q++) {
-        const float x = X[q][r];
+    // weight gradient (128 x 64) += [h; m]^T (128 x 16) dz (16 x 64): warp w -> rows 32w ..
 #pragma unroll
-        for (int c = 0; c < 64; c++) gacc[c] = fmaf(x, DZ[q][c], gacc[c]);
+    for (int mt = 0; mt < 2; mt++) {
+      const int r0 = 32 * warp + 16 * mt;
+      const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&XT[r0 + g][2 * tq]);
+      const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&XT[r0 + g + 8][2 * tq]);
+      const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&XT[r0 + g][8 + 2 * tq]);
+      const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&XT[r0 + g + 8][8 + 2 * tq]);
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+#pragma unroll
+        for (int part = 0; part < 2; part++) {
+          const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&DZT[part][8 * nt + g][2 * tq]);
+          const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&DZT[part][8 * nt + g][8 + 2 * tq]);
+          mma_bf16_16816(gacc[mt][nt], a0, a1, a2, a3, b0, b1);
+        }
       }
-      if (r < H)
-        for (int q = 0; q < MP_NODES; q++) gb += DZ[q][r];
     }
+    if (threadIdx.x < H)
+      for (int q = 0; q < MP_NODES; q++)
+        gb += __bfloat162float(DZ[0][q][threadIdx.x]) + __bfloat162float(DZ[1][q][threadIdx.x]);
   }
   float* gp = gpart + (long)blockIdx.x * LAYER;
 #pragma unroll
-  for (int c = 0; c < 64; c++) gp[threadIdx.x * H + c] = gacc[c];
+  for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+      const int r = 32 * warp + 16 * mt + g, c = 8 * nt + 2 * tq;
+      *reinterpret_cast<float2*>(gp + (long)r * H + c) = make_float2(gacc[mt][nt][0], gacc[mt][nt][1]);
+      *reinterpret_cast<float2*>(gp + (long)(r + 8) * H + c) = make_float2(gacc[mt][nt][2], gacc[mt][nt][3]);
+    }
   if (threadIdx.x < H) gp[2 * H * H + threadIdx.x] = gb;
 }
 

@@ -1,6 +1,7 @@
 // Minimal-residual initial guess of a mixed-precision solve from the previous time
-// step's increment of the same Newton iteration (g) and, with the learned network, the
-// network's correction (d):
+// step's increment of the same Newton iteration and the current step's increment of
+// the previous Newton iteration (combined into g, guess_combine_kernel) and, with the
+// learned network, the network's correction (d):
 //   X0 = a1 g + a2 d,  (a1, a2) = argmin || r - a1 K g - a2 K d ||_2,
 // computed from FP64 dot products (deterministic CTA partials reduced in a fixed
 // order) by the 2x2 normal equations; with one direction a1 = (r . Kg) / (Kg . Kg).
@@ -103,7 +104,36 @@ __global__ void scale_f32_kernel(long n, const double* __restrict__ coef, const 
     p[k] = a * g[k];
 }
 
+// g = c1 g + c2 g2, w = c1 w + c2 w2: the minimal-residual combination of two
+// directions and its product
+__global__ void guess_combine_kernel(long n, const double* __restrict__ coef, double* __restrict__ g,
+                                     const double* __restrict__ g2, double* __restrict__ w,
+                                     const double* __restrict__ w2) {
+  const double c1 = coef[0], c2 = coef[1];
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    g[k] = c1 * g[k] + c2 * g2[k];
+    w[k] = c1 * w[k] + c2 * w2[k];
+  }
+}
+
+// p = a1 g in FP32 (the network's prior, from an FP64 direction)
+__global__ void scale_f64_f32_kernel(long n, const double* __restrict__ coef, const double* __restrict__ g,
+                                     float* __restrict__ p) {
+  const double a = coef[0];
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    p[k] = (float)(a * g[k]);
+}
+
 }  // namespace
+
+void launch_guess_combine(cudaStream_t s, long n, const double* coef, double* g, const double* g2, double* w,
+                          const double* w2) {
+  guess_combine_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, coef, g, g2, w, w2);
+}
+
+void launch_scale_f64_f32(cudaStream_t s, long n, const double* coef, const double* g, float* p) {
+  scale_f64_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, coef, g, p);
+}
 
 void launch_guess_dots(cudaStream_t s, long n, int nd, const double* const* a, const double* const* b, double* part,
                        int sm_count) {
