@@ -39,3 +39,17 @@ g++ $FLAGS -c "$HERE/lapack_shim.cpp" -o "$OUT/obj/lapack_shim.o"
 g++ $FLAGS $INC -c "$HERE/ref_unused_stubs.cpp" -o "$OUT/obj/ref_unused_stubs.o"
 g++ -o "$OUT/ref_harness" "$OUT/obj/harness.o" "$OUT/obj/lapack_shim.o" "$OUT/obj/ref_unused_stubs.o" "${objs[@]}" 2> "$OUT/link.err" || { head -50 "$OUT/link.err"; exit 1; }
 echo "built $OUT/ref_harness"
+# The reference-side GPU back-end, compiled against the
+# reference's headers and linked with its objects and the svgpu library: the check
+# that the back-end a maintainer adds builds as written (linked, not run).
+ROOT="$(dirname "$HERE")"
+SVLIB="$ROOT/svfsiplus_gb300/_build/libsvgpu.so"
+GINC="-I$ROOT/include -I$ROOT/svfsiplus_gb300/integration"
+g++ $FLAGS $INC $GINC -c "$ROOT/svfsiplus_gb300/integration/GpuLinearAlgebra.cpp" -o "$OUT/obj/GpuLinearAlgebra.o"
+g++ $FLAGS $INC $GINC -c "$HERE/gpu_backend_main.cpp" -o "$OUT/obj/gpu_backend_main.o"
+if [ -f "$SVLIB" ]; then
+  g++ -o "$OUT/gpu_backend_check" "$OUT/obj/gpu_backend_main.o" "$OUT/obj/GpuLinearAlgebra.o" \
+      "$OUT/obj/lapack_shim.o" "$OUT/obj/ref_unused_stubs.o" "${objs[@]}" "$SVLIB" -Wl,-rpath,"$(dirname "$SVLIB")" \
+      2> "$OUT/link_gpu.err" || { head -50 "$OUT/link_gpu.err"; exit 1; }
+  echo "built $OUT/gpu_backend_check"
+fi

@@ -154,3 +154,68 @@ def test_learned_initial_guess_ab(golden):
         assert a["ev"] <= 1e-6 and a["ep"] <= 1e-6
     assert arms["H"]["its"] < arms["A"]["its"]
     assert arms["L"]["its"] <= 1.05 * arms["H"]["its"]
+
+
+def _pipe50k_learned(g, ps, **kw):
+    m = named_pipe("pipe50k")
+    s = api.PipeFluidSolver(m, rowPtr=g["rowPtr"], colPtr=g["colPtr"], precision=api.SVGPU_MIXED, **kw)
+    s.enable_learning()
+    s.ctx.set_solver_mode(2)
+    return s
+
+
+def _train_then(s, ps, mode, steps=10, switch=6):
+    """Steps 1..switch-1 in mode 2 storing the solves' triples (Adam after steps 2..),
+    then the given mode with the network frozen."""
+    for step in range(1, steps + 1):
+        if step == switch:
+            s.ctx.gnn_collect(False)
+            s.ctx.set_solver_mode(mode)
+        st = s.step(u_mean=ps["u_mean"], u_amp=ps["u_amp"], freq=ps["u_freq"])
+        assert all(x["suc"] for x in st), (mode, step, st)
+        if step < switch and s.ctx.gnn_pair_count() > 0:
+            s.ctx.gnn_train(100, 1e-3)
+    return s
+
+
+@pytest.mark.parametrize("mode", [1, 3])
+def test_learned_modes_reach_reference_pipe50k(golden, mode):
+    """Mode 1 (the trained network as the only right preconditioner of FGMRES) and mode
+    3 (the trained network as the V-cycle's finest pre-smoother), at the reference's
+    settings on the 50k-tet pipe after 5 steps of online training: the fields after step
+    10 within 1e-6 of the reference's own.  Cycles that do not lower the FP64 residual
+    are rejected and the method without the network finishes the solve; the rejections
+    are printed."""
+    g = golden("pipe50k")
+    ps = eval(str(g["params"]))
+    s = _pipe50k_learned(g, ps, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
+                         absTol=ps["ls_abs_tol"], newton_min=ps["newton_min"], newton_max=ps["newton_max"],
+                         newton_tol=ps["newton_tol"])
+    r0 = s.ctx.learned_rejects
+    _train_then(s, ps, mode)
+    ref = g["Yn_10"]
+    ev, ep = rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])
+    print(f"mode {mode}: velocity {ev:.2e}, pressure {ep:.2e}, learned cycles rejected "
+          f"{s.ctx.learned_rejects - r0}")
+    assert ev <= 1e-6 and ep <= 1e-6
+    s.ctx.close()
+
+
+def test_headline_settings_pipe50k(golden):
+    """The headline's settings on the 50k-tet pipe: mixed precision, multilevel FGMRES(50)
+    from the learned initial guess (mode 4) after 5 steps of online training, tangent
+    kept within a step, the extrapolating Newton predictor, linear relative tolerance
+    1e-2, Newton to picc's 1e-8 (at most 8 iterations).  The reference ran the same 10
+    steps at its own settings (GMRES to 1e-8, 3 Newton iterations); the fields after step
+    10 must agree within 1e-6 per field."""
+    g = golden("pipe50k")
+    ps = eval(str(g["params"]))
+    s = _pipe50k_learned(g, ps, sD=50, mItr=40, relTol=1e-2, absTol=1e-17, newton_min=1, newton_max=8,
+                         newton_tol=1e-8, reuse_tangent=True)
+    s.ctx.set_predictor(1)
+    _train_then(s, ps, 4)
+    ref = g["Yn_10"]
+    ev, ep = rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])
+    print(f"headline settings on pipe50k: velocity {ev:.2e}, pressure {ep:.2e}, guesses {s.ctx.guess_stats}")
+    assert ev <= 1e-6 and ep <= 1e-6
+    s.ctx.close()
