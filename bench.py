@@ -844,10 +844,20 @@ def run_config1(args):
 
 def run_fsi(args):
     """The coupled ALE FSI pipe (lumen + 1 mm neo-Hookean wall, linear-elastic mesh
-    motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s): s per time step through the C ABI
-    (svgpu_fsi_step, host state copied in and out every step) for the multilevel
-    mixed-precision FSI solve and for the plain FP64 GMRES + diagonal solve, both from
-    rest over the same steps, and the per-field relative L2 difference of the two."""
+    motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s), every path from rest over the same
+    warm-up + timed steps through the C ABI (svgpu_fsi_step, host state copied in and
+    out every step):
+      learned    -- mixed-precision assembly (svgpu_construct_fsi_mixed), multilevel
+                    FGMRES started from the learned initial guess (mode 4; the network
+                    trained with Adam on the FSI solves' triples after every warm-up step);
+      history    -- the same without the network (mode 5);
+      multilevel -- the same from a zero guess (mode 2);
+      plain      -- (--fsi-plain) FP64, GMRES + diagonal preconditioner, the reference's method.
+    Each path's fields after every step are compared with the FP64 solution of the same
+    steps: FP64 assembly, both equations' Newton loops to 1e-10 with FGMRES to 1e-4 /
+    1e-6 on FP32 copies inside the FP64 defect correction.  Per-step time: the device
+    time between the step's inputs' arrival and its outputs' copy-back (value) and the
+    host clock around the call (e2e)."""
     import torch
     from svfsiplus_gb300 import api
     from svfsiplus_gb300.mesh import named_pipe
@@ -855,58 +865,73 @@ def run_fsi(args):
     name = args.workload if args.workload != WORKLOAD else "fsi5m"
     mesh = named_pipe(name)
     rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    nsteps = args.warmup + args.steps
     out = {"workload": name, "tets": mesh.nEl, "solid_tets": int((mesh.eid == 2).sum()), "nodes": mesh.nNo,
-           "blocks": int(colPtr.size), "mesh_rel_tol": args.mesh_cg_tol,
-           "mesh_solver_mixed_path": "multilevel FGMRES" if args.mesh_multilevel else "CG + diagonal"}
+           "blocks": int(colPtr.size), "warmup": args.warmup, "steps": args.steps,
+           "newton_tol": NEWTON_TOL, "fsi_lin_rel_tol": LIN_REL_TOL, "mesh_rel_tol": args.mesh_cg_tol}
+    solid = np.zeros(mesh.nNo, bool)
+    solid[mesh.ien[mesh.eid == 2].ravel()] = True
+    paths = ["fp64", "learned", "history", "multilevel"] + (["plain"] if args.fsi_plain else [])
     fields = {}
-    for path in ("history", "multilevel", "plain"):
-        mixed = path != "plain"
-        s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=(1, NEWTON_MAX, NEWTON_TOL),
-                              mesh_newton=(1, NEWTON_MAX, NEWTON_TOL),
-                              gmres=(LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM), cg=(args.mesh_cg_tol, 1e-17, 5000),
-                              rowPtr=rowPtr, colPtr=colPtr, precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
-                              mesh_gmres=(args.mesh_cg_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM)
-                              if (mixed and args.mesh_multilevel) else None)
-        if mixed:  # multilevel FGMRES; "history" starts both equations' solves from the
-            # previous step's increment of the same Newton iteration (mode 5)
-            s.ctx.set_solver_mode(5 if path == "history" else 2)
-        steps = []
-        for k in range(args.warmup + args.steps):
+    for path in paths:
+        tight = path == "fp64"
+        mixed = path in ("learned", "history", "multilevel")
+        newton = (1, 14, 1e-10) if tight else (1, NEWTON_MAX, NEWTON_TOL)
+        gm = (1e-4 if tight else LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM)
+        mesh_tol = 1e-6 if tight else args.mesh_cg_tol
+        s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=newton, mesh_newton=newton, gmres=gm,
+                              cg=(mesh_tol, 1e-17, 5000), rowPtr=rowPtr, colPtr=colPtr,
+                              precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
+                              mesh_gmres=(mesh_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM) if path != "plain" else None)
+        mode = {"fp64": 2, "learned": 5, "history": 5, "multilevel": 2, "plain": 0}[path]
+        if path == "learned":
+            s.ctx.gnn_create(api.pipe_node_features(mesh), 1)
+            s.ctx.gnn_collect(2)
+        s.ctx.set_solver_mode(mode)
+        steps, Ys, Ds = [], [], []
+        for k in range(nsteps):
+            if path == "learned" and k == args.warmup:
+                s.ctx.gnn_collect(False)
+                s.ctx.set_solver_mode(4)
             torch.cuda.synchronize()
             t = time.perf_counter()
             st = s.step(15.0, 5.0, 1.0)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t
-            rec = {"s": round(dt, 4), "fsi_its": [d["itr"] for q, d in st if q == 0],
-                   "mesh_its": [d["itr"] for q, d in st if q == 1],
-                   "fsi_solve_s": round(sum(d["callD"] for q, d in st if q == 0), 4),
-                   "mesh_solve_s": round(sum(d["callD"] for q, d in st if q == 1), 4),
-                   "fsi_final_over_first": [d["iNorm"] for q, d in st if q == 0][-1] /
-                                           [d["iNorm"] for q, d in st if q == 0][0],
-                   "timed": k >= args.warmup}
-            steps.append(rec)
-        timed = [r["s"] for r in steps if r["timed"]]
-        # phases of one more step (CUDA events at phase boundaries, outside the timed steps)
+            wall = time.perf_counter() - t
+            dev_ms = s.ctx.step_device_ms()
+            if path == "learned" and k < args.warmup and s.ctx.gnn_pair_count() > 0:
+                s.ctx.gnn_train(TRAIN_ITERS, TRAIN_LR)
+            steps.append({"device_s": round(dev_ms / 1e3, 4), "e2e_s": round(wall, 4),
+                          "fsi_its": [d["itr"] for q, d in st if q == 0],
+                          "mesh_its": [d["itr"] for q, d in st if q == 1], "timed": k >= args.warmup})
+            Ys.append(s.Yn.copy())
+            Ds.append(s.Dn.copy())
+        timed = [r for r in steps if r["timed"]]
+        # phases of one more step (CUDA events at phase boundaries)
         s.ctx.phase_timing(True)
         s.ctx.phase_times()
         s.step(15.0, 5.0, 1.0)
-        phases = {k: round(v[0], 2) for k, v in s.ctx.phase_times().items() if v[1]}
+        phases = {k2: round(v[0], 2) for k2, v in s.ctx.phase_times().items() if v[1]}
         s.ctx.phase_timing(False)
-        out[path] = {"s_per_step": float(np.mean(timed)), "steps": steps, "phases_ms_one_step": phases}
-        fields[path] = (s.Yn.copy(), s.Dn.copy())
-        solid = np.zeros(mesh.nNo, bool)
-        solid[s.solid_nodes] = True
+        out[path] = {"s_per_step": float(np.mean([r["device_s"] for r in timed])),
+                     "e2e_s_per_step": float(np.mean([r["e2e_s"] for r in timed])),
+                     "fsi_krylov_its_timed": int(sum(sum(r["fsi_its"]) for r in timed)),
+                     "guesses_tried_rejected_with_network": s.ctx.guess_stats if mode >= 4 else None,
+                     "phases_ms_one_step": phases, "steps": steps if args.steps <= 10 else None}
+        fields[path] = (Ys, Ds)
         s.ctx.close()
         torch.cuda.empty_cache()
     rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
-    Yp, Dp = fields["plain"]
-    for path in ("multilevel", "history"):
-        Ym, Dm = fields[path]
-        out[f"{path}_vs_fp64_rel_l2"] = {"velocity": rel(Ym[~solid, :3], Yp[~solid, :3]),
-                                         "pressure": rel(Ym[:, 3], Yp[:, 3]),
-                                         "solid_displacement": rel(Dm[solid, :3], Dp[solid, :3]),
-                                         "mesh_displacement": rel(Dm[:, 4:7], Dp[:, 4:7])}
-        out[f"speedup_plain_over_{path}"] = out["plain"]["s_per_step"] / out[path]["s_per_step"]
+    Yr, Dr = fields["fp64"]
+    for path in paths[1:]:
+        Ys, Ds = fields[path]
+        err = {"velocity": [rel(a[~solid, :3], b[~solid, :3]) for a, b in zip(Ys, Yr)],
+               "pressure": [rel(a[:, 3], b[:, 3]) for a, b in zip(Ys, Yr)],
+               "solid_displacement": [rel(a[solid, :3], b[solid, :3]) for a, b in zip(Ds, Dr)],
+               "mesh_displacement": [rel(a[:, 4:7], b[:, 4:7]) for a, b in zip(Ds, Dr)]}
+        out[path]["error_vs_fp64"] = {k: {"max": max(v), "last": v[-1]} for k, v in err.items()}
+        out[path]["error_vs_fp64"]["within_1e-6"] = bool(max(max(v) for v in err.values()) <= 1e-6)
+    for path in paths[2:]:
+        out[f"learned_speedup_over_{path}"] = out[path]["s_per_step"] / out["learned"]["s_per_step"]
     print(json.dumps({"fsi": out}), flush=True)
 
 
@@ -1141,8 +1166,8 @@ def main():
                     help="only the 50k-tet pipe at the reference's settings, 10 steps, GPU and CPU")
     ap.add_argument("--mesh-cg-tol", type=float, default=1e-3,
                     help="--fsi: relative tolerance of the mesh equation's solves")
-    ap.add_argument("--mesh-multilevel", type=int, default=1,
-                    help="--fsi: 1 solves the mixed path's mesh equation by the multilevel FGMRES, 0 by CG")
+    ap.add_argument("--fsi-plain", action="store_true",
+                    help="--fsi: also the reference's method (FP64 GMRES + diagonal; about 12 s per step on fsi5m)")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     ap.add_argument("--reuse-tangent", type=int, default=None,

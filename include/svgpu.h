@@ -180,6 +180,16 @@ int svgpu_mesh_domains(svgpu_ctx* ctx, const int* eId);
  * Val (16, nnz) are added to. */
 int svgpu_construct_fsi(svgpu_ctx* ctx, const svgpu_fluid_props* fluid, const svgpu_solid_props* solid, int tDof,
                         const double* Ag, const double* Yg, const double* Dg, double* R, double* Val);
+/* The same system in mixed precision (no reference counterpart): the ALE fluid
+ * elements' residual rows in double-word FP32 arithmetic (about 48 bits, accumulated
+ * into the FP64 R) and their tangent in FP32; the solid elements in FP64 arithmetic
+ * with FP64 rows and FP32 blocks.  Adds into R (4, nNo) and Val32 (16, nnz) as
+ * svgpu_construct_fsi adds into R and Val.  Device arrays only (16-byte aligned);
+ * svgpu_mesh_domains first.  svgpu_fsi_step with precision SVGPU_MIXED assembles this
+ * way. */
+int svgpu_construct_fsi_mixed(svgpu_ctx* ctx, const svgpu_fluid_props* fluid, const svgpu_solid_props* solid,
+                              int tDof, const double* Ag, const double* Yg, const double* Dg, double* R,
+                              float* Val32);
 /* Replaces construct_dsolid (solver/sv_struct.cpp:213, struct_3d_carray :552) for
  * linear tets: adds into R (dof,nNo) and Val (dof*dof,nnz), dof = 3 (the struct
  * equation) or 4 (the solid blocks of the FSI equation, fsi.cpp:213-262).  State
@@ -305,9 +315,11 @@ int svgpu_gnn_train(svgpu_ctx* ctx, int iters, float lr, double* loss);
  * then the better one is kept and the other retried every eighth visit); 5 as 2 with
  * the minimal-residual multiple of g alone (no network).
  * Initial guesses and flexible cycles that do not lower the FP64 residual, or whose
- * Arnoldi step breaks down (a zero or non-finite preconditioned vector), are rejected:
- * the solve goes on with the method without the learned part (mode 3: the plain
- * V-cycle; then, and in the other modes, plain FP32 GMRES cycles). */
+ * Arnoldi step breaks down (a zero or non-finite preconditioned vector), are rejected
+ * (rolled back): the solve goes on with the method without the learned part (after a
+ * cycle with the network, modes 1 and 3: the plain V-cycle; after a V-cycle: plain FP32
+ * GMRES cycles).  A cycle with the network that lowers the FP64 residual less than
+ * twofold is kept, and the solve goes on with the plain V-cycle. */
 int svgpu_set_solver_mode(svgpu_ctx* ctx, int mode);
 /* History of modes 4 and 5: the slot (0..15) whose previous increment the next mixed
  * solves use and replace; svgpu_fluid_step and svgpu_fsi_step set it to the Newton
@@ -428,12 +440,15 @@ typedef struct {
   const int* incL[2];
   int outletFace;   /* mesh face (svgpu_face_create) of the lumen outlet, -1 for none */
   double outletH;   /* Neumann value on it; backflow stabilisation in the moving configuration */
-  /* SVGPU_FP64 (fsils_solve as the reference) or SVGPU_MIXED: the FSI equation's solve
-   * takes an FP32 copy of the FP64-assembled tangent in the FP64 defect-correction loop,
-   * with the context's solver mode (svgpu_set_solver_mode) as preconditioner (GMRES
-   * only); a mesh equation set to GMRES is solved the same way, its dof-3 system padded
-   * to 4x4 blocks (a fourth unknown with a unit diagonal), in a solver context of its
-   * own on the same stream.  A mesh equation set to CG keeps the reference's FP64 CG. */
+  /* SVGPU_FP64: the FSI system assembled in FP64; with solver mode 0 (the default)
+   * fsils_solve as the reference, with a flexible solver mode (svgpu_set_solver_mode,
+   * no reference counterpart) solved on an FP32 copy of the FP64 tangent in the FP64
+   * defect-correction loop.  SVGPU_MIXED: assembled in mixed precision
+   * (svgpu_construct_fsi_mixed) and solved on its FP32 tangent in the FP64 defect
+   * correction with the context's solver mode (GMRES only).  In both flexible cases a
+   * mesh equation set to GMRES is solved the same way, its dof-3 system padded to 4x4
+   * blocks (a fourth unknown with a unit diagonal), in a solver context of its own on
+   * the same stream; a mesh equation set to CG keeps the reference's FP64 CG. */
   int precision;
 } svgpu_fsi_opts;
 

@@ -759,15 +759,20 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
       if (rc) return rc;
       if (learned && !(nrm < before)) {
         // the flexible cycle did not lower the true FP64 residual: undo it and go on
-        // with the method without the learned part (mode 3: the plain V-cycle), or,
-        // after a V-cycle, with plain GMRES cycles
+        // with the method without the learned part (after a cycle with the network:
+        // the plain V-cycle; after a V-cycle: plain GMRES cycles)
         ctx->learned_rejects++;
-        cycle_kind = cycle_kind == 4 ? 3 : 1;
+        cycle_kind = (cycle_kind == 2 || cycle_kind == 4) ? 3 : 1;
         learned = cycle_kind >= 2;
         SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.X.p, kw.mask.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, kw.rbak.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
                                         ctx->stream));
         nrm = before;
+      } else if ((cycle_kind == 2 || cycle_kind == 4) && nrm > 0.5 * before) {
+        // a cycle with the network that did not halve the FP64 residual: its progress
+        // is kept, the solve goes on with the plain V-cycle
+        ctx->learned_rejects++;
+        cycle_kind = 3;
       }
       st->fNorm = nrm;
       if (nrm <= eps) {
@@ -799,7 +804,7 @@ int gmres_mixed(svgpu_ctx* ctx, const float* Val32, const double* Rs, double* Xo
       // an untrained network's zero output): reject it like a cycle that did not lower
       // the FP64 residual, and go on without its preconditioner
       ctx->learned_rejects++;
-      cycle_kind = cycle_kind == 4 ? 3 : 1;
+      cycle_kind = (cycle_kind == 2 || cycle_kind == 4) ? 3 : 1;
       learned = cycle_kind >= 2;
       SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.X.p, kw.mask.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
       SVGPU_CUDA(ctx, cudaMemcpyAsync(kw.r64.p, kw.rbak.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
@@ -857,7 +862,7 @@ int solve_device_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
   launch_vmul(ctx->stream, n, kw.Wc.p, R);
   ctx->launches += 3;
   if ((rc = setup_coupled(ctx, 4, incL, res, kw.Wc.p))) return rc;
-  if (ctx->learned_mode >= 2) {
+  if (ctx->learned_mode >= 1) {  // mode 1 falls back to the V-cycle
     if (!ctx->amg && (rc = amg_build(ctx))) return rc;
     ctx->amg->gnn_smoother = ctx->learned_mode == 3 && ctx->gnn;
     ctx->amg_val0 = Val32;
@@ -1064,6 +1069,63 @@ int svgpu::solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL,
 }
 
 svgpu::FluidConsts svgpu::fluid_consts_of(const svgpu_fluid_props* p) { return fluid_consts(p); }
+
+namespace svgpu {
+
+SolidConsts solid_consts(const svgpu_solid_props* sp) {
+  SolidConsts c;
+  c.rho = sp->rho;
+  c.damping = sp->damping;
+  c.f[0] = sp->f[0];
+  c.f[1] = sp->f[1];
+  c.f[2] = sp->f[2];
+  c.C10 = sp->C10;
+  c.Kpen = sp->Kpen;
+  c.volType = sp->volType;
+  c.dt = sp->dt;
+  c.am = sp->am;
+  c.af = sp->af;
+  c.gam = sp->gam;
+  c.beta = sp->beta;
+  return c;
+}
+
+// The FSI equation's system in mixed precision on device arrays: the ALE fluid elements'
+// residual rows in double-word FP32 (dw copies of the node data, the current
+// coordinates and the mesh velocity) and their tangent in FP32; the solid elements in
+// FP64 arithmetic with FP64 rows and FP32 blocks.  Adds into R (4, nNo) and Val32.
+int construct_fsi_mixed_device(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp,
+                                      int ld, const double* Ag, const double* Yg, const double* Dg, double* R,
+                                      float* Val32) {
+  MeshData& m = *ctx->mesh;
+  if (m.split_fluid.empty()) return set_err(ctx, SVGPU_ESTATE, "construct_fsi: call svgpu_mesh_domains first");
+  const long n4 = 4L * ctx->nNo;
+  SVGPU_CUDA(ctx, ctx->xaw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Agw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Ygw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Ymw.resize(n4));
+  SVGPU_CUDA(ctx, ctx->Rw.resize(n4));
+  launch_to_dw_ale(ctx->stream, ctx->nNo, ld, m.x4.p, Ag, Yg, Dg, ctx->xaw.p, ctx->Agw.p, ctx->Ygw.p, ctx->Ymw.p);
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Rw.p, 0, n4 * sizeof(float2), ctx->stream));
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
+  ctx->launches++;
+  DwState dws{ctx->xaw.p, ctx->Agw.p, ctx->Ygw.p, ctx->Rw.p, ctx->Ymw.p};
+  const FluidConsts fc = fluid_consts(fp);
+  const SolidConsts c = solid_consts(sp);
+  for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+    const int e0 = m.color_start[k], sf = m.split_fluid[k], ss = m.split_solid[k];
+    launch_fluid_ale_mixed(ctx->stream, fc, e0, sf - e0, m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, ld, Ag, Yg, Dg,
+                           ctx->rowPtr.p, Val32, ctx->errflag.p, dws);
+    launch_struct_assembly_f32(ctx->stream, 4, c, sf, ss - sf, m.ien.p, m.boff.p, m.elem_id.p, m.x4.p, ld, 0, Ag, Yg,
+                               Dg, ctx->rowPtr.p, R, Val32, ctx->errflag.p);
+    ctx->launches += 3;
+  }
+  launch_add_dw(ctx->stream, n4, ctx->Rw.p, R);
+  ctx->launches++;
+  return check_errflag(ctx);
+}
+
+}  // namespace svgpu
 
 // =============================================================================== ABI
 extern "C" {
@@ -1672,26 +1734,26 @@ static int assemble_generic(svgpu_ctx* ctx, int dof, int tDof, const double* con
   return SVGPU_OK;
 }
 
+int svgpu_construct_fsi_mixed(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp, int tDof,
+                              const double* Ag, const double* Yg, const double* Dg, double* R, float* Val32) {
+  if (!ctx || !fp || !sp) return SVGPU_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (tDof < 7) return set_err(ctx, SVGPU_EINVAL, "construct_fsi: tDof must hold the FSI (4) and mesh (3) rows");
+  if (!ctx->mesh) return set_err(ctx, SVGPU_ESTATE, "assembly before mesh_create");
+  const void* arrays[5] = {Ag, Yg, Dg, R, Val32};
+  for (const void* a : arrays)
+    if (!a || !is_device_ptr(a) || (reinterpret_cast<uintptr_t>(a) & 15u))
+      return set_err(ctx, SVGPU_EINVAL, "construct_fsi_mixed: device arrays, 16-byte aligned");
+  return construct_fsi_mixed_device(ctx, fp, sp, tDof, Ag, Yg, Dg, R, Val32);
+}
+
 int svgpu_construct_fsi(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp, int tDof,
                         const double* Ag, const double* Yg, const double* Dg, double* R, double* Val) {
   if (!ctx || !fp || !sp) return SVGPU_EINVAL;
   cudaSetDevice(ctx->device);
   if (tDof < 7) return set_err(ctx, SVGPU_EINVAL, "construct_fsi: tDof must hold the FSI (4) and mesh (3) rows");
   const FluidConsts fc = fluid_consts(fp);
-  SolidConsts c;
-  c.rho = sp->rho;
-  c.damping = sp->damping;
-  c.f[0] = sp->f[0];
-  c.f[1] = sp->f[1];
-  c.f[2] = sp->f[2];
-  c.C10 = sp->C10;
-  c.Kpen = sp->Kpen;
-  c.volType = sp->volType;
-  c.dt = sp->dt;
-  c.am = sp->am;
-  c.af = sp->af;
-  c.gam = sp->gam;
-  c.beta = sp->beta;
+  const SolidConsts c = solid_consts(sp);
   const double* states[3] = {Ag, Yg, Dg};
   MeshData& m = *ctx->mesh;
   int k = 0;  // colour index of the next call

@@ -144,7 +144,11 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
   }
   if (opts->precision != SVGPU_FP64 && opts->precision != SVGPU_MIXED)
     return set_err(ctx, SVGPU_EINVAL, "fsi_step: bad precision");
-  const bool mixed = opts->precision == SVGPU_MIXED;
+  // mixed_asm: the FSI system assembled in mixed precision (construct_fsi_mixed_device);
+  // mixed: the solves run on the FP32 tangent in the FP64 defect correction -- with
+  // mixed_asm, or with FP64 assembly when a flexible solver mode is set
+  const bool mixed_asm = opts->precision == SVGPU_MIXED;
+  const bool mixed = mixed_asm || ctx->learned_mode != 0;
   if (mixed && opts->lsType[0] != SVGPU_LS_GMRES)
     return set_err(ctx, SVGPU_EINVAL, "fsi_step: the mixed-precision FSI solve is (F)GMRES");
   if (opts->outletFace >= 0 && !ctx->mfaces.count(opts->outletFace))
@@ -237,21 +241,31 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     if (cEq == 0) {
       // ls_alloc zeroes R and Val (ls.cpp:51-61); construct_fsi + the outlet's Neumann term
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, 4L * nNo * sizeof(double), ctx->stream));
-      SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val.p, 0, (size_t)16 * ctx->nnz * sizeof(double), ctx->stream));
-      if ((rc = svgpu_construct_fsi(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, ctx->Val.p))) break;
+      if (mixed_asm) {
+        // residual rows in double-word FP32 (fluid) and FP64 (solid), tangent in FP32
+        SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val32.p, 0, (size_t)16 * ctx->nnz * sizeof(float), ctx->stream));
+        if ((rc = construct_fsi_mixed_device(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, ctx->Val32.p)))
+          break;
+      } else {
+        SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val.p, 0, (size_t)16 * ctx->nnz * sizeof(double), ctx->stream));
+        if ((rc = svgpu_construct_fsi(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, ctx->Val.p))) break;
+      }
       if (opts->outletFace >= 0) {
         MeshFace& f = *ctx->mfaces[opts->outletFace];
         const FluidConsts fc = fluid_consts_of(&fp);
         for (size_t k = 0; k + 1 < f.color_start.size(); k++) {
           launch_neu_backflow_ale(ctx->stream, fc, opts->outletH, f.color_start[k],
                                   f.color_start[k + 1] - f.color_start[k], f.fien.p, f.inner.p, f.boff.p, m.x4.p, 7,
-                                  w.Yg.p, w.Do.p, ctx->rowPtr.p, ctx->R.p, ctx->Val.p);
+                                  w.Yg.p, w.Do.p, ctx->rowPtr.p, ctx->R.p, mixed_asm ? nullptr : ctx->Val.p,
+                                  mixed_asm ? ctx->Val32.p : nullptr);
           ctx->launches++;
         }
       }
-      if (mixed) {
+      if (mixed && !mixed_asm) {  // FP64 system, flexible solve on its FP32 copy
         launch_f64_to_f32(ctx->stream, (long)16 * ctx->nnz, ctx->Val.p, ctx->Val32.p);
         ctx->launches++;
+      }
+      if (mixed) {
         const int slot0 = ctx->hist_slot;  // the equation's Newton iteration is the history slot
         ctx->hist_slot = itr[0] - 1 < kHistSlots ? itr[0] - 1 : -1;
         rc = solve_mixed(ctx, ctx->R.p, ctx->Val32.p, opts->incL[0], &st);

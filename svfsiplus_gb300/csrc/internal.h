@@ -289,6 +289,7 @@ struct svgpu_ctx {
   bool resident_mixed = false;  // the resident tangent is Val32
   svgpu::DevBuf<double> Ag, Yg, An, Yn, Dn, Ao, Yo, Do, Bf, dirY, dirA;
   svgpu::DevBuf<float2> Agw, Ygw, Rw;  // double-word copies for the mixed residual
+  svgpu::DevBuf<float2> xaw, Ymw;      // ALE (FSI): current coordinates, mesh velocity
   svgpu::DevBuf<int> errflag;  // [0] status, [1] element id
   svgpu::KrylovWork kw;
   svgpu::PhaseTimer phases;
@@ -334,6 +335,11 @@ struct svgpu_ctx {
 };
 
 namespace svgpu {
+
+// The FSI equation's system in mixed precision on device arrays (construct_fsi's
+// fluid and solid elements): adds into R (4, nNo, FP64) and Val32.
+int construct_fsi_mixed_device(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp, int ld,
+                               const double* Ag, const double* Yg, const double* Dg, double* R, float* Val32);
 
 // Step timing (svgpu_step_device_ms): mark the start of a time step's device work (its
 // inputs enqueued) and its end (before its outputs are copied back); step_time_read
@@ -522,8 +528,18 @@ struct DwState {
   const float2* Ag;
   const float2* Yg;
   float2* R;
+  const float2* Ym = nullptr;  // ALE: the mesh velocity (4 per node, the 4th unused)
 };
 void launch_to_dw(cudaStream_t s, long n, const double* a, float2* b);
+// Double-word node data of an ALE fluid assembly from (ld, nNo) state arrays: the
+// current coordinates x + Dg(4..6), Ag and Yg rows 0..3, the mesh velocity Yg(4..6).
+void launch_to_dw_ale(cudaStream_t s, int nNo, int ld, const double* x4, const double* Ag, const double* Yg,
+                      const double* Dg, float2* xw, float2* Agw, float2* Ygw, float2* Ymw);
+// Mixed-precision ALE fluid elements of the FSI equation: residual rows in double-word
+// FP32 into dws.R, tangent blocks in FP32 into Val32.
+void launch_fluid_ale_mixed(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
+                            const int* elem_id, const double* x4, int ld, const double* Ag, const double* Yg,
+                            const double* Dg, const int* rowPtr, float* Val32, int* errflag, const DwState& dws);
 void launch_add_dw(cudaStream_t s, long n, const float2* a, double* b);
 // FP64 fluid elements of the FSI equation (ALE: state arrays with ld rows per node)
 void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien,
@@ -551,6 +567,11 @@ struct SolidConsts {
 struct MeshConsts {
   double E, nu, rho, dt, am, af, beta;
 };
+// neo-Hookean solid elements with FP64 arithmetic, FP64 residual rows and FP32 tangent blocks
+void launch_struct_assembly_f32(cudaStream_t st, int dof, const SolidConsts& c, int e0, int ne, const int* ien,
+                                const uint8_t* boff, const int* elem_id, const double* x4, int tDof, int s,
+                                const double* Ag, const double* Yg, const double* Dg, const int* rowPtr, double* R,
+                                float* Val32, int* errflag);
 void launch_struct_assembly(cudaStream_t st, int dof, const SolidConsts& c, int e0, int ne, const int* ien,
                             const uint8_t* boff, const int* elem_id, const double* x4, int tDof, int s,
                             const double* Ag, const double* Yg, const double* Dg, const int* rowPtr, double* R,
@@ -560,7 +581,8 @@ void launch_mesh_assembly(cudaStream_t st, const MeshConsts& c, int e0, int ne, 
                           const double* Do, const int* rowPtr, double* R, double* Val, int* errflag);
 void launch_neu_backflow_ale(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne, const int* fien,
                              const int* inner, const uint8_t* boff, const double* x4, int ld, const double* Yg,
-                             const double* Do, const int* rowPtr, double* R, double* Val64);
+                             const double* Do, const int* rowPtr, double* R, double* Val64,
+                             float* Val32 = nullptr);
 // ---- k_fsi.cu: generalised-alpha updates of the 7-row FSI state ------------------
 void launch_fsi_predict(cudaStream_t s, int nNo, const FsiCoefs& c, const double* Ao, const double* Yo,
                         const double* Do, double* An, double* Yn, double* Dn);

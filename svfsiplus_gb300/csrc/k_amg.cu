@@ -106,52 +106,7 @@ __global__ void to_half_kernel(long m, const float* __restrict__ v, __half* __re
 
 // r = b - A x with the FP16 matrix: 2 threads per block row, each one 16-byte load of
 // two rows of the block (8 halves) and one 16-byte load of x per block, FP32
-// accumulation.  Blocks go in groups of four whose loads are all issued before use, and
-// the column indices of the next group are loaded while the current group's x is
-// gathered (the x gather waits on its index, so the index latency would otherwise add
-// to every group); a group past the row's end loads nothing and adds zeros.
-__device__ __forceinline__ void half_block_fma(const uint4& raw, const float4& xv, float& a0, float& a1) {
-  const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
-  const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-  const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
-  const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
-  a0 = fmaf(v0.x, xv.x, a0);
-  a0 = fmaf(v0.y, xv.y, a0);
-  a0 = fmaf(v1.x, xv.z, a0);
-  a0 = fmaf(v1.y, xv.w, a0);
-  a1 = fmaf(v2.x, xv.x, a1);
-  a1 = fmaf(v2.y, xv.y, a1);
-  a1 = fmaf(v3.x, xv.z, a1);
-  a1 = fmaf(v3.y, xv.w, a1);
-}
-
-// Row products of a half-precision block matrix (2 threads per block row, q = the
-// thread's half of the block): a0, a1 = rows 2q, 2q + 1 of sum_k B_k x_{col k}.
-__device__ __forceinline__ void half_row_product(int k, int e, int q, const int* __restrict__ col,
-                                                 const __half* __restrict__ val, const float* __restrict__ x,
-                                                 float& a0, float& a1) {
-  int c[4];
-#pragma unroll
-  for (int u = 0; u < 4; u++) c[u] = k + u < e ? __ldg(col + k + u) : 0;
-  for (; k < e; k += 4) {
-    int cn[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) cn[u] = k + 4 + u < e ? __ldg(col + k + 4 + u) : 0;
-    uint4 raw[4];
-    float4 xv[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const bool on = k + u < e;
-      raw[u] = on ? __ldcs(reinterpret_cast<const uint4*>(val + 16L * (k + u) + 8 * q)) : make_uint4(0u, 0u, 0u, 0u);
-      xv[u] = on ? *reinterpret_cast<const float4*>(x + 4L * c[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) half_block_fma(raw[u], xv[u], a0, a1);
-#pragma unroll
-    for (int u = 0; u < 4; u++) c[u] = cn[u];
-  }
-}
-
+// accumulation
 __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __restrict__ rowPtr,
                                                          const int* __restrict__ colPtr,
                                                          const __half* __restrict__ val,
@@ -163,7 +118,39 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   const int q = (int)(t & 1);
   if (row >= n) return;
   float a0 = 0.f, a1 = 0.f;
-  half_row_product(rowPtr[row], rowPtr[row + 1], q, colPtr, val, x, a0, a1);
+  auto blk = [&](const uint4& raw, const float4& xv) {
+    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
+    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
+    a0 = fmaf(v0.x, xv.x, a0);
+    a0 = fmaf(v0.y, xv.y, a0);
+    a0 = fmaf(v1.x, xv.z, a0);
+    a0 = fmaf(v1.y, xv.w, a0);
+    a1 = fmaf(v2.x, xv.x, a1);
+    a1 = fmaf(v2.y, xv.y, a1);
+    a1 = fmaf(v3.x, xv.z, a1);
+    a1 = fmaf(v3.y, xv.w, a1);
+  };
+  const int e = rowPtr[row + 1];
+  int k = rowPtr[row];
+  for (; k + 3 < e; k += 4) {  // four blocks per step: all loads issued before use
+    int c[4];
+    uint4 raw[4];
+    float4 xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
+#pragma unroll
+    for (int u = 0; u < 4; u++) raw[u] = __ldcs(reinterpret_cast<const uint4*>(val + 16L * (k + u) + 8 * q));
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) blk(raw[u], xv[u]);
+  }
+  for (; k < e; k++) {
+    const int col = __ldg(colPtr + k);
+    blk(__ldcs(reinterpret_cast<const uint4*>(val + 16L * k + 8 * q)), *reinterpret_cast<const float4*>(x + 4L * col));
+  }
   const float2 bb = *reinterpret_cast<const float2*>(b + 4 * row + 2 * q);
   *reinterpret_cast<float2*>(r + 4 * row + 2 * q) = make_float2(bb.x - a0, bb.y - a1);
 }
@@ -258,7 +245,23 @@ __global__ void __launch_bounds__(256) correct_kernel(int n, const int* __restri
   const int q = (int)(t & 1);
   if (row >= n) return;
   float a0 = 0.f, a1 = 0.f;
-  half_row_product(apRow[row], apRow[row + 1], q, apCol, apVal, xc, a0, a1);
+  for (int k = apRow[row]; k < apRow[row + 1]; k++) {
+    const int col = __ldg(apCol + k);
+    const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(apVal + 16L * k + 8 * q));
+    const float4 xv = *reinterpret_cast<const float4*>(xc + 4L * col);
+    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
+    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
+    a0 = fmaf(v0.x, xv.x, a0);
+    a0 = fmaf(v0.y, xv.y, a0);
+    a0 = fmaf(v1.x, xv.z, a0);
+    a0 = fmaf(v1.y, xv.w, a0);
+    a1 = fmaf(v2.x, xv.x, a1);
+    a1 = fmaf(v2.y, xv.y, a1);
+    a1 = fmaf(v3.x, xv.z, a1);
+    a1 = fmaf(v3.y, xv.w, a1);
+  }
   const long o = 4 * row + 2 * q;
   const float2 pc = *reinterpret_cast<const float2*>(xc + 4L * agg[row] + 2 * q);
   float2 xr, rr;

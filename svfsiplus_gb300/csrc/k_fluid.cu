@@ -157,6 +157,13 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
       }
       yl[a][0] = dwv(y01.x, y01.y); yl[a][1] = dwv(y01.z, y01.w);
       yl[a][2] = dwv(y23.x, y23.y); yl[a][3] = dwv(y23.z, y23.w);
+      if (ALE) {  // the mesh velocity; xl above already holds the current coordinates
+        const float4* mw = reinterpret_cast<const float4*>(dws.Ym + 4L * nd[a]);
+        const float4 m01 = mw[0], m23 = mw[1];
+        ym[ALE ? a : 0][0] = dwv(m01.x, m01.y);
+        ym[ALE ? a : 0][1] = dwv(m01.z, m01.w);
+        ym[ALE ? a : 0][2] = dwv(m23.x, m23.y);
+      }
     }
   }
 #pragma unroll
@@ -627,6 +634,48 @@ void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int
       DwState{nullptr, nullptr, nullptr, nullptr});
 }
 
+namespace {
+__device__ __forceinline__ float2 split_dw(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+__global__ void to_dw_ale_kernel(int nNo, int ld, const double* __restrict__ x4, const double* __restrict__ Ag,
+                                 const double* __restrict__ Yg, const double* __restrict__ Dg,
+                                 float2* __restrict__ xw, float2* __restrict__ Agw, float2* __restrict__ Ygw,
+                                 float2* __restrict__ Ymw) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4L * nNo) return;
+  const long i = t >> 2;
+  const int k = (int)(t & 3);
+  const double* A = Ag + (long)ld * i;
+  const double* Y = Yg + (long)ld * i;
+  const double* D = Dg + (long)ld * i;
+  xw[t] = split_dw(k < 3 ? x4[t] + D[4 + k] : 0.0);  // x + Dg(4..6), as the FP64 kernel forms it
+  Agw[t] = split_dw(A[k]);
+  Ygw[t] = split_dw(Y[k]);
+  Ymw[t] = split_dw(k < 3 ? Y[4 + k] : 0.0);
+}
+}  // namespace
+
+void launch_to_dw_ale(cudaStream_t s, int nNo, int ld, const double* x4, const double* Ag, const double* Yg,
+                      const double* Dg, float2* xw, float2* Agw, float2* Ygw, float2* Ymw) {
+  to_dw_ale_kernel<<<(unsigned)((4L * nNo + 255) / 256), 256, 0, s>>>(nNo, ld, x4, Ag, Yg, Dg, xw, Agw, Ygw, Ymw);
+}
+
+void launch_fluid_ale_mixed(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
+                            const int* elem_id, const double* x4, int ld, const double* Ag, const double* Yg,
+                            const double* Dg, const int* rowPtr, float* Val32, int* errflag, const DwState& dws) {
+  if (ne <= 0) return;
+  const int grid = (ne + 127) / 128;
+  fluid_p1_kernel<dwf::dw, double, true, false, true><<<grid, 128, 0, s>>>(
+      c, e0, ne, ien, boff, elem_id, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, errflag, ld,
+      nullptr, dws);
+  fluid_p1_kernel<float, float, false, true, true><<<grid, 128, 0, s>>>(
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, nullptr, rowPtr, nullptr, Val32, errflag, ld, Dg,
+      DwState{nullptr, nullptr, nullptr, nullptr});
+}
+
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
                          const int* fien, const int* inner, const uint8_t* boff, const double* x4,
                          const double* Yg, const int* rowPtr, double* R, double* Val64, float* Val32) {
@@ -642,10 +691,15 @@ void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0,
 
 void launch_neu_backflow_ale(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne, const int* fien,
                              const int* inner, const uint8_t* boff, const double* x4, int ld, const double* Yg,
-                             const double* Do, const int* rowPtr, double* R, double* Val64) {
+                             const double* Do, const int* rowPtr, double* R, double* Val64, float* Val32) {
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
-  neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, ld, Yg, Do, rowPtr, R, Val64);
+  if (Val64 || !Val32)
+    neu_backflow_kernel<double><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, ld, Yg, Do, rowPtr, R,
+                                                     Val64);
+  else
+    neu_backflow_kernel<float><<<grid, 128, 0, s>>>(c, h, e0, ne, fien, inner, boff, x4, ld, Yg, Do, rowPtr, R,
+                                                    Val32);
 }
 
 void launch_pic_predict_extrap(cudaStream_t s, long n4, double dt, double gam, const double* Ao, const double* Aoo,

@@ -69,14 +69,15 @@ __device__ __forceinline__ double det3(const double a[3][3]) {
 }
 
 // one thread per element; state arrays are (tDof, nNo) with this equation's
-// displacement components at rows s..s+2
-template <int DOF>
+// displacement components at rows s..s+2; tangent blocks stored as TV (FP64, or FP32
+// for the mixed-precision FSI solve; the arithmetic is FP64 either way)
+template <int DOF, typename TV>
 __global__ void __launch_bounds__(128) struct_p1_kernel(SolidConsts c, int e0, int ne, const int* __restrict__ ien,
                                                         const uint8_t* __restrict__ boff, const int* __restrict__ elem_id,
                                                         const double* __restrict__ x4, int tDof, int s,
                                                         const double* __restrict__ Ag, const double* __restrict__ Yg,
                                                         const double* __restrict__ Dg, const int* __restrict__ rowPtr,
-                                                        double* __restrict__ R, double* __restrict__ Val,
+                                                        double* __restrict__ R, TV* __restrict__ Val,
                                                         int* __restrict__ errflag) {
   const int le = blockIdx.x * blockDim.x + threadIdx.x;
   if (le >= ne) return;
@@ -200,12 +201,12 @@ __global__ void __launch_bounds__(128) struct_p1_kernel(SolidConsts c, int e0, i
           for (int u = 0; u < 6; u++) sum += Dm[v][u] * Bm[b][u][j];
           DB[v][j] = sum;
         }
-      double* blk = Val + (long)DOF * DOF * (rowbase + boff[16L * e + 4 * a + b]);
+      TV* blk = Val + (long)DOF * DOF * (rowbase + boff[16L * e + 4 * a + b]);
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
           double BDB = 0.0;
           for (int v = 0; v < 6; v++) BDB += Bm[a][v][i] * DB[v][j];
-          blk[DOF * i + j] += (i == j ? T1 : 0.0) + 4.0 * w * afu * BDB;
+          blk[DOF * i + j] += (TV)((i == j ? T1 : 0.0) + 4.0 * w * afu * BDB);
         }
     }
   }
@@ -308,11 +309,25 @@ void launch_struct_assembly(cudaStream_t st, int dof, const SolidConsts& c, int 
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
   if (dof == 3)
-    struct_p1_kernel<3><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr, R, Val,
+    struct_p1_kernel<3, double><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr, R, Val,
                                               errflag);
   else
-    struct_p1_kernel<4><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr, R, Val,
+    struct_p1_kernel<4, double><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr, R, Val,
                                               errflag);
+}
+
+void launch_struct_assembly_f32(cudaStream_t st, int dof, const SolidConsts& c, int e0, int ne, const int* ien,
+                                const uint8_t* boff, const int* elem_id, const double* x4, int tDof, int s,
+                                const double* Ag, const double* Yg, const double* Dg, const int* rowPtr, double* R,
+                                float* Val32, int* errflag) {
+  if (ne <= 0) return;
+  const int grid = (ne + 127) / 128;
+  if (dof == 3)
+    struct_p1_kernel<3, float><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr,
+                                                     R, Val32, errflag);
+  else
+    struct_p1_kernel<4, float><<<grid, 128, 0, st>>>(c, e0, ne, ien, boff, elem_id, x4, tDof, s, Ag, Yg, Dg, rowPtr,
+                                                     R, Val32, errflag);
 }
 
 void launch_mesh_assembly(cudaStream_t st, const MeshConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,

@@ -46,6 +46,42 @@ def test_gpu_fsi_assembly_matches_reference(golden):
     assert er <= 1e-12 and ev <= 1e-12
 
 
+@pytest.mark.gpu
+def test_gpu_fsi_mixed_assembly_matches_reference(golden):
+    """svgpu_construct_fsi_mixed (the mixed-precision FSI step's assembly: fluid residual
+    rows in double-word FP32, fluid tangent in FP32, solid elements in FP64 arithmetic
+    with FP32 blocks) against the reference's FP64 system: R within 1e-12 relative (the
+    FP64 parity tolerance), Val within 1e-6 relative (FP32 storage and arithmetic)."""
+    import ctypes as C
+    import torch
+    from svfsiplus_gb300 import api
+    g = golden("fsi_small")
+    ps = eval(str(g["params"]))
+    m = named_pipe("small")
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(m.nNo, g["rowPtr"], g["colPtr"], 0)
+    ctx.mesh_create(m.x, m.ien)
+    ctx.mesh_domains(g["eid"])
+    fp = api.fluid_props(rho=ps["rho_f"], mu=ps["mu"], dt=ps["dt"], rho_inf=ps["rho_inf"],
+                         backflow_beta=ps["backflow_beta"])
+    sp = api.solid_props(ps["rho_s"], ps["E"], ps["nu"], ps["dt"], ps["rho_inf"])
+    sp.am, sp.af, sp.gam, sp.beta = fp.am, fp.af, fp.gam, fp.beta
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()  # noqa: E731
+    A, Y, D = dev(g["A"]), dev(g["Y"]), dev(g["D"])
+    for _ in range(2):  # a second call into cleared arrays gives the same system
+        R = torch.zeros((m.nNo, 4), dtype=torch.float64, device="cuda")
+        V = torch.zeros((g["colPtr"].size, 16), dtype=torch.float32, device="cuda")
+        ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+        rc = api.lib().svgpu_construct_fsi_mixed(ctx._h, C.byref(fp), C.byref(sp), 7, ptr(A), ptr(Y), ptr(D), ptr(R),
+                                                 ptr(V))
+        assert rc == 0, api.lib().svgpu_last_error(ctx._h)
+        er = rel(R.cpu().numpy(), g["R_asm"])
+        ev = rel(V.cpu().numpy().astype(np.float64), g["Val_asm"])
+        print("mixed FSI assembly rel err: R", er, "Val", ev)
+        assert er <= 1e-12 and ev <= 1e-6
+    ctx.close()
+
+
 # ---- coupled FSI time steps (iterate_solution with the FSI and mesh equations) -------
 # Golden: tests/golden/ref_fsi_run_small.npz, made by make_golden.py from the compiled
 # reference (main.cpp's loop with construct_fsi, construct_mesh, b_assem_neu_bc on the
@@ -180,13 +216,15 @@ def test_gpu_fsi_steps_mixed_multilevel(golden):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [2, 5])
+@pytest.mark.parametrize("mode", [2, 5, 4])
 def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden, mode):
     """The mixed path with the mesh equation solved by the multilevel FGMRES as well (its
     dof-3 system padded to 4x4 blocks in a solver context of its own): per-field
     relative L2 within 1e-6 of the reference's fields after every step.  Mode 5 starts
     both equations' solves from the previous step's increment of the same Newton
-    iteration (kept only where it lowers the FP64 residual)."""
+    iteration (kept only where it lowers the FP64 residual); mode 4 adds the learned
+    network's correction to the FSI equation's guess, trained on the FSI solves of
+    steps 1-2 (stored triples, Adam) and used in step 3."""
     from svfsiplus_gb300 import api
     g = golden("fsi_run_small")
     ps = _run_params(g)
@@ -196,10 +234,18 @@ def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden, mode):
     s = api.PipeFsiSolver(m, p, newton=(3, 3, 1e-11), mesh_newton=(3, 3, 1e-11),
                           gmres=(ps["ls_rel_tol"], ps["ls_abs_tol"], ps["ls_max_itr"], ps["ls_krylov_dim"]),
                           precision=api.SVGPU_MIXED, mesh_gmres=(1e-10, 1e-17, 100, 50))
-    s.ctx.set_solver_mode(mode)
+    if mode == 4:
+        s.ctx.gnn_create(api.pipe_node_features(m), 1)
+        s.ctx.gnn_collect(1)
+    s.ctx.set_solver_mode(5 if mode == 4 else mode)
     solid = np.zeros(m.nNo, bool)
     solid[s.solid_nodes] = True
     for step in (1, 2, 3):
+        if mode == 4 and step == 3:
+            assert s.ctx.gnn_pair_count() > 0
+            s.ctx.gnn_train(100, 1e-3)
+            s.ctx.gnn_collect(False)
+            s.ctx.set_solver_mode(4)
         st = s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"])
         assert all(d["suc"] == 1 for _, d in st)
         Yr, Dr = g[f"Yn_{step}"], g[f"Dn_{step}"]

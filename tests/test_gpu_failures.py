@@ -164,8 +164,7 @@ def test_bad_network_cycles_are_rejected(golden, mode):
     breaks down) as the only right preconditioner of FGMRES; mode 3 uses a network with
     a NaN in its decoder as the V-cycle's finest pre-smoother (every cycle ends with a
     non-finite Arnoldi norm).  Those cycles are rejected (learned_rejects > 0) and each
-    solve is finished by the method without the learned part (mode 1: plain FP32 GMRES
-    cycles with the diagonal preconditioner; mode 3: the plain V-cycle); the fields
+    solve is finished by the method without the learned part (the plain V-cycle); the fields
     after steps 1 and 2 match the reference's own run (ref_small) within 1e-6."""
     g = golden("small")
     ps = eval(str(g["params"]))

@@ -183,9 +183,9 @@ def test_learned_modes_reach_reference_pipe50k(golden, mode):
     """Mode 1 (the trained network as the only right preconditioner of FGMRES) and mode
     3 (the trained network as the V-cycle's finest pre-smoother), at the reference's
     settings on the 50k-tet pipe after 5 steps of online training: the fields after step
-    10 within 1e-6 of the reference's own.  Cycles that do not lower the FP64 residual
-    are rejected and the method without the network finishes the solve; the rejections
-    are printed."""
+    10 within 1e-6 of the reference's own.  Cycles with the network that do not lower
+    the FP64 residual are rolled back, those that do not halve it are kept; in either case
+    the plain V-cycle finishes the solve.  The network's cycles given up are printed."""
     g = golden("pipe50k")
     ps = eval(str(g["params"]))
     s = _pipe50k_learned(g, ps, sD=ps["ls_krylov_dim"], mItr=ps["ls_max_itr"], relTol=ps["ls_rel_tol"],
