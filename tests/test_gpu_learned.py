@@ -205,17 +205,23 @@ def test_headline_settings_pipe50k(golden):
     """The headline's settings on the 50k-tet pipe: mixed precision, multilevel FGMRES(50)
     from the learned initial guess (mode 4) after 5 steps of online training, tangent
     kept within a step, the extrapolating Newton predictor, linear relative tolerance
-    1e-2, Newton to picc's 1e-8 (at most 8 iterations).  The reference ran the same 10
-    steps at its own settings (GMRES to 1e-8, 3 Newton iterations); the fields after step
-    10 must agree within 1e-6 per field."""
+    1e-2, Newton to picc's 1e-8 (at most 8 iterations).  Checked against the reference
+    run to convergence on the same 10 steps (ref_pipe50k_conv: the compiled reference,
+    Newton to 1e-11 within 12 iterations, GMRES to 1e-8): per-field relative L2 within
+    1e-6 after step 10.  The reference's fixed-3-iteration run (ref_pipe50k) is itself
+    1e-7 (velocity) and 1.4e-6 (pressure) from its converged solution at step 10, so
+    the settings are held to the converged one."""
     g = golden("pipe50k")
+    gc = golden("pipe50k_conv")
     ps = eval(str(g["params"]))
     s = _pipe50k_learned(g, ps, sD=50, mItr=40, relTol=1e-2, absTol=1e-17, newton_min=1, newton_max=8,
                          newton_tol=1e-8, reuse_tangent=True)
     s.ctx.set_predictor(1)
     _train_then(s, ps, 4)
-    ref = g["Yn_10"]
+    ref = gc["Yn_10"]
     ev, ep = rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])
-    print(f"headline settings on pipe50k: velocity {ev:.2e}, pressure {ep:.2e}, guesses {s.ctx.guess_stats}")
+    e3v, e3p = rel(g["Yn_10"][:, :3], ref[:, :3]), rel(g["Yn_10"][:, 3], ref[:, 3])
+    print(f"headline settings on pipe50k vs the converged reference: velocity {ev:.2e}, pressure {ep:.2e} "
+          f"(the reference's 3-iteration run: {e3v:.2e}, {e3p:.2e}); guesses {s.ctx.guess_stats}")
     assert ev <= 1e-6 and ep <= 1e-6
     s.ctx.close()
