@@ -270,17 +270,20 @@ def spmv_roofline(ctx, colPtr, nNo, mode, stream, reps=20):
     bytes_ = spmv_bytes(colPtr.size, nNo, vb, vb)
     peak, kind = peaks()
     achieved = bytes_ / (ms * 1e-3) / 1e9
-    # DRAM bytes per launch of this kernel on the 8M-tet pipe from one ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum, mean of two launches)
+    # DRAM bytes per launch of this kernel on the 8M-tet pipe from one ncu capture of the
+    # unchanged kernel (dram__bytes_read.sum + dram__bytes_write.sum, mean of two
+    # launches; the command is in profiles/spmv4_f32_pipe8m_traffic.md): ncu cannot run
+    # inside this timed program, so the capture is a separate run of the same kernel
     traffic = TRAFFIC_SPMV4_F32_PIPE8M if (mode >= 0 and colPtr.size == BLOCKS_PIPE8M) else None
     return {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
-            "traffic_source": "ncu capture of spmv4_f32_kernel on pipe8m" if traffic else None, "launch_ms": ms,
+            "traffic_source": "separate ncu capture of spmv4_f32_kernel on pipe8m (1.063-1.067 x algorithmic)"
+            if traffic else None, "launch_ms": ms,
             "algorithmic_bytes": bytes_, "launches_timed": reps}
 
 
 BLOCKS_PIPE8M = 20334561
-TRAFFIC_SPMV4_F32_PIPE8M = 1.5249e9
+TRAFFIC_SPMV4_F32_PIPE8M = 1.5245e9
 
 
 def kernel_breakdown(step_fn, path):
@@ -726,48 +729,38 @@ def run_study(args):
 
 
 def run_sweep(args):
-    """The mixed multilevel path (the headline's settings) on pipes of several sizes:
-    s per time step and, at every step, the per-field relative L2 difference from the
-    FP64 solution of the same steps.  The FP64 solution is the Newton iteration on the
-    FP64 residual driven to a tight tolerance (relative 1e-10, linear relative 1e-4): the
-    FP32 tangent and Krylov basis change only the path of that iteration, not its fixed
-    point, which the FP64 residual alone defines."""
+    """The mixed-precision path (FP32 tangent and Krylov basis, double-word residual
+    rows, multilevel FGMRES, the headline's Newton and linear tolerances, the
+    extrapolating predictor) on pipes of several sizes: s per time step and, at every
+    step, the per-field relative L2 difference from the FP64 solution of the same steps
+    from the same start (fp64_solution: FP64 assembly, Newton to 1e-10).  Every run
+    starts from rest; the first `warmup` steps are run and compared but not timed."""
     import torch
     from svfsiplus_gb300 import api
     from svfsiplus_gb300.mesh import named_pipe
 
-    sizes = args.sweep.split(",")
-    for name in sizes:
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    for name in args.sweep.split(","):
         mesh = named_pipe(name)
         rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
-        runs = {}
-        for kind in ("headline", "fp64_tight"):
-            tight = kind == "fp64_tight"
-            s, _ = make_solver(api, mesh, rowPtr, colPtr, "multilevel", newton_tol=1e-10 if tight else None,
-                               newton_max=14 if tight else None, lin_rel_tol=1e-4 if tight else None)
-            s.ctx.set_solver_mode(2)
-            recs = []
-            for k in range(args.steps):
-                torch.cuda.synchronize()
-                t = time.perf_counter()
-                st = s.step(U_MEAN, U_AMP, U_FREQ)
-                torch.cuda.synchronize()
-                recs.append({"s": time.perf_counter() - t, "newton": len(st), "krylov": sum(q["itr"] for q in st),
-                             "final_over_first": st[-1]["iNorm"] / st[0]["iNorm"], "Y": s.Yn.copy()})
-            runs[kind] = recs
-            s.ctx.close()
-            torch.cuda.empty_cache()
-        rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
-        steps = []
-        for a, b in zip(runs["headline"], runs["fp64_tight"]):
-            steps.append({"s": round(a["s"], 4), "newton": a["newton"], "krylov": a["krylov"],
-                          "final_over_first": a["final_over_first"],
-                          "velocity_rel_l2": rel(a["Y"][:, :3], b["Y"][:, :3]),
-                          "pressure_rel_l2": rel(a["Y"][:, 3], b["Y"][:, 3]),
-                          "fp64_newton": b["newton"], "fp64_final_over_first": b["final_over_first"]})
+        s, _ = make_solver(api, mesh, rowPtr, colPtr, "multilevel", 0)
+        api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
+        snap = snapshot(s)  # rest
+        rec = timed_steps(s, args.warmup + args.steps, keep_fields=True)
+        s.ctx.close()
+        torch.cuda.empty_cache()
+        ref = fp64_solution(api, mesh, rowPtr, colPtr, snap, args.warmup + args.steps, 0, stream)
+        ev, ep = field_errors(rec["Y"], ref)
+        dev = rec["device_ms"][args.warmup:]
         print(json.dumps({"sweep": name, "tets": mesh.nEl, "nodes": mesh.nNo, "blocks": int(colPtr.size),
-                          "s_per_step_after_first": float(np.mean([q["s"] for q in steps[1:]] or [steps[0]["s"]])),
-                          "steps": steps}), flush=True)
+                          "s_per_step": float(np.mean(dev)) / 1e3, "timed_steps": args.steps,
+                          "newton": [len(q) for q in rec["stats"]],
+                          "krylov": [sum(r["itr"] for r in q) for q in rec["stats"]],
+                          "velocity_rel_l2": [float("%.3g" % v) for v in ev],
+                          "pressure_rel_l2": [float("%.3g" % v) for v in ep],
+                          "max_velocity": max(ev), "max_pressure": max(ep),
+                          "fp64_newton": [r[1] for r in ref]}), flush=True)
 
 
 def config1_gpu(api):

@@ -104,9 +104,10 @@ __global__ void to_half_kernel(long m, const float* __restrict__ v, __half* __re
     h[k] = __float2half_rn(fminf(fmaxf(v[k], -65504.f), 65504.f));
 }
 
-// r = b - A x with the FP16 matrix: 2 threads per block row, each one 16-byte load of
-// two rows of the block (8 halves) and one 16-byte load of x per block, FP32
-// accumulation
+// r = b - A x with the FP16 matrix: 4 threads per block row (the mapping of the FP32
+// Krylov product spmv4_f32_kernel), each one 8-byte load of its row of the block (4
+// halves) and one 16-byte load of x per block, FP32 accumulation; four blocks per step,
+// all loads issued before use.
 __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __restrict__ rowPtr,
                                                          const int* __restrict__ colPtr,
                                                          const __half* __restrict__ val,
@@ -114,34 +115,28 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
                                                          float* __restrict__ r, const int* flags) {
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long row = t >> 1;
-  const int q = (int)(t & 1);
+  const long row = t >> 2;
+  const int q = (int)(t & 3);
   if (row >= n) return;
-  float a0 = 0.f, a1 = 0.f;
-  auto blk = [&](const uint4& raw, const float4& xv) {
+  float acc = 0.f;
+  auto blk = [&](const uint2& raw, const float4& xv) {
     const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
     const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
-    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
-    a0 = fmaf(v0.x, xv.x, a0);
-    a0 = fmaf(v0.y, xv.y, a0);
-    a0 = fmaf(v1.x, xv.z, a0);
-    a0 = fmaf(v1.y, xv.w, a0);
-    a1 = fmaf(v2.x, xv.x, a1);
-    a1 = fmaf(v2.y, xv.y, a1);
-    a1 = fmaf(v3.x, xv.z, a1);
-    a1 = fmaf(v3.y, xv.w, a1);
+    acc = fmaf(v0.x, xv.x, acc);
+    acc = fmaf(v0.y, xv.y, acc);
+    acc = fmaf(v1.x, xv.z, acc);
+    acc = fmaf(v1.y, xv.w, acc);
   };
   const int e = rowPtr[row + 1];
   int k = rowPtr[row];
-  for (; k + 3 < e; k += 4) {  // four blocks per step: all loads issued before use
+  for (; k + 3 < e; k += 4) {
     int c[4];
-    uint4 raw[4];
+    uint2 raw[4];
     float4 xv[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
 #pragma unroll
-    for (int u = 0; u < 4; u++) raw[u] = __ldcs(reinterpret_cast<const uint4*>(val + 16L * (k + u) + 8 * q));
+    for (int u = 0; u < 4; u++) raw[u] = __ldcs(reinterpret_cast<const uint2*>(val + 16L * (k + u) + 4 * q));
 #pragma unroll
     for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
 #pragma unroll
@@ -149,10 +144,9 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   }
   for (; k < e; k++) {
     const int col = __ldg(colPtr + k);
-    blk(__ldcs(reinterpret_cast<const uint4*>(val + 16L * k + 8 * q)), *reinterpret_cast<const float4*>(x + 4L * col));
+    blk(__ldcs(reinterpret_cast<const uint2*>(val + 16L * k + 4 * q)), *reinterpret_cast<const float4*>(x + 4L * col));
   }
-  const float2 bb = *reinterpret_cast<const float2*>(b + 4 * row + 2 * q);
-  *reinterpret_cast<float2*>(r + 4 * row + 2 * q) = make_float2(bb.x - a0, bb.y - a1);
+  r[4 * row + q] = b[4 * row + q] - acc;
 }
 
 
@@ -318,7 +312,7 @@ void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h) {
 
 void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
                     const float* b, float* r, const int* flags) {
-  spmv_res_h_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+  spmv_res_h_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
       n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, b, r, flags);
 }
 
