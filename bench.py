@@ -763,6 +763,86 @@ def run_sweep(args):
                           "fp64_newton": [r[1] for r in ref]}), flush=True)
 
 
+def run_tol_study(args):
+    """The timed steps' error against the FP64 solution as the Newton tolerance and the
+    predictor change: one warm-up from rest (history path, 5 steps), then for each
+    variant the same `steps` steps from that state through the C ABI, every field after
+    every step compared with fp64_solution from the same start."""
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    mesh = named_pipe(args.workload)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    s, mode = make_solver(api, mesh, rowPtr, colPtr, "history", 0)
+    api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
+    warm_up(api, s, mode, args.warmup)
+    snap = snapshot(s)
+    s.ctx.close()
+    ref = fp64_solution(api, mesh, rowPtr, colPtr, snap, args.steps, 0, stream)
+    for spec in args.tol_study.split(","):
+        f = spec.split(":")
+        tol, pred, prec = f[0], f[1] if len(f) > 1 else "1", f[2] if len(f) > 2 else "mixed"
+        s, mode = make_solver(api, mesh, rowPtr, colPtr, "history", 0, newton_tol=float(tol),
+                              precision=api.SVGPU_FP64 if prec == "fp64" else None)
+        s.ctx.set_predictor(int(pred))
+        api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
+        restore(s, snap)
+        rec = timed_steps(s, args.steps, keep_fields=True)
+        ev, ep = field_errors(rec["Y"], ref)
+        summ = step_summary(rec)
+        print(json.dumps({"workload": args.workload, "newton_tol": float(tol), "predictor": int(pred),
+                          "assembly": prec,
+                          "s_per_step": round(summ["s_per_step"], 4), "newton": summ["newton_iters"],
+                          "krylov": summ["krylov_iters_per_step"], "max_velocity": max(ev), "max_pressure": max(ep),
+                          "pressure_rel_l2": [float("%.2g" % v) for v in ep]}), flush=True)
+        s.ctx.close()
+        torch.cuda.empty_cache()
+
+
+def run_fsi_assembly(args):
+    """The FSI equation's system assembly on an FSI pipe (device arrays, seeded state):
+    svgpu_construct_fsi (FP64) and svgpu_construct_fsi_mixed (double-word residual rows,
+    FP32 tangent), host clock around `steps` synchronised calls after one warm-up call."""
+    import ctypes
+    import torch
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    name = args.workload if args.workload != WORKLOAD else "fsi5m"
+    m = named_pipe(name)
+    rowPtr, colPtr = api.csr_pattern(m.nNo, m.ien)
+    ctx = api.Context(0)
+    ctx.fsils_lhs_create(m.nNo, rowPtr, colPtr, 0)
+    ctx.mesh_create(m.x, m.ien)
+    ctx.mesh_domains(m.eid)
+    p = api.fsi_props()
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    rnd = lambda sc: sc * torch.randn((m.nNo, 7), dtype=torch.float64, device="cuda", generator=gen)  # noqa: E731
+    A, Y, D = rnd(0.01), rnd(0.1), rnd(1e-4)
+    R = torch.zeros((m.nNo, 4), dtype=torch.float64, device="cuda")
+    V64 = torch.zeros((colPtr.size, 16), dtype=torch.float64, device="cuda")
+    V32 = torch.zeros((colPtr.size, 16), dtype=torch.float32, device="cuda")
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    calls = {"fp64": lambda: api.lib().svgpu_construct_fsi(ctx._h, ctypes.byref(p.fluid), ctypes.byref(p.solid), 7,
+                                                           ptr(A), ptr(Y), ptr(D), ptr(R), ptr(V64)),
+             "mixed": lambda: api.lib().svgpu_construct_fsi_mixed(ctx._h, ctypes.byref(p.fluid),
+                                                                  ctypes.byref(p.solid), 7, ptr(A), ptr(Y), ptr(D),
+                                                                  ptr(R), ptr(V32))}
+    out = {"workload": name, "tets": m.nEl, "solid_tets": int((m.eid == 2).sum())}
+    for k, fn in calls.items():
+        if fn() != 0:
+            raise RuntimeError(api.lib().svgpu_last_error(ctx._h).decode())
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        out[k + "_ms"] = (time.perf_counter() - t) * 1e3 / args.steps
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def config1_gpu(api):
     """The CPU-runnable case at the reference's settings (the 50k-tet pipe, 10 time
     steps, 3 Newton iterations each, GMRES(50) + diagonal preconditioner to relative
@@ -1161,6 +1241,10 @@ def main():
                     help="--fsi: relative tolerance of the mesh equation's solves")
     ap.add_argument("--fsi-plain", action="store_true",
                     help="--fsi: also the reference's method (FP64 GMRES + diagonal; about 12 s per step on fsi5m)")
+    ap.add_argument("--tol-study", default=None,
+                    help="comma-separated 'newton_tol[:predictor[:mixed|fp64]]': error vs the FP64 solution per "
+                         "variant (fp64: FP64 assembly, the same flexible solve)")
+    ap.add_argument("--fsi-assembly", action="store_true", help="time the FSI system assembly, FP64 and mixed")
     ap.add_argument("--sweep", default=None, help="comma-separated pipes: mixed path vs the FP64 solution per step")
     ap.add_argument("--lin-rel-tol", type=float, default=None, help="linear relative tolerance of every solve")
     ap.add_argument("--reuse-tangent", type=int, default=None,
@@ -1190,6 +1274,10 @@ def main():
         run_config1(args)
     elif args.sweep:
         run_sweep(args)
+    elif args.tol_study:
+        run_tol_study(args)
+    elif args.fsi_assembly:
+        run_fsi_assembly(args)
     elif args.long:
         run_long(args)
     elif args.increments:
