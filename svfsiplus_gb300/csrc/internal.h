@@ -259,6 +259,7 @@ struct svgpu_ctx {
   // restart cycles as CUDA graphs (default) or as individual launches (environment
   // SVGPU_GRAPHS=0 at context creation: per-kernel profilers see plain launches)
   bool use_graphs = true;
+  bool krylov_half = false;  // the flexible cycles' Krylov product with the V-cycle's FP16 matrix
   // multilevel preconditioner options (svgpu_multilevel_options)
   float ml_omega = 0.7f;
   int ml_coarse_sweeps = 30;
@@ -464,6 +465,8 @@ int launch_multidot(cudaStream_t s, long n, int m, const double* V, long ldv, co
                     double* partial, int sm_count);
 void launch_reduce_partials(cudaStream_t s, int nparts, int m, const double* partial, double* out);
 int multidot_ctas(long n, int sm_count);
+// CTAs of the FP32 float4 dot kernel (launch_multidot32): its partials need this many rows
+int multidot32_ctas(long n, int sm_count);
 void launch_residual_init(cudaStream_t s, long n, const double* R, double* u0, double* X, bool x_zero,
                           const double* AX);
 void launch_scale_by_inv_norm(cudaStream_t s, long n, double* u, const double* nrm2, double* err0,

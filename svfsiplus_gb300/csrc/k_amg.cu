@@ -5,6 +5,7 @@
 #include <cuda_fp16.h>
 
 #include "amg.h"
+#include "bsr4.cuh"
 
 namespace svgpu {
 
@@ -104,10 +105,8 @@ __global__ void to_half_kernel(long m, const float* __restrict__ v, __half* __re
     h[k] = __float2half_rn(fminf(fmaxf(v[k], -65504.f), 65504.f));
 }
 
-// r = b - A x with the FP16 matrix: 4 threads per block row (the mapping of the FP32
-// Krylov product spmv4_f32_kernel), each one 8-byte load of its row of the block (4
-// halves) and one 16-byte load of x per block, FP32 accumulation; four blocks per step,
-// all loads issued before use.
+// r = b - A x with the FP16 matrix (r = A x when b is null), FP32 accumulation; 4
+// lanes per block row, each taking whole blocks (bsr4_row).
 __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __restrict__ rowPtr,
                                                          const int* __restrict__ colPtr,
                                                          const __half* __restrict__ val,
@@ -117,36 +116,9 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
   const int q = (int)(t & 3);
-  if (row >= n) return;
-  float acc = 0.f;
-  auto blk = [&](const uint2& raw, const float4& xv) {
-    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
-    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-    acc = fmaf(v0.x, xv.x, acc);
-    acc = fmaf(v0.y, xv.y, acc);
-    acc = fmaf(v1.x, xv.z, acc);
-    acc = fmaf(v1.y, xv.w, acc);
-  };
-  const int e = rowPtr[row + 1];
-  int k = rowPtr[row];
-  for (; k + 3 < e; k += 4) {
-    int c[4];
-    uint2 raw[4];
-    float4 xv[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
-#pragma unroll
-    for (int u = 0; u < 4; u++) raw[u] = __ldcs(reinterpret_cast<const uint2*>(val + 16L * (k + u) + 4 * q));
-#pragma unroll
-    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
-#pragma unroll
-    for (int u = 0; u < 4; u++) blk(raw[u], xv[u]);
-  }
-  for (; k < e; k++) {
-    const int col = __ldg(colPtr + k);
-    blk(__ldcs(reinterpret_cast<const uint2*>(val + 16L * k + 4 * q)), *reinterpret_cast<const float4*>(x + 4L * col));
-  }
-  r[4 * row + q] = b[4 * row + q] - acc;
+  const bool live = row < n;
+  const float acc = bsr4_row<BSR4_U_F16>(live, row, q, rowPtr, colPtr, Bsr4F16{val}, x);
+  if (live) r[4 * row + q] = b ? b[4 * row + q] - acc : acc;
 }
 
 
@@ -172,6 +144,8 @@ __global__ void prolong_kernel(int n, const int* __restrict__ agg, const float* 
 }
 
 // y = A x, or with b given y = b - A x (the residual fused into the product)
+// y = A x or r = b - A x on the coarse levels (FP32 blocks), 4 lanes per block row
+// taking whole blocks (bsr4_row)
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict__ rowPtr,
                                                    const int* __restrict__ colPtr, const float* __restrict__ val,
                                                    const float* __restrict__ x, float* __restrict__ y,
@@ -179,38 +153,10 @@ __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict_
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
-  const int r = (int)(t & 3);
-  if (row >= n) return;
-  float acc = 0.f;
-  const int e = rowPtr[row + 1];
-  int k = rowPtr[row];
-  for (; k + 3 < e; k += 4) {  // four blocks per step: all loads issued before use
-    int c[4];
-    float4 v[4], xv[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
-#pragma unroll
-    for (int u = 0; u < 4; u++) v[u] = *reinterpret_cast<const float4*>(val + 16L * (k + u) + 4 * r);
-#pragma unroll
-    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      acc = fmaf(v[u].x, xv[u].x, acc);
-      acc = fmaf(v[u].y, xv[u].y, acc);
-      acc = fmaf(v[u].z, xv[u].z, acc);
-      acc = fmaf(v[u].w, xv[u].w, acc);
-    }
-  }
-  for (; k < e; k++) {
-    const int col = __ldg(colPtr + k);
-    const float4 v = *reinterpret_cast<const float4*>(val + 16L * k + 4 * r);
-    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
-    acc = fmaf(v.x, xv.x, acc);
-    acc = fmaf(v.y, xv.y, acc);
-    acc = fmaf(v.z, xv.z, acc);
-    acc = fmaf(v.w, xv.w, acc);
-  }
-  y[4 * row + r] = b ? b[4 * row + r] - acc : acc;
+  const int q = (int)(t & 3);
+  const bool live = row < n;
+  const float acc = bsr4_row<BSR4_U_F32>(live, row, q, rowPtr, colPtr, Bsr4F32{val}, x);
+  if (live) y[4 * row + q] = b ? b[4 * row + q] - acc : acc;
 }
 
 // A P block b, entry e: FP16 of the sum of entry e over the listed fine blocks
@@ -225,8 +171,9 @@ __global__ void ap_values_kernel(int nb, const int* __restrict__ sumPtr, const i
   out[t] = __float2half_rn(fminf(fmaxf(s, -65504.f), 65504.f));
 }
 
-// Coarse correction on the finest level, 2 threads per node (rows 2q, 2q+1 of its
-// blocks): x += P xc (or x = P xc) and r -= (A P) xc (or r = b - (A P) xc)
+// Coarse correction on the finest level: x += P xc (or x = P xc) and r -= (A P) xc (or
+// r = b - (A P) xc), the product with the FP16 A P by 4 lanes per block row taking
+// whole blocks (bsr4_row; a row of A P has about 4 blocks)
 __global__ void __launch_bounds__(256) correct_kernel(int n, const int* __restrict__ apRow,
                                                       const int* __restrict__ apCol,
                                                       const __half* __restrict__ apVal,
@@ -235,42 +182,20 @@ __global__ void __launch_bounds__(256) correct_kernel(int n, const int* __restri
                                                       float* __restrict__ r, int from_zero, const int* flags) {
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long row = t >> 1;
-  const int q = (int)(t & 1);
-  if (row >= n) return;
-  float a0 = 0.f, a1 = 0.f;
-  for (int k = apRow[row]; k < apRow[row + 1]; k++) {
-    const int col = __ldg(apCol + k);
-    const uint4 raw = __ldcs(reinterpret_cast<const uint4*>(apVal + 16L * k + 8 * q));
-    const float4 xv = *reinterpret_cast<const float4*>(xc + 4L * col);
-    const float2 v0 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
-    const float2 v1 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-    const float2 v2 = __half22float2(*reinterpret_cast<const __half2*>(&raw.z));
-    const float2 v3 = __half22float2(*reinterpret_cast<const __half2*>(&raw.w));
-    a0 = fmaf(v0.x, xv.x, a0);
-    a0 = fmaf(v0.y, xv.y, a0);
-    a0 = fmaf(v1.x, xv.z, a0);
-    a0 = fmaf(v1.y, xv.w, a0);
-    a1 = fmaf(v2.x, xv.x, a1);
-    a1 = fmaf(v2.y, xv.y, a1);
-    a1 = fmaf(v3.x, xv.z, a1);
-    a1 = fmaf(v3.y, xv.w, a1);
-  }
-  const long o = 4 * row + 2 * q;
-  const float2 pc = *reinterpret_cast<const float2*>(xc + 4L * agg[row] + 2 * q);
-  float2 xr, rr;
+  const long row = t >> 2;
+  const int q = (int)(t & 3);
+  const bool live = row < n;
+  const float acc = bsr4_row<BSR4_U_F16>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
+  if (!live) return;
+  const long o = 4 * row + q;
+  const float pc = xc[4L * agg[row] + q];
   if (from_zero) {
-    xr = pc;
-    const float2 bb = *reinterpret_cast<const float2*>(b + o);
-    rr = make_float2(bb.x - a0, bb.y - a1);
+    x[o] = pc;
+    r[o] = b[o] - acc;
   } else {
-    const float2 xo = *reinterpret_cast<const float2*>(x + o);
-    const float2 ro = *reinterpret_cast<const float2*>(r + o);
-    xr = make_float2(xo.x + pc.x, xo.y + pc.y);
-    rr = make_float2(ro.x - a0, ro.y - a1);
+    x[o] += pc;
+    r[o] -= acc;
   }
-  *reinterpret_cast<float2*>(x + o) = xr;
-  *reinterpret_cast<float2*>(r + o) = rr;
 }
 
 }  // namespace
@@ -282,13 +207,13 @@ void amg_ap_values(cudaStream_t s, int nb, const int* sumPtr, const int* sumIdx,
 
 void amg_correct(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh, const int* agg,
                  const float* xc, float* x, float* r, const int* flags) {
-  correct_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+  correct_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
       n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, nullptr, x, r, 0, flags);
 }
 
 void amg_correct_from_zero(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
                            const int* agg, const float* xc, const float* b, float* x, float* r, const int* flags) {
-  correct_kernel<<<(unsigned)((2L * n + 255) / 256), 256, 0, s>>>(
+  correct_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
       n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, b, x, r, 1, flags);
 }
 
@@ -316,6 +241,12 @@ void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr,
       n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, b, r, flags);
 }
 
+
+void amg_spmv_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
+                float* y, const int* flags) {
+  spmv_res_h_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
+      n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, nullptr, y, flags);
+}
 
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags) {

@@ -10,6 +10,7 @@
 // returns at once when flags[0] (converged) or flags[2] (breakdown) is set, so that a
 // whole restart cycle can be launched as one CUDA graph and stop early on the device.
 #include "dword.h"
+#include "bsr4.cuh"
 #include "internal.h"
 
 namespace svgpu {
@@ -509,8 +510,8 @@ __global__ void scale_val32_kernel(long nnz, const int* __restrict__ blkRow, con
   Val[t] = (float)(((double)Val[t] * W[4L * blkRow[k] + r]) * W[4L * colPtr[k] + c]);
 }
 
-// y = K x, FP32 matrix and vectors, FP32 accumulation; 4 threads per block row, one
-// 128-bit load of the block row and one of x per block.
+// y = K x, FP32 matrix and vectors, FP32 accumulation; 4 lanes per block row, each
+// taking whole blocks (bsr4_row).
 __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __restrict__ rowPtr,
                                                         const int* __restrict__ colPtr,
                                                         const float* __restrict__ Val,
@@ -519,38 +520,10 @@ __global__ void __launch_bounds__(256) spmv4_f32_kernel(int nNo, const int* __re
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
-  const int r = (int)(t & 3);
-  if (row >= nNo) return;
-  const int s = rowPtr[row], e = rowPtr[row + 1];
-  float acc = 0.f;
-  int k = s;
-  for (; k + 3 < e; k += 4) {  // four blocks per step, loads first (see spmv4_f64_kernel)
-    int c[4];
-    float4 v[4], xv[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) c[u] = __ldg(colPtr + k + u);
-#pragma unroll
-    for (int u = 0; u < 4; u++) v[u] = __ldcs(reinterpret_cast<const float4*>(Val + 16L * (k + u) + 4 * r));
-#pragma unroll
-    for (int u = 0; u < 4; u++) xv[u] = *reinterpret_cast<const float4*>(x + 4L * c[u]);
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      acc = fmaf(v[u].x, xv[u].x, acc);
-      acc = fmaf(v[u].y, xv[u].y, acc);
-      acc = fmaf(v[u].z, xv[u].z, acc);
-      acc = fmaf(v[u].w, xv[u].w, acc);
-    }
-  }
-  for (; k < e; k++) {
-    const int col = __ldg(colPtr + k);
-    const float4 v = __ldcs(reinterpret_cast<const float4*>(Val + 16L * k + 4 * r));
-    const float4 xv = *reinterpret_cast<const float4*>(x + 4L * col);
-    acc = fmaf(v.x, xv.x, acc);
-    acc = fmaf(v.y, xv.y, acc);
-    acc = fmaf(v.z, xv.z, acc);
-    acc = fmaf(v.w, xv.w, acc);
-  }
-  y[4 * row + r] = acc;
+  const int q = (int)(t & 3);
+  const bool live = row < nNo;
+  const float v = bsr4_row<BSR4_U_F32>(live, row, q, rowPtr, colPtr, Bsr4F32{Val}, x);
+  if (live) y[4 * row + q] = v;
 }
 
 // y = K x with the FP32 matrix, FP64 vectors and FP64 accumulation (true residual).
@@ -653,44 +626,68 @@ __global__ void __launch_bounds__(256) multidot32_kernel(long n, int m, const fl
   }
 }
 
-// Partial <V_j, w> over FP32 vectors read as float4: every thread keeps JB FP32
-// accumulators (JB independent 16-byte loads in flight per step), FP64 across threads
-// and CTAs.  n4 = n / 4 float4 entries per vector, ldv4 = ldv / 4.
-template <int JB>
-__global__ void __launch_bounds__(256) multidot32v4_kernel(long n4, int m, const float4* __restrict__ V, long ldv4,
-                                                           const float4* __restrict__ w, double* __restrict__ partial,
-                                                           const int* flags) {
+// Partial <V_j, w>, j < m <= MDW_MAXM, over FP32 vectors read as float4.  Each CTA
+// owns one contiguous range of the vectors (equal shares), walked in tiles of
+// MDW_T x 256 float4: the tile of w stays in registers (MDW_T float4 per thread) while
+// one pass over the m basis vectors streams their tiles with MDW_U x MDW_T loads in
+// flight per thread.  Per vector and tile a warp sums its 32 x MDW_T x 4 products in
+// FP32 (a shuffle tree) and adds the sum in FP64 to its own shared-memory accumulator;
+// the CTA's warps are summed in FP64 at the end, in a fixed order (deterministic).
+// w is read once per launch instead of once per group of vectors.
+constexpr int MDW_T = 4, MDW_U = 4, MDW_MAXM = 256;
+
+__global__ void __launch_bounds__(256) multidot32w_kernel(long n4, int m, const float4* __restrict__ V, long ldv4,
+                                                          const float4* __restrict__ w, double* __restrict__ partial,
+                                                          const int* flags) {
   if (stopped(flags)) return;
-  __shared__ double red[JB][8];
+  __shared__ double red[8][MDW_MAXM];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (int j0 = 0; j0 < m; j0 += JB) {
-    float acc[JB];
+  for (int j = lane; j < m; j += 32) red[warp][j] = 0.0;
+  __syncwarp();
+  const long share = (n4 + gridDim.x - 1) / gridDim.x;
+  const long beg = (long)blockIdx.x * share;
+  const long end = beg + share < n4 ? beg + share : n4;
+  constexpr long tile = (long)MDW_T * 256;
+  for (long base = beg; base < end; base += tile) {
+    float4 wr[MDW_T];
+    bool in[MDW_T];
 #pragma unroll
-    for (int q = 0; q < JB; q++) acc[q] = 0.f;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += stride) {
-      const float4 wk = w[k];
+    for (int t = 0; t < MDW_T; t++) {
+      const long k = base + (long)t * 256 + threadIdx.x;
+      in[t] = k < end;
+      wr[t] = in[t] ? w[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int j0 = 0; j0 < m; j0 += MDW_U) {
+      float a[MDW_U];
 #pragma unroll
-      for (int q = 0; q < JB; q++) {
-        if (j0 + q < m) {
-          const float4 v = __ldcs(V + (long)(j0 + q) * ldv4 + k);
-          acc[q] = fmaf(v.x, wk.x, fmaf(v.y, wk.y, fmaf(v.z, wk.z, fmaf(v.w, wk.w, acc[q]))));
+      for (int u = 0; u < MDW_U; u++) {
+        a[u] = 0.f;
+        if (j0 + u < m) {
+          const float4* vj = V + (long)(j0 + u) * ldv4 + base + threadIdx.x;
+#pragma unroll
+          for (int t = 0; t < MDW_T; t++) {
+            if (in[t]) {
+              const float4 v = __ldcs(vj + t * 256);
+              a[u] = fmaf(v.x, wr[t].x, fmaf(v.y, wr[t].y, fmaf(v.z, wr[t].z, fmaf(v.w, wr[t].w, a[u]))));
+            }
+          }
         }
       }
-    }
 #pragma unroll
-    for (int q = 0; q < JB; q++) {
-      double v = (double)acc[q];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[q][warp] = v;
+      for (int u = 0; u < MDW_U; u++) {
+        float v = a[u];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && j0 + u < m) red[warp][j0 + u] += (double)v;
+      }
     }
-    __syncthreads();
-    if (threadIdx.x < JB && j0 + (int)threadIdx.x < m) {
-      double v = 0.0;
-      for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += red[threadIdx.x][q];
-      partial[(long)blockIdx.x * m + j0 + threadIdx.x] = v;
-    }
-    __syncthreads();
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    double v = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) v += red[q][j];
+    partial[(long)blockIdx.x * m + j] = v;
   }
 }
 
@@ -825,14 +822,26 @@ void launch_spmv4_f32_f64(cudaStream_t s, int nNo, const int* rowPtr, const int*
   spmv4_f32_dw_kernel<<<grid, 256, 0, s>>>(nNo, rowPtr, colPtr, Val, reinterpret_cast<const float4*>(xw), y);
 }
 
+int multidot32_ctas(long n, int sm_count) {
+  long c = (n / 4 + (long)MDW_T * 256 - 1) / ((long)MDW_T * 256);  // at least one tile per CTA
+  const long cap = 4L * sm_count;
+  if (c > cap) c = cap;
+  if (c < 1) c = 1;
+  return (int)c;
+}
+
 int launch_multidot32(cudaStream_t s, long n, int m, const float* V, long ldv, const float* w, double* partial,
                       int sm_count, const int* flags) {
+  const bool v4 = (n % 4 == 0) && (ldv % 4 == 0) && m <= MDW_MAXM &&
+                  ((reinterpret_cast<uintptr_t>(V) | reinterpret_cast<uintptr_t>(w)) % 16 == 0);
+  if (v4) {
+    const int ctas = multidot32_ctas(n, sm_count);
+    multidot32w_kernel<<<ctas, 256, 0, s>>>(n / 4, m, reinterpret_cast<const float4*>(V), ldv / 4,
+                                            reinterpret_cast<const float4*>(w), partial, flags);
+    return ctas;
+  }
   const int ctas = multidot_ctas(n, sm_count);
-  const bool v4 = (n % 4 == 0) && (ldv % 4 == 0) && ((reinterpret_cast<uintptr_t>(V) | reinterpret_cast<uintptr_t>(w)) % 16 == 0);
-  if (v4)
-    multidot32v4_kernel<16><<<ctas, 256, 0, s>>>(n / 4, m, reinterpret_cast<const float4*>(V), ldv / 4,
-                                                 reinterpret_cast<const float4*>(w), partial, flags);
-  else if (m <= 8 * MD_JMAX)
+  if (m <= 8 * MD_JMAX)
     multidot2_kernel<float, float><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);
   else
     multidot32_kernel<8><<<ctas, 256, 0, s>>>(n, m, V, ldv, w, partial, flags);

@@ -205,7 +205,7 @@ def test_headline_settings_pipe50k(golden):
     """The headline's settings on the 50k-tet pipe: mixed precision, multilevel FGMRES(50)
     from the learned initial guess (mode 4) after 5 steps of online training, tangent
     kept within a step, the extrapolating Newton predictor, linear relative tolerance
-    1e-2, Newton to picc's 1e-8 (at most 8 iterations).  Checked against the reference
+    1e-2, Newton to picc's 5e-9 (at most 8 iterations).  Checked against the reference
     run to convergence on the same 10 steps (ref_pipe50k_conv: the compiled reference,
     Newton to 1e-11 within 12 iterations, GMRES to 1e-8): per-field relative L2 within
     1e-6 after step 10.  The reference's fixed-3-iteration run (ref_pipe50k) is itself
@@ -215,7 +215,7 @@ def test_headline_settings_pipe50k(golden):
     gc = golden("pipe50k_conv")
     ps = eval(str(g["params"]))
     s = _pipe50k_learned(g, ps, sD=50, mItr=40, relTol=1e-2, absTol=1e-17, newton_min=1, newton_max=8,
-                         newton_tol=1e-8, reuse_tangent=True)
+                         newton_tol=5e-9, reuse_tangent=True)
     s.ctx.set_predictor(1)
     _train_then(s, ps, 4)
     ref = gc["Yn_10"]
