@@ -178,8 +178,9 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, 
   AmgLevel& C = st.lv[l + 1];
   // pre-smoothing from zero (on the finest level optionally the learned network),
   // coarse-grid correction of the residual, post-smoothing.  On the finest level the
-  // products use the FP16 matrix, the residual after the correction comes from A P,
-  // and the pre-smoothing may be left out (pre_sweeps 0).
+  // products use the FP16 matrix, the residual after the correction comes from A P
+  // in the same pass as the correction and the post-smoothing, and the pre-smoothing
+  // may be left out (pre_sweeps 0).
   const bool fine = l == 0 && st.ap_nnz > 0;
   const bool marks = l == 0 && !ctx->use_graphs;  // finer phase marks, individual launches only
   const bool pre = !fine || st.pre_sweeps > 0 || (st.gnn_smoother && ctx->gnn);
@@ -204,13 +205,9 @@ void vcycle(svgpu_ctx* ctx, int l, const float* Val0, const float* b, float* x, 
   vcycle(ctx, l + 1, Val0, C.b.p, C.x.p, fl);
   if (marks) phase_mark(ctx, PH_VC_TRANSFER);
   if (fine) {
-    if (pre)
-      amg_correct(s, A.n, st.apRow.p, st.apCol.p, st.apValh.p, A.agg.p, C.x.p, x, A.r.p, fl);
-    else
-      amg_correct_from_zero(s, A.n, st.apRow.p, st.apCol.p, st.apValh.p, A.agg.p, C.x.p, b, x, A.r.p, fl);
-    if (marks) phase_mark(ctx, PH_CYC_PRECOND);
-    amg_jacobi(s, A.n, st.omega, A.dinv.p, b, A.r.p, x, 2, fl);
-    ctx->launches += 2;
+    amg_correct_smooth(s, A.n, st.apRow.p, st.apCol.p, st.apValh.p, A.agg.p, C.x.p, A.dinv.p, st.omega, b, x, A.r.p,
+                       pre ? 0 : 1, fl);
+    ctx->launches += 1;
   } else {
     amg_prolong_add(s, A.n, A.agg.p, C.x.p, x, fl);
     amg_spmv(s, A.n, rp, cp, val, x, A.r.p, fl);

@@ -51,12 +51,12 @@ void ap_pattern(int n, const std::vector<int>& rowPtr, const std::vector<int>& c
                 std::vector<int>& apRow, std::vector<int>& apCol, std::vector<int>& sumPtr, std::vector<int>& sumIdx);
 // FP16 sums of fine blocks into the blocks of A P (sumPtr / sumIdx as from ap_pattern)
 void amg_ap_values(cudaStream_t s, int nb, const int* sumPtr, const int* sumIdx, const float* fineVal, uint16_t* apValh);
-// x += P xc and r <- r - (A P) xc on the finest level (FP16 A P)
-void amg_correct(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh, const int* agg,
-                 const float* xc, float* x, float* r, const int* flags);
-// x = P xc (no pre-smoothing) and r = b - (A P) xc
-void amg_correct_from_zero(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
-                           const int* agg, const float* xc, const float* b, float* x, float* r, const int* flags);
+// finest level's coarse correction and post-smoothing (FP16 A P):
+// x <- x + P xc + omega D^-1 (r - (A P) xc), or with from_zero (no pre-smoothing)
+// x <- P xc + omega D^-1 (b - (A P) xc)
+void amg_correct_smooth(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
+                        const int* agg, const float* xc, const float* dinv, float omega, const float* b, float* x,
+                        const float* r, int from_zero, const int* flags);
 
 // k_amg.cu
 void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal, float* coarseVal);

@@ -71,31 +71,39 @@ __global__ void diag_inv_kernel(int n, const int* __restrict__ diagPtr, const fl
 }
 
 // mode 0: x <- omega D^-1 b;  mode 1: x <- x + omega D^-1 (b - Ax);
-// mode 2: x <- x + omega D^-1 r with the residual r given in place of Ax (b unused)
-__global__ void jacobi_kernel(int n, float omega, const float* __restrict__ dinv, const float* __restrict__ b,
-                              const float* __restrict__ Ax, float* __restrict__ x, int mode,
-                              const int* flags) {
+// mode 2: x <- x + omega D^-1 r with the residual r given in place of Ax (b unused).
+// One thread per node: its 4x4 inverse (four 16-byte loads) and one 16-byte load of
+// each vector, so that every thread has all its loads in flight at once.
+__global__ void __launch_bounds__(256) jacobi_kernel(int n, float omega, const float4* __restrict__ dinv,
+                                                     const float4* __restrict__ b, const float4* __restrict__ Ax,
+                                                     float4* __restrict__ x, int mode, const int* flags) {
   if (stopped(flags)) return;
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long i = t >> 2;
-  const int r = (int)(t & 3);
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float4 rw = *reinterpret_cast<const float4*>(dinv + 16 * i + 4 * r);
-  float4 res;
+  const float4 d0 = dinv[4 * i], d1 = dinv[4 * i + 1], d2 = dinv[4 * i + 2], d3 = dinv[4 * i + 3];
+  float4 r;
   if (mode == 2) {
-    res = *reinterpret_cast<const float4*>(Ax + 4 * i);
+    r = Ax[i];
   } else {
-    res = *reinterpret_cast<const float4*>(b + 4 * i);
+    r = b[i];
     if (mode == 1) {
-      const float4 ax = *reinterpret_cast<const float4*>(Ax + 4 * i);
-      res.x -= ax.x;
-      res.y -= ax.y;
-      res.z -= ax.z;
-      res.w -= ax.w;
+      const float4 ax = Ax[i];
+      r.x -= ax.x;
+      r.y -= ax.y;
+      r.z -= ax.z;
+      r.w -= ax.w;
     }
   }
-  const float d = rw.x * res.x + rw.y * res.y + rw.z * res.z + rw.w * res.w;
-  x[4 * i + r] = mode == 0 ? omega * d : x[4 * i + r] + omega * d;
+  const float4 o = make_float4(d0.x * r.x + d0.y * r.y + d0.z * r.z + d0.w * r.w,
+                               d1.x * r.x + d1.y * r.y + d1.z * r.z + d1.w * r.w,
+                               d2.x * r.x + d2.y * r.y + d2.z * r.z + d2.w * r.w,
+                               d3.x * r.x + d3.y * r.y + d3.z * r.z + d3.w * r.w);
+  if (mode == 0) {
+    x[i] = make_float4(omega * o.x, omega * o.y, omega * o.z, omega * o.w);
+  } else {
+    const float4 xo = x[i];
+    x[i] = make_float4(xo.x + omega * o.x, xo.y + omega * o.y, xo.z + omega * o.z, xo.w + omega * o.w);
+  }
 }
 
 // FP16 copy of the finest level's matrix for the V-cycle products, saturated at the
@@ -171,31 +179,40 @@ __global__ void ap_values_kernel(int nb, const int* __restrict__ sumPtr, const i
   out[t] = __float2half_rn(fminf(fmaxf(s, -65504.f), 65504.f));
 }
 
-// Coarse correction on the finest level: x += P xc (or x = P xc) and r -= (A P) xc (or
-// r = b - (A P) xc), the product with the FP16 A P by 4 lanes per block row taking
-// whole blocks (bsr4_row; a row of A P has about 4 blocks)
-__global__ void __launch_bounds__(256) correct_kernel(int n, const int* __restrict__ apRow,
-                                                      const int* __restrict__ apCol,
-                                                      const __half* __restrict__ apVal,
-                                                      const int* __restrict__ agg, const float* __restrict__ xc,
-                                                      const float* __restrict__ b, float* __restrict__ x,
-                                                      float* __restrict__ r, int from_zero, const int* flags) {
+// Coarse correction and post-smoothing of the finest level in one pass:
+//   r' = r - (A P) xc            (from_zero: r' = b - (A P) xc)
+//   x <- x + P xc + omega D^-1 r'  (from_zero: x <- P xc + omega D^-1 r')
+// The product with the FP16 A P runs with 4 lanes per block row taking whole blocks
+// (bsr4_row; a row of A P has about 4 blocks), after which lane q holds r'_q; the 4
+// lanes of a row exchange their r' by shuffles and lane q applies row q of the node's
+// 4x4 inverse.  r' itself is not stored: nothing after the post-smoothing reads it.
+__global__ void __launch_bounds__(256) correct_smooth_kernel(int n, const int* __restrict__ apRow,
+                                                             const int* __restrict__ apCol,
+                                                             const __half* __restrict__ apVal,
+                                                             const int* __restrict__ agg,
+                                                             const float* __restrict__ xc,
+                                                             const float* __restrict__ dinv, float omega,
+                                                             const float* __restrict__ b, float* __restrict__ x,
+                                                             const float* __restrict__ r, int from_zero,
+                                                             const int* flags) {
   if (stopped(flags)) return;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long row = t >> 2;
   const int q = (int)(t & 3);
   const bool live = row < n;
   const float acc = bsr4_row<BSR4_U_F16>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
-  if (!live) return;
   const long o = 4 * row + q;
+  const float rq = live ? (from_zero ? b[o] : r[o]) - acc : 0.f;
+  const int base = (int)(threadIdx.x & 31) & ~3;
+  const float r0 = __shfl_sync(0xffffffffu, rq, base);
+  const float r1 = __shfl_sync(0xffffffffu, rq, base + 1);
+  const float r2 = __shfl_sync(0xffffffffu, rq, base + 2);
+  const float r3 = __shfl_sync(0xffffffffu, rq, base + 3);
+  if (!live) return;
+  const float4 d = *reinterpret_cast<const float4*>(dinv + 16 * row + 4 * q);
+  const float sm = omega * (d.x * r0 + d.y * r1 + d.z * r2 + d.w * r3);
   const float pc = xc[4L * agg[row] + q];
-  if (from_zero) {
-    x[o] = pc;
-    r[o] = b[o] - acc;
-  } else {
-    x[o] += pc;
-    r[o] -= acc;
-  }
+  x[o] = (from_zero ? pc : x[o] + pc) + sm;
 }
 
 }  // namespace
@@ -205,16 +222,11 @@ void amg_ap_values(cudaStream_t s, int nb, const int* sumPtr, const int* sumIdx,
                                                                       reinterpret_cast<__half*>(apValh));
 }
 
-void amg_correct(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh, const int* agg,
-                 const float* xc, float* x, float* r, const int* flags) {
-  correct_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
-      n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, nullptr, x, r, 0, flags);
-}
-
-void amg_correct_from_zero(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
-                           const int* agg, const float* xc, const float* b, float* x, float* r, const int* flags) {
-  correct_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
-      n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, b, x, r, 1, flags);
+void amg_correct_smooth(cudaStream_t s, int n, const int* apRow, const int* apCol, const uint16_t* apValh,
+                        const int* agg, const float* xc, const float* dinv, float omega, const float* b, float* x,
+                        const float* r, int from_zero, const int* flags) {
+  correct_smooth_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
+      n, apRow, apCol, reinterpret_cast<const __half*>(apValh), agg, xc, dinv, omega, b, x, r, from_zero, flags);
 }
 
 void amg_galerkin(cudaStream_t s, int ncb, const int* sumPtr, const int* sumIdx, const float* fineVal,
@@ -228,7 +240,9 @@ void amg_diag_inv(cudaStream_t s, int n, const int* diagPtr, const float* val, f
 
 void amg_jacobi(cudaStream_t s, int n, float omega, const float* dinv, const float* b, const float* Ax, float* x,
                 int mode, const int* flags) {
-  jacobi_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(n, omega, dinv, b, Ax, x, mode, flags);
+  jacobi_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+      n, omega, reinterpret_cast<const float4*>(dinv), reinterpret_cast<const float4*>(b),
+      reinterpret_cast<const float4*>(Ax), reinterpret_cast<float4*>(x), mode, flags);
 }
 
 void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h) {
