@@ -37,9 +37,6 @@ __device__ __forceinline__ T cst(const FluidConsts& c, int k, double v) {
     return (T)v;
 }
 
-// A double-word value from a (hi, lo) pair
-__device__ __forceinline__ dwf::dw dwv(float h, float l) { return dwf::dw(h, l); }
-
 // utils::is_zero(v, 0) (utils.cpp:170-189): |v| / max(|v|, eps) < 10 eps.  With eps =
 // 2^-52 the division is an exact power-of-two scaling, so the test is exactly
 // |v| < 10 * 2^-104, which needs no FP64 division (and no FP64 at all for T = float).
@@ -110,9 +107,9 @@ __device__ __forceinline__ void add_block<float>(float* __restrict__ dst, const 
   }
 }
 
-// T: arithmetic type of the element integrals; TV: storage type of Val.  WR / WK
-// select writing the residual rows / the tangent blocks (the mixed-precision path
-// runs the residual in FP64 and the tangent in FP32 as two launches).
+// T: arithmetic type of the element integrals (double, or float for the tangent of the
+// mixed-precision path, whose residual rows come from fluid_res_dw_kernel); TV:
+// storage type of Val.  WR / WK select writing the residual rows / the tangent blocks.
 // ALE (construct_fsi, fsi.cpp:158-164 and fluid.cpp:1508-1516/1835-1843): the state
 // arrays have ld rows per node (the FSI equation's 4, then the mesh equation's 3); the
 // element is integrated in the current configuration x + Dg(4..6) and convects with
@@ -129,7 +126,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
                                                        const int* __restrict__ rowPtr,
                                                        double* __restrict__ R, TV* __restrict__ Val,
                                                        int* __restrict__ errflag, int ld,
-                                                       const double* __restrict__ Dg, DwState dws) {
+                                                       const double* __restrict__ Dg) {
   const int le = blockIdx.x * blockDim.x + threadIdx.x;
   if (le >= ne) return;
   const int e = e0 + le;
@@ -141,33 +138,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
   T xl[4][3], al[4][3], yl[4][4];
   T ym[ALE ? 4 : 1][3];  // mesh velocity
 #pragma unroll
-  for (int a = 0; a < 4 && kIsDw<T>; a++) {
-    // double words straight from their (hi, lo) copies: no FP64 operation
-    const float4* xw = reinterpret_cast<const float4*>(dws.x4 + 4L * nd[a]);
-    const float4* aw = reinterpret_cast<const float4*>(dws.Ag + 4L * nd[a]);
-    const float4* yw = reinterpret_cast<const float4*>(dws.Yg + 4L * nd[a]);
-    const float4 x01 = xw[0], x23 = xw[1], a01 = aw[0], a23 = aw[1], y01 = yw[0], y23 = yw[1];
-    if constexpr (kIsDw<T>) {
-      xl[a][0] = dwv(x01.x, x01.y); xl[a][1] = dwv(x01.z, x01.w); xl[a][2] = dwv(x23.x, x23.y);
-      al[a][0] = dwv(a01.x, a01.y); al[a][1] = dwv(a01.z, a01.w); al[a][2] = dwv(a23.x, a23.y);
-      if (Bf) {
-        al[a][0] = al[a][0] - (T)Bf[3L * nd[a]];
-        al[a][1] = al[a][1] - (T)Bf[3L * nd[a] + 1];
-        al[a][2] = al[a][2] - (T)Bf[3L * nd[a] + 2];
-      }
-      yl[a][0] = dwv(y01.x, y01.y); yl[a][1] = dwv(y01.z, y01.w);
-      yl[a][2] = dwv(y23.x, y23.y); yl[a][3] = dwv(y23.z, y23.w);
-      if (ALE) {  // the mesh velocity; xl above already holds the current coordinates
-        const float4* mw = reinterpret_cast<const float4*>(dws.Ym + 4L * nd[a]);
-        const float4 m01 = mw[0], m23 = mw[1];
-        ym[ALE ? a : 0][0] = dwv(m01.x, m01.y);
-        ym[ALE ? a : 0][1] = dwv(m01.z, m01.w);
-        ym[ALE ? a : 0][2] = dwv(m23.x, m23.y);
-      }
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < 4 && !kIsDw<T>; a++) {
+  for (int a = 0; a < 4; a++) {
     const double2 x01 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a]);
     const double2 x23 = *reinterpret_cast<const double2*>(x4 + 4L * nd[a] + 2);
     double b0 = 0.0, b1 = 0.0, b2 = 0.0;
@@ -360,22 +331,7 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
 
   // residual rows (lR, fluid.cpp:2038-2040, 1658-1660)
 #pragma unroll
-  for (int a = 0; a < 4 && WR && kIsDw<T>; a++) {
-    if constexpr (kIsDw<T>) {  // double-word rows into dws.R (colour order: no conflicts)
-      float4* Ra = reinterpret_cast<float4*>(dws.R + 4L * nd[a]);
-      const T r0 = w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]);
-      const T r1 = w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]);
-      const T r2 = w * (RV[a][2] + Nx[0][a] * RM[0][2] + Nx[1][a] * RM[1][2] + Nx[2][a] * RM[2][2]);
-      const T r3 = w * RC[a];
-      float4 v01 = Ra[0], v23 = Ra[1];
-      const T s0 = dwv(v01.x, v01.y) + r0, s1 = dwv(v01.z, v01.w) + r1;
-      const T s2 = dwv(v23.x, v23.y) + r2, s3 = dwv(v23.z, v23.w) + r3;
-      Ra[0] = make_float4(s0.hi, s0.lo, s1.hi, s1.lo);
-      Ra[1] = make_float4(s2.hi, s2.lo, s3.hi, s3.lo);
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < 4 && WR && !kIsDw<T>; a++) {
+  for (int a = 0; a < 4 && WR; a++) {
     double* Ra = R + 4L * nd[a];
     double r0 = (double)(w * (RV[a][0] + Nx[0][a] * RM[0][0] + Nx[1][a] * RM[1][0] + Nx[2][a] * RM[2][0]));
     double r1 = (double)(w * (RV[a][1] + Nx[0][a] * RM[0][1] + Nx[1][a] * RM[1][1] + Nx[2][a] * RM[2][1]));
@@ -417,6 +373,235 @@ __global__ void __launch_bounds__(128) fluid_p1_kernel(FluidConsts c, int e0, in
       const long pos = rowbase + boff[16L * e + 4 * a + b];
       add_block<TV>(Val + 16 * pos, blk);
     }
+  }
+}
+
+// Residual rows of the mixed-precision path in double-word arithmetic, one thread per
+// element: the integrand of fluid_p1_kernel (fluid.cpp:1745-2040 and 1658-1660)
+// regrouped with two properties of the P1 tet and its 4-point rule, so that the
+// Gauss-point loop carries about half of the operations it would otherwise:
+//  * the shape-function gradients are constant, so the velocity and pressure
+//    gradients (ux, px, div u) and the viscous part of RM are element constants;
+//  * the rule is symmetric, N_g(a) = s for a = g and t otherwise (s + 3t = 1), so a
+//    Gauss-point value is t * (sum over the nodes) + (s - t) * (the value at node g),
+//    and a node's Gauss-point sum is t * (sum over the points) + (s - t) * (the value
+//    at point a): sum_g N_g(a) v_g for the rows RV, sum_g N_g(a) div u = SN div u and
+//    sum_g up_g . grad N_a = (sum_g up_g) . grad N_a for the continuity row, and
+//    sum_g p_g = SN * (sum over the nodes) for the pressure term of RM.
+// The node values picked by the Gauss point and the per-point rV2 stay in shared
+// memory (one slot per thread), out of the registers the loop needs.
+constexpr int RDW_BLOCK = 128;
+
+template <bool ALE>
+__global__ void __launch_bounds__(RDW_BLOCK) fluid_res_dw_kernel(FluidConsts c, int e0, int ne,
+                                                                 const int* __restrict__ ien,
+                                                                 const int* __restrict__ elem_id,
+                                                                 const double* __restrict__ Bf,
+                                                                 int* __restrict__ errflag, DwState dws) {
+  using dwf::dw;
+  constexpr int NV = ALE ? 10 : 7;  // y(0..3), a(0..2), the mesh velocity(0..2)
+  __shared__ float2 sh_node[NV][4][RDW_BLOCK];
+  __shared__ float2 sh_rv2[4][3][RDW_BLOCK];
+  const int tid = threadIdx.x;
+  const int le = blockIdx.x * blockDim.x + tid;
+  if (le >= ne) return;
+  const int e = e0 + le;
+  int nd[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) nd[a] = ien[4L * e + a];
+
+  // Jacobian and shape-function gradients (gnn, nn.cpp:489-545)
+  dw J[3][3];
+  {
+    dw xl[4][3];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const float4* xw = reinterpret_cast<const float4*>(dws.x4 + 4L * nd[a]);
+      const float4 x01 = xw[0], x23 = xw[1];
+      xl[a][0] = dw(x01.x, x01.y);
+      xl[a][1] = dw(x01.z, x01.w);
+      xl[a][2] = dw(x23.x, x23.y);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      J[i][0] = xl[0][i] - xl[3][i];
+      J[i][1] = xl[1][i] - xl[3][i];
+      J[i][2] = xl[2][i] - xl[3][i];
+    }
+  }
+  const dw Jac = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] + J[0][2] * J[1][0] * J[2][1] -
+                 J[0][0] * J[1][2] * J[2][1] - J[0][1] * J[1][0] * J[2][2] - J[0][2] * J[1][1] * J[2][0];
+  if (is_zero_ref(Jac)) {
+    if (atomicCAS(errflag, 0, SVGPU_EJAC) == 0) errflag[1] = elem_id ? elem_id[e] : e;
+    return;
+  }
+  const dw iJ = dw(1) / Jac;
+  dw Nx[3][4];  // dN_a/dx_k: xiX(a, k) for a < 3
+  Nx[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * iJ;
+  Nx[1][0] = (J[2][1] * J[0][2] - J[2][2] * J[0][1]) * iJ;
+  Nx[2][0] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * iJ;
+  Nx[0][1] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * iJ;
+  Nx[1][1] = (J[2][2] * J[0][0] - J[2][0] * J[0][2]) * iJ;
+  Nx[2][1] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * iJ;
+  Nx[0][2] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * iJ;
+  Nx[1][2] = (J[2][0] * J[0][1] - J[2][1] * J[0][0]) * iJ;
+  Nx[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * iJ;
+#pragma unroll
+  for (int k = 0; k < 3; k++) Nx[k][3] = -(Nx[k][0] + Nx[k][1] + Nx[k][2]);
+  // metric ks = xiX^T xiX, its six distinct entries
+  dw K00 = Nx[0][0] * Nx[0][0] + Nx[0][1] * Nx[0][1] + Nx[0][2] * Nx[0][2];
+  dw K11 = Nx[1][0] * Nx[1][0] + Nx[1][1] * Nx[1][1] + Nx[1][2] * Nx[1][2];
+  dw K22 = Nx[2][0] * Nx[2][0] + Nx[2][1] * Nx[2][1] + Nx[2][2] * Nx[2][2];
+  dw K01 = Nx[0][0] * Nx[1][0] + Nx[0][1] * Nx[1][1] + Nx[0][2] * Nx[1][2];
+  dw K02 = Nx[0][0] * Nx[2][0] + Nx[0][1] * Nx[2][1] + Nx[0][2] * Nx[2][2];
+  dw K12 = Nx[1][0] * Nx[2][0] + Nx[1][1] * Nx[2][1] + Nx[1][2] * Nx[2][2];
+
+  const dw rho = cst<dw>(c, FDW_RHO, c.rho), mu = cst<dw>(c, FDW_MU, c.mu), kd = cst<dw>(c, FDW_KD, c.kd);
+  const dw w = Jac * cst<dw>(c, FDW_W24, 1.0 / 24.0);
+  const dw mur = mu / rho, mukd = mu * kd;
+  // tauM pieces that do not depend on the Gauss point (fluid.cpp:1924-1941)
+  const dw kTS = cst<dw>(c, FDW_KT, 4.0 / (c.dt * c.dt)) + (kd * mur) * (kd * mur) +
+                 dw(36) * (K00 * K00 + K11 * K11 + K22 * K22 + dw(2) * (K01 * K01 + K02 * K02 + K12 * K12)) *
+                     (mur * mur);
+  const dw trK = K00 + K11 + K22;
+
+  // node values: element sums, the constant gradients, and the per-node copies the
+  // Gauss-point loop picks from
+  dw ux[3][3], px[3], Sy[4], Sa[3], Sm[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ux[k][0] = ux[k][1] = ux[k][2] = dw(0);
+    px[k] = dw(0);
+    Sa[k] = dw(0);
+    Sm[k] = dw(0);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) Sy[i] = dw(0);
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const float4* aw = reinterpret_cast<const float4*>(dws.Ag + 4L * nd[a]);
+    const float4* yw = reinterpret_cast<const float4*>(dws.Yg + 4L * nd[a]);
+    const float4 a01 = aw[0], a23 = aw[1], y01 = yw[0], y23 = yw[1];
+    dw y[4] = {dw(y01.x, y01.y), dw(y01.z, y01.w), dw(y23.x, y23.y), dw(y23.z, y23.w)};
+    dw al[3] = {dw(a01.x, a01.y), dw(a01.z, a01.w), dw(a23.x, a23.y)};
+    if (Bf) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) al[i] = al[i] - dw(Bf[3L * nd[a] + i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      Sy[i] += y[i];
+      sh_node[i][a][tid] = make_float2(y[i].hi, y[i].lo);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      Sa[i] += al[i];
+      sh_node[4 + i][a][tid] = make_float2(al[i].hi, al[i].lo);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) ux[k][i] += Nx[k][a] * y[i];
+      px[k] += Nx[k][a] * y[3];
+    }
+    if constexpr (ALE) {
+      const float4* mw = reinterpret_cast<const float4*>(dws.Ym + 4L * nd[a]);
+      const float4 m01 = mw[0], m23 = mw[1];
+      const dw m[3] = {dw(m01.x, m01.y), dw(m01.z, m01.w), dw(m23.x, m23.y)};
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        Sm[i] += m[i];
+        sh_node[7 + i][a][tid] = make_float2(m[i].hi, m[i].lo);
+      }
+    }
+  }
+  const dw divU = ux[0][0] + ux[1][1] + ux[2][2];
+  // the 4-point rule (nn_elem_gip.h:501-515, qmTET4 = (5 + 3 sqrt 5)/20, ComMod.h:1011)
+  constexpr double qs = (5.0 + 3.0 * 2.23606797749978969640917366873) / 20.0;
+  constexpr double qt = (1.0 - qs) / 3.0;
+  const dw t = from_const<dw>(qt), st = from_const<dw>(qs - qt), SN = from_const<dw>(qs + 3.0 * qt);
+  dw Cy[4], Ca[3], Cm[3];
+#pragma unroll
+  for (int i = 0; i < 4; i++) Cy[i] = t * Sy[i];
+  Ca[0] = t * Sa[0] - cst<dw>(c, FDW_F0, c.f0);
+  Ca[1] = t * Sa[1] - cst<dw>(c, FDW_F1, c.f1);
+  Ca[2] = t * Sa[2] - cst<dw>(c, FDW_F2, c.f2);
+#pragma unroll
+  for (int i = 0; i < 3; i++) Cm[i] = t * Sm[i];
+
+  // Gauss-point sums; RM starts with its viscous part, 4 mu (grad u + grad u^T)
+  dw RM[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) RM[k][i] = dw(4) * mu * (ux[k][i] + ux[i][k]);
+  dw SrV2[3] = {dw(0), dw(0), dw(0)}, Sup[3] = {dw(0), dw(0), dw(0)}, sTauC = dw(0);
+
+#pragma unroll 1
+  for (int g = 0; g < 4; g++) {
+    dw u[3], ud[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float2 yv = sh_node[i][g][tid], av = sh_node[4 + i][g][tid];
+      u[i] = Cy[i] + st * dw(yv.x, yv.y);
+      ud[i] = Ca[i] + st * dw(av.x, av.y);
+      if constexpr (ALE) {  // convection relative to the mesh (fluid.cpp:1837-1843)
+        const float2 mv = sh_node[7 + i][g][tid];
+        u[i] = u[i] - (Cm[i] + st * dw(mv.x, mv.y));
+      }
+    }
+    // stabilisation (fluid.cpp:1922-1995)
+    const dw kU = u[0] * u[0] * K00 + u[1] * u[1] * K11 + u[2] * u[2] * K22 +
+                  dw(2) * (u[0] * u[1] * K01 + u[0] * u[2] * K02 + u[1] * u[2] * K12);
+    const dw tauM = dw(1) / (rho * sqrt(kTS + kU));
+    dw up[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const dw rV = ud[i] + u[0] * ux[0][i] + u[1] * ux[1][i] + u[2] * ux[2][i];
+      up[i] = -tauM * (rho * rV + px[i] + mukd * u[i]);
+    }
+    sTauC += dw(1) / (tauM * trK);
+    dw tauB = up[0] * up[0] * K00 + up[1] * up[1] * K11 + up[2] * up[2] * K22 +
+              dw(2) * (up[0] * up[1] * K01 + up[0] * up[2] * K02 + up[1] * up[2] * K12);
+    if (is_zero_ref(tauB)) tauB = dw(2.220446049250313e-16f);  // 2^-52, exact in float
+    tauB = rho / sqrt(tauB);
+    const dw ua[3] = {u[0] + up[0], u[1] + up[1], u[2] + up[2]};
+    // residual pieces (fluid.cpp:2002-2036); the pressure term of RM follows the loop
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const dw rVb = tauB * (up[0] * ux[0][i] + up[1] * ux[1][i] + up[2] * ux[2][i]);
+      const dw rup = rho * up[i];
+#pragma unroll
+      for (int k = 0; k < 3; k++) RM[k][i] += rVb * up[k] - rup * ua[k];
+      const dw rV2 = rho * (ud[i] + ua[0] * ux[0][i] + ua[1] * ux[1][i] + ua[2] * ux[2][i]) + mukd * ua[i];
+      SrV2[i] += rV2;
+      sh_rv2[g][i][tid] = make_float2(rV2.hi, rV2.lo);
+      Sup[i] += up[i];
+    }
+  }
+  // - sum_g pa_g = - sum_g p_g + div u sum_g tauC_g on the diagonal
+  const dw Pd = divU * sTauC - SN * Sy[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) RM[i][i] += Pd;
+  const dw SNdiv = SN * divU;
+
+  // residual rows (lR, fluid.cpp:2038-2040, 1658-1660), double words into dws.R
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    dw r[4];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float2 v = sh_rv2[a][i][tid];
+      const dw RV = t * SrV2[i] + st * dw(v.x, v.y);
+      r[i] = w * (RV + Nx[0][a] * RM[0][i] + Nx[1][a] * RM[1][i] + Nx[2][a] * RM[2][i]);
+    }
+    r[3] = w * (SNdiv - (Sup[0] * Nx[0][a] + Sup[1] * Nx[1][a] + Sup[2] * Nx[2][a]));
+    float4* Ra = reinterpret_cast<float4*>(dws.R + 4L * nd[a]);
+    const float4 v01 = Ra[0], v23 = Ra[1];
+    const dw s0 = dw(v01.x, v01.y) + r[0], s1 = dw(v01.z, v01.w) + r[1];
+    const dw s2 = dw(v23.x, v23.y) + r[2], s3 = dw(v23.z, v23.w) + r[3];
+    Ra[0] = make_float4(s0.hi, s0.lo, s1.hi, s1.lo);
+    Ra[1] = make_float4(s2.hi, s2.lo, s3.hi, s3.lo);
   }
 }
 
@@ -578,25 +763,23 @@ void launch_fluid_assembly(cudaStream_t s, int precision, const FluidConsts& c, 
   if (ne <= 0) return;
   const int block = 128;
   const int grid = (ne + block - 1) / block;
-  const DwState none{nullptr, nullptr, nullptr, nullptr};
   if (precision == SVGPU_FP64) {
     fluid_p1_kernel<double, double, true, true, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr, none);
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, 4, nullptr);
   } else {
     // residual rows in double-word FP32 (about 48 bits) into dws->R, tangent blocks in FP32
-    fluid_p1_kernel<dwf::dw, double, true, false, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, nullptr, errflag, 4, nullptr, *dws);
+    fluid_res_dw_kernel<false><<<(ne + RDW_BLOCK - 1) / RDW_BLOCK, RDW_BLOCK, 0, s>>>(c, e0, ne, ien, elem_id, Bf,
+                                                                                     errflag, *dws);
     fluid_p1_kernel<float, float, false, true, false><<<grid, block, 0, s>>>(
-        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr, none);
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val32, errflag, 4, nullptr);
   }
 }
 
 void launch_fluid_residual(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
                            const int* elem_id, const double* Bf, int* errflag, const DwState& dws) {
   if (ne <= 0) return;
-  fluid_p1_kernel<dwf::dw, double, true, false, false><<<(ne + 127) / 128, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, nullptr, nullptr, nullptr, Bf, nullptr, nullptr, nullptr, errflag, 4, nullptr,
-      dws);
+  fluid_res_dw_kernel<false><<<(ne + RDW_BLOCK - 1) / RDW_BLOCK, RDW_BLOCK, 0, s>>>(c, e0, ne, ien, elem_id, Bf,
+                                                                                   errflag, dws);
 }
 
 namespace {
@@ -630,8 +813,7 @@ void launch_fluid_ale_assembly(cudaStream_t s, const FluidConsts& c, int e0, int
                                double* Val64, int* errflag) {
   if (ne <= 0) return;
   fluid_p1_kernel<double, double, true, true, true><<<(ne + 127) / 128, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, ld, Dg,
-      DwState{nullptr, nullptr, nullptr, nullptr});
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, Bf, rowPtr, R, Val64, errflag, ld, Dg);
 }
 
 namespace {
@@ -668,12 +850,10 @@ void launch_fluid_ale_mixed(cudaStream_t s, const FluidConsts& c, int e0, int ne
                             const double* Dg, const int* rowPtr, float* Val32, int* errflag, const DwState& dws) {
   if (ne <= 0) return;
   const int grid = (ne + 127) / 128;
-  fluid_p1_kernel<dwf::dw, double, true, false, true><<<grid, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, errflag, ld,
-      nullptr, dws);
+  fluid_res_dw_kernel<true><<<(ne + RDW_BLOCK - 1) / RDW_BLOCK, RDW_BLOCK, 0, s>>>(c, e0, ne, ien, elem_id, nullptr,
+                                                                                  errflag, dws);
   fluid_p1_kernel<float, float, false, true, true><<<grid, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, nullptr, rowPtr, nullptr, Val32, errflag, ld, Dg,
-      DwState{nullptr, nullptr, nullptr, nullptr});
+      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, nullptr, rowPtr, nullptr, Val32, errflag, ld, Dg);
 }
 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,
