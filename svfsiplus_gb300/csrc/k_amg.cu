@@ -200,19 +200,23 @@ __global__ void __launch_bounds__(256) correct_smooth_kernel(int n, const int* _
   const long row = t >> 2;
   const int q = (int)(t & 3);
   const bool live = row < n;
-  const float acc = bsr4_row<BSR4_U_F16>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
   const long o = 4 * row + q;
-  const float rq = live ? (from_zero ? b[o] : r[o]) - acc : 0.f;
+  // the loads that do not depend on the product go first
+  float rin = 0.f, xo = 0.f, pc = 0.f;
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (live) {
+    rin = from_zero ? b[o] : r[o];
+    if (!from_zero) xo = x[o];
+    d = *reinterpret_cast<const float4*>(dinv + 16 * row + 4 * q);
+    pc = xc[4L * agg[row] + q];
+  }
+  const float rq = rin - bsr4_row<BSR4_U_F16>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
   const int base = (int)(threadIdx.x & 31) & ~3;
   const float r0 = __shfl_sync(0xffffffffu, rq, base);
   const float r1 = __shfl_sync(0xffffffffu, rq, base + 1);
   const float r2 = __shfl_sync(0xffffffffu, rq, base + 2);
   const float r3 = __shfl_sync(0xffffffffu, rq, base + 3);
-  if (!live) return;
-  const float4 d = *reinterpret_cast<const float4*>(dinv + 16 * row + 4 * q);
-  const float sm = omega * (d.x * r0 + d.y * r1 + d.z * r2 + d.w * r3);
-  const float pc = xc[4L * agg[row] + q];
-  x[o] = (from_zero ? pc : x[o] + pc) + sm;
+  if (live) x[o] = xo + pc + omega * (d.x * r0 + d.y * r1 + d.z * r2 + d.w * r3);
 }
 
 }  // namespace
