@@ -274,19 +274,19 @@ def spmv_roofline(ctx, colPtr, nNo, mode, stream, reps=20):
     peak, kind = peaks()
     achieved = bytes_ / (ms * 1e-3) / 1e9
     # DRAM bytes per launch of this kernel on the 8M-tet pipe from one ncu capture of the
-    # unchanged kernel (dram__bytes_read.sum + dram__bytes_write.sum, mean of two
+    # unchanged kernel (dram__bytes_read.sum + dram__bytes_write.sum, mean of six
     # launches; the command is in profiles/spmv4_f32_pipe8m_traffic.md): ncu cannot run
     # inside this timed program, so the capture is a separate run of the same kernel
     traffic = TRAFFIC_SPMV4_F32_PIPE8M if (mode >= 0 and colPtr.size == BLOCKS_PIPE8M) else None
     return {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
-            "traffic_source": "separate ncu capture of spmv4_f32_kernel on pipe8m (1.063-1.067 x algorithmic)"
+            "traffic_source": "separate ncu capture of spmv4_f32_kernel on pipe8m (1.043-1.046 x algorithmic)"
             if traffic else None, "launch_ms": ms,
             "algorithmic_bytes": bytes_, "launches_timed": reps}
 
 
 BLOCKS_PIPE8M = 20334561
-TRAFFIC_SPMV4_F32_PIPE8M = 1.5245e9
+TRAFFIC_SPMV4_F32_PIPE8M = 1.4954e9
 
 
 def kernel_breakdown(step_fn, path):

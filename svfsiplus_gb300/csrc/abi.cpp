@@ -449,7 +449,6 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32, int kind) {
   const int sD = kw.sD;
   double* hraw = kw.givens.p + 4 * sD + 1;
   if (ctx->amg) ctx->amg->gnn_smoother = kind == 4 && ctx->gnn;
-  const bool half = ctx->krylov_half && ctx->amg && ctx->amg_val0 == Val32 && ctx->amg->val0h.p;
   for (int i = 0; i < sD; i++) {
     float* ui = kw.V32.p + (long)i * n;
     float* ui1 = kw.V32.p + (long)(i + 1) * n;
@@ -460,10 +459,7 @@ void enqueue_cycle_flex(svgpu_ctx* ctx, const float* Val32, int kind) {
     else
       amg_vcycle(ctx, ui, zi, kw.flags.p);
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_SPMV);
-    if (half)
-      amg_spmv_h(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, ctx->amg->val0h.p, zi, ui1, kw.flags.p);
-    else
-      launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
+    launch_spmv4_f32(ctx->stream, ctx->nNo, ctx->rowPtr.p, ctx->colPtr.p, Val32, zi, ui1, kw.flags.p);
     add_coupled32(ctx, zi, ui1, kw.flags.p);
     if (!ctx->use_graphs) phase_mark(ctx, PH_CYC_ORTHO);
     const int ctas = launch_multidot32(ctx->stream, n, i + 2, kw.V32.p, n, ui1, kw.partial.p, ctx->sm_count,
@@ -1156,7 +1152,6 @@ int svgpu_create(svgpu_ctx** out, int device) {
   }
   cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (const char* g = std::getenv("SVGPU_GRAPHS")) ctx->use_graphs = std::strcmp(g, "0") != 0;
-  if (const char* g = std::getenv("SVGPU_KRYLOV_HALF")) ctx->krylov_half = std::strcmp(g, "0") != 0;
   if (ctx->errflag.resize(2) != cudaSuccess) {
     delete ctx;
     return SVGPU_ECUDA;

@@ -71,9 +71,6 @@ void amg_to_half(cudaStream_t s, long m, const float* v, uint16_t* h);
 // r = b - A x with an FP16 block matrix
 void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
                     const float* b, float* r, const int* flags);
-// y = A x with the FP16 copy of the finest level's matrix
-void amg_spmv_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
-                float* y, const int* flags);
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags);
 void amg_prolong_add(cudaStream_t s, int n, const int* agg, const float* xc, float* x, const int* flags);

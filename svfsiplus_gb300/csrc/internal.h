@@ -259,7 +259,6 @@ struct svgpu_ctx {
   // restart cycles as CUDA graphs (default) or as individual launches (environment
   // SVGPU_GRAPHS=0 at context creation: per-kernel profilers see plain launches)
   bool use_graphs = true;
-  bool krylov_half = false;  // the flexible cycles' Krylov product with the V-cycle's FP16 matrix
   // multilevel preconditioner options (svgpu_multilevel_options)
   float ml_omega = 0.7f;
   int ml_coarse_sweeps = 30;

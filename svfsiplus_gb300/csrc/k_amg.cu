@@ -113,8 +113,8 @@ __global__ void to_half_kernel(long m, const float* __restrict__ v, __half* __re
     h[k] = __float2half_rn(fminf(fmaxf(v[k], -65504.f), 65504.f));
 }
 
-// r = b - A x with the FP16 matrix (r = A x when b is null), FP32 accumulation; 4
-// lanes per block row, each taking whole blocks (bsr4_row).
+// r = b - A x with the FP16 matrix, FP32 accumulation; 4 lanes per block row, each
+// taking whole blocks (bsr4_row).
 __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __restrict__ rowPtr,
                                                          const int* __restrict__ colPtr,
                                                          const __half* __restrict__ val,
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256) spmv_res_h_kernel(int n, const int* __res
   const int q = (int)(t & 3);
   const bool live = row < n;
   const float acc = bsr4_row<BSR4_U_F16>(live, row, q, rowPtr, colPtr, Bsr4F16{val}, x);
-  if (live) r[4 * row + q] = b ? b[4 * row + q] - acc : acc;
+  if (live) r[4 * row + q] = b[4 * row + q] - acc;
 }
 
 
@@ -259,12 +259,6 @@ void amg_spmv_res_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr,
       n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, b, r, flags);
 }
 
-
-void amg_spmv_h(cudaStream_t s, int n, const int* rowPtr, const int* colPtr, const uint16_t* val, const float* x,
-                float* y, const int* flags) {
-  spmv_res_h_kernel<<<(unsigned)((4L * n + 255) / 256), 256, 0, s>>>(
-      n, rowPtr, colPtr, reinterpret_cast<const __half*>(val), x, nullptr, y, flags);
-}
 
 void amg_restrict(cudaStream_t s, int nc, const int* aggPtr, const int* aggList, const float* r, float* bc,
                   const int* flags) {
