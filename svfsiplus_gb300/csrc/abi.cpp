@@ -1065,13 +1065,28 @@ int svgpu::solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int
 }
 
 int svgpu::solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
-                       const double* res) {
-  return solve_device_mixed(ctx, R, Val32, incL, st, res);
+                       const double* res, bool reuse) {
+  return solve_device_mixed(ctx, R, Val32, incL, st, res, reuse);
 }
 
 svgpu::FluidConsts svgpu::fluid_consts_of(const svgpu_fluid_props* p) { return fluid_consts(p); }
 
 namespace svgpu {
+
+int construct_mesh_residual(svgpu_ctx* ctx, double E, double nu, double rho, double dt, double am, double af,
+                            double beta, int tDof, int s, const double* Ag, const double* Dg, const double* Do,
+                            double* R) {
+  if (s < 0 || s + 3 > tDof) return set_err(ctx, SVGPU_EINVAL, "construct_mesh: bad rows");
+  const MeshConsts c{E, nu, rho, dt, am, af, beta};
+  MeshData& m = *ctx->mesh;
+  SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->errflag.p, 0, 2 * sizeof(int), ctx->stream));
+  for (size_t k = 0; k + 1 < m.color_start.size(); k++) {
+    launch_mesh_assembly(ctx->stream, c, m.color_start[k], m.color_start[k + 1] - m.color_start[k], m.ien.p, m.boff.p,
+                         m.elem_id.p, m.x4.p, tDof, s, Ag, Dg, Do, ctx->rowPtr.p, R, nullptr, ctx->errflag.p);
+    ctx->launches++;
+  }
+  return check_errflag(ctx);
+}
 
 SolidConsts solid_consts(const svgpu_solid_props* sp) {
   SolidConsts c;

@@ -228,6 +228,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
   int itr[2] = {0, 0};
   bool ok[2] = {false, false};
   int cEq = 0, total = 0;
+  bool mesh_kept = false;  // the mesh context holds this step's scaled, set-up mesh tangent
   const int cap = opts->maxItr[0] + opts->maxItr[1];
   rc = SVGPU_OK;
   for (;;) {
@@ -279,26 +280,39 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
                          w.Dn.p);
       ctx->launches++;
     } else {
+      // The mesh equation's tangent depends only on the configuration x + Do at the start
+      // of the step (mesh.cpp:124-130) and on constants, so the mixed multilevel path
+      // assembles, pads, scales and sets it up at the step's first mesh iteration and
+      // keeps it for the later ones, which assemble the residual rows alone.  The kept
+      // tangent is the one the reference reassembles, so the iteration is unchanged.
+      const bool ml = mixed && opts->lsType[1] == SVGPU_LS_GMRES;
+      const bool keep = ml && mesh_kept;
       SVGPU_CUDA(ctx, cudaMemsetAsync(w.R3.p, 0, 3L * nNo * sizeof(double), ctx->stream));
-      SVGPU_CUDA(ctx, cudaMemsetAsync(w.Val9.p, 0, (size_t)9 * ctx->nnz * sizeof(double), ctx->stream));
-      rc = svgpu_construct_mesh(ctx, props->mesh_E, props->mesh_nu, props->mesh_rho, dt, am[1], af[1], beta[1], 7, 4,
-                                w.Ag.p, w.Dg.p, w.Do.p, w.R3.p, w.Val9.p);
+      if (keep) {
+        rc = construct_mesh_residual(ctx, props->mesh_E, props->mesh_nu, props->mesh_rho, dt, am[1], af[1], beta[1], 7,
+                                     4, w.Ag.p, w.Dg.p, w.Do.p, w.R3.p);
+      } else {
+        SVGPU_CUDA(ctx, cudaMemsetAsync(w.Val9.p, 0, (size_t)9 * ctx->nnz * sizeof(double), ctx->stream));
+        rc = svgpu_construct_mesh(ctx, props->mesh_E, props->mesh_nu, props->mesh_rho, dt, am[1], af[1], beta[1], 7,
+                                  4, w.Ag.p, w.Dg.p, w.Do.p, w.R3.p, w.Val9.p);
+      }
       if (rc) break;
-      if (mixed && opts->lsType[1] == SVGPU_LS_GMRES) {
+      if (ml) {
         // mixed precision with the multilevel FGMRES, on the system padded to 4x4 blocks
         if ((rc = mesh_context(ctx, opts, w))) break;
         svgpu_ctx* mc = w.mctx.get();
-        launch_pad_mesh_system(ctx->stream, nNo, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, w.Val9.p, w.R3.p,
-                               mc->Val32.p, mc->R.p);
-        ctx->launches += 2;
+        launch_pad_mesh_system(ctx->stream, nNo, ctx->nnz, ctx->blkRow.p, ctx->colPtr.p, keep ? nullptr : w.Val9.p,
+                               w.R3.p, mc->Val32.p, mc->R.p);
+        ctx->launches += keep ? 1 : 2;
         const long long l0 = mc->launches;
         mc->hist_slot = itr[1] - 1 < kHistSlots ? itr[1] - 1 : -1;
-        rc = solve_mixed(mc, mc->R.p, mc->Val32.p, opts->incL[1], &st);
+        rc = solve_mixed(mc, mc->R.p, mc->Val32.p, opts->incL[1], &st, nullptr, keep);
         ctx->launches += mc->launches - l0;
         if (rc) {
           rc = set_err(ctx, rc, std::string("fsi_step (mesh solver): ") + mc->err);
           break;
         }
+        mesh_kept = true;
         launch_unpad_vec(ctx->stream, nNo, mc->R.p, w.R3.p);
         ctx->launches++;
       } else {

@@ -439,9 +439,14 @@ int ns_solve_device(svgpu_ctx* ctx, const double* Val, double* R, svgpu_ls_stats
 int solve_fp64(svgpu_ctx* ctx, int dof, double* R, double* Val, const int* incL, svgpu_ls_stats* st,
                const double* res = nullptr);
 // the mixed-precision solve of a dof-4 system with an FP32 tangent (abi.cpp), with the
-// context's solver mode
+// context's solver mode; reuse: Val32 is the tangent an earlier solve of this context
+// already scaled and set up (only R is scaled)
 int solve_mixed(svgpu_ctx* ctx, double* R, float* Val32, const int* incL, svgpu_ls_stats* st,
-                const double* res = nullptr);
+                const double* res = nullptr, bool reuse = false);
+// the residual rows alone of construct_mesh (svgpu_construct_mesh's R, no tangent)
+int construct_mesh_residual(svgpu_ctx* ctx, double E, double nu, double rho, double dt, double am, double af,
+                            double beta, int tDof, int s, const double* Ag, const double* Dg, const double* Do,
+                            double* R);
 // k_cg.cu / cg.cpp: conjugate gradients (cgrad_v)
 int cg_parts(long n);
 void launch_cg_iteration(cudaStream_t s, int nNo, int dof, const int* rowPtr, const int* colPtr, const double* K,
@@ -597,6 +602,7 @@ void launch_fsi_correct(cudaStream_t s, int nNo, double c0, double c1, const dou
                         double* An, double* Yn, double* Dn);
 void launch_mesh_correct(cudaStream_t s, int nNo, double c0, double c1, const double* R, double* An, double* Yn,
                          double* Dn);
+// Val9 == nullptr pads the residual alone
 void launch_pad_mesh_system(cudaStream_t s, int nNo, long nnz, const int* blkRow, const int* colPtr,
                             const double* Val9, const double* R3, float* Val16, double* R4);
 void launch_unpad_vec(cudaStream_t s, int nNo, const double* R4, double* R3);

@@ -135,7 +135,7 @@ __global__ void unpad_vec_kernel(int nNo, const double* __restrict__ R4, double*
 
 void launch_pad_mesh_system(cudaStream_t s, int nNo, long nnz, const int* blkRow, const int* colPtr,
                             const double* Val9, const double* R3, float* Val16, double* R4) {
-  pad_mesh_matrix_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, Val9, Val16);
+  if (Val9) pad_mesh_matrix_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, Val9, Val16);
   pad_vec_kernel<<<(nNo + 255) / 256, 256, 0, s>>>(nNo, R3, R4);
 }
 

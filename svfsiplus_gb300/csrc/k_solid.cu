@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(128) mesh_p1_kernel(MeshConsts c, int e0, int 
     double* Ra = R + 3L * nd[a];
     for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
   }
+  if (!Val) return;  // residual rows only
   for (int a = 0; a < 4; a++) {
     const int rowbase = rowPtr[nd[a]];
     for (int b = 0; b < 4; b++) {

@@ -106,3 +106,29 @@ def test_reuse_tangent_reaches_the_reference_solution(golden):
         assert st[-1]["iNorm"] / st[0]["iNorm"] <= 1e-10 * 10
         assert ev <= 1e-6 and ep <= 1e-6
     s.ctx.close()
+
+
+@pytest.mark.parametrize("mode,sD", [(2, 20), (2, 150), (2, 250), (0, 120)])
+def test_krylov_dimensions_match_reference(golden, mode, sD):
+    """Restart lengths far from the reference's 50, on the small pipe: the FP32
+    Gram-Schmidt dots keep one shared-memory accumulator per basis vector (up to 256),
+    so a long cycle runs the dot kernel with up to 251 vectors and a short one with at
+    most 21.  (Much shorter restarts stagnate on this system: FGMRES(3) stalls near 5e-3
+    of the first residual.)
+    Mode 2 (multilevel FGMRES) and mode 0 (plain FP32 GMRES + diagonal, the mixed
+    path's first solver) reach the reference's fields within 1e-6 after 2 steps."""
+    g = golden("small")
+    m = named_pipe("small")
+    ps = eval(str(g["params"]))
+    s = api.PipeFluidSolver(m, sD=sD, mItr=4000 // sD, relTol=ps["ls_rel_tol"], absTol=ps["ls_abs_tol"],
+                            newton_min=ps["newton_min"], newton_max=ps["newton_max"], newton_tol=ps["newton_tol"],
+                            precision=api.SVGPU_MIXED)
+    s.ctx.set_solver_mode(mode)
+    for step in (1, 2):
+        st = s.step(u_mean=ps["u_mean"], u_amp=ps["u_amp"], freq=ps["u_freq"])
+        assert all(x["suc"] for x in st), (sD, step, st)
+        ref = g[f"Yn_{step}"]
+        ev, ep = rel(s.Yn[:, :3], ref[:, :3]), rel(s.Yn[:, 3], ref[:, 3])
+        print("mode", mode, "sD", sD, "step", step, "its", [x["itr"] for x in st], "rel", ev, ep)
+        assert ev <= 1e-6 and ep <= 1e-6
+    s.ctx.close()
