@@ -944,7 +944,8 @@ def run_fsi(args):
     nsteps = args.warmup + args.steps
     out = {"workload": name, "tets": mesh.nEl, "solid_tets": int((mesh.eid == 2).sum()), "nodes": mesh.nNo,
            "blocks": int(colPtr.size), "warmup": args.warmup, "steps": args.steps,
-           "newton_tol": NEWTON_TOL, "fsi_lin_rel_tol": LIN_REL_TOL, "mesh_rel_tol": args.mesh_cg_tol}
+           "newton_tol": NEWTON_TOL, "fsi_lin_rel_tol": LIN_REL_TOL, "mesh_rel_tol": args.mesh_cg_tol,
+           "fsi_tangent_kept_within_step": bool(REUSE_TANGENT)}
     solid = np.zeros(mesh.nNo, bool)
     solid[mesh.ien[mesh.eid == 2].ravel()] = True
     paths = ["fp64", "learned", "history", "multilevel"] + (["plain"] if args.fsi_plain else [])
@@ -959,6 +960,9 @@ def run_fsi(args):
                               cg=(mesh_tol, 1e-17, 5000), rowPtr=rowPtr, colPtr=colPtr,
                               precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
                               mesh_gmres=(mesh_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM) if path != "plain" else None)
+        # the mixed paths keep the FSI equation's tangent within a step, as the fluid
+        # path keeps its own (svgpu_fsi_opts.reuse_tangent; --reuse-tangent 0 turns it off)
+        s.opts.reuse_tangent = int(mixed and REUSE_TANGENT)
         mode = {"fp64": 2, "learned": 5, "history": 5, "multilevel": 2, "plain": 0}[path]
         if path == "learned":
             s.ctx.gnn_create(api.pipe_node_features(mesh), 1)

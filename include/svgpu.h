@@ -450,6 +450,14 @@ typedef struct {
    * blocks (a fourth unknown with a unit diagonal), in a solver context of its own on
    * the same stream; a mesh equation set to CG keeps the reference's FP64 CG. */
   int precision;
+  /* SVGPU_MIXED only, no reference counterpart: 1 assembles the FSI equation's tangent
+   * (and its scaling and multilevel set-up) at the step's first FSI iteration and keeps
+   * it for the later ones, which assemble the residual rows alone (a modified Newton
+   * iteration, as svgpu_newton_opts.reuse_tangent); an FSI iteration with the kept
+   * tangent that lowers the residual less than tenfold makes the next one reassemble it.
+   * 0: every iteration, as the reference.  (The mesh equation's tangent, which depends
+   * only on the step's start, is kept within a step on the mixed path either way.) */
+  int reuse_tangent;
 } svgpu_fsi_opts;
 
 /* Strong Dirichlet values of one equation: n nodes, Y and A values (3, n) for the

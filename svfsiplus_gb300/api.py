@@ -94,7 +94,7 @@ class FsiOpts(C.Structure):
     _fields_ = [("minItr", C.c_int * 2), ("maxItr", C.c_int * 2), ("tol", C.c_double * 2), ("lsType", C.c_int * 2),
                 ("relTol", C.c_double * 2), ("absTol", C.c_double * 2), ("lsMaxItr", C.c_int * 2),
                 ("dimKry", C.c_int * 2), ("incL", C.c_void_p * 2), ("outletFace", C.c_int), ("outletH", C.c_double),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("reuse_tangent", C.c_int)]
 
 
 class DirichletSet(C.Structure):

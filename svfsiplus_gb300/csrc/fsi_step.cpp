@@ -229,6 +229,8 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
   bool ok[2] = {false, false};
   int cEq = 0, total = 0;
   bool mesh_kept = false;  // the mesh context holds this step's scaled, set-up mesh tangent
+  bool reuse_fsi = false, refresh_fsi = false;  // FSI tangent kept / to be reassembled
+  double prev_fsi_iN = 0.0;
   const int cap = opts->maxItr[0] + opts->maxItr[1];
   rc = SVGPU_OK;
   for (;;) {
@@ -242,7 +244,12 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     if (cEq == 0) {
       // ls_alloc zeroes R and Val (ls.cpp:51-61); construct_fsi + the outlet's Neumann term
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, 4L * nNo * sizeof(double), ctx->stream));
-      if (mixed_asm) {
+      // modified Newton (opts->reuse_tangent): the tangent of the step's first FSI
+      // iteration, its scaling and multilevel set-up serve the later iterations
+      reuse_fsi = opts->reuse_tangent && mixed_asm && itr[0] > 1 && !refresh_fsi;
+      if (mixed_asm && reuse_fsi) {  // residual rows alone
+        if ((rc = construct_fsi_mixed_device(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, nullptr))) break;
+      } else if (mixed_asm) {
         // residual rows in double-word FP32 (fluid) and FP64 (solid), tangent in FP32
         SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->Val32.p, 0, (size_t)16 * ctx->nnz * sizeof(float), ctx->stream));
         if ((rc = construct_fsi_mixed_device(ctx, &fp, &sp, 7, w.Ag.p, w.Yg.p, w.Dg.p, ctx->R.p, ctx->Val32.p)))
@@ -258,7 +265,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
           launch_neu_backflow_ale(ctx->stream, fc, opts->outletH, f.color_start[k],
                                   f.color_start[k + 1] - f.color_start[k], f.fien.p, f.inner.p, f.boff.p, m.x4.p, 7,
                                   w.Yg.p, w.Do.p, ctx->rowPtr.p, ctx->R.p, mixed_asm ? nullptr : ctx->Val.p,
-                                  mixed_asm ? ctx->Val32.p : nullptr);
+                                  mixed_asm && !reuse_fsi ? ctx->Val32.p : nullptr);
           ctx->launches++;
         }
       }
@@ -269,7 +276,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
       if (mixed) {
         const int slot0 = ctx->hist_slot;  // the equation's Newton iteration is the history slot
         ctx->hist_slot = itr[0] - 1 < kHistSlots ? itr[0] - 1 : -1;
-        rc = solve_mixed(ctx, ctx->R.p, ctx->Val32.p, opts->incL[0], &st);
+        rc = solve_mixed(ctx, ctx->R.p, ctx->Val32.p, opts->incL[0], &st, nullptr, reuse_fsi);
         ctx->hist_slot = slot0;
       } else {
         rc = solve_fp64(ctx, 4, ctx->R.p, ctx->Val.p, opts->incL[0], &st);
@@ -339,6 +346,10 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
                l4 = itr[cEq] >= opts->minItr[cEq];
     if (l1 || ((l2 || l3) && l4)) ok[cEq] = true;
     if (ok[0] && ok[1]) break;
+    if (cEq == 0) {  // a kept FSI tangent serves while every iteration lowers the residual tenfold
+      refresh_fsi = reuse_fsi && iN > 0.1 * prev_fsi_iN;
+      prev_fsi_iN = iN;
+    }
     // both equations are coupled: the next one in turn (pic.cpp:292-318)
     cEq = (cEq + 1) % 2;
   }

@@ -337,7 +337,8 @@ struct svgpu_ctx {
 namespace svgpu {
 
 // The FSI equation's system in mixed precision on device arrays (construct_fsi's
-// fluid and solid elements): adds into R (4, nNo, FP64) and Val32.
+// fluid and solid elements): adds into R (4, nNo, FP64) and Val32 (the residual rows
+// alone when Val32 is null).
 int construct_fsi_mixed_device(svgpu_ctx* ctx, const svgpu_fluid_props* fp, const svgpu_solid_props* sp, int ld,
                                const double* Ag, const double* Yg, const double* Dg, double* R, float* Val32);
 
@@ -543,7 +544,7 @@ void launch_to_dw(cudaStream_t s, long n, const double* a, float2* b);
 void launch_to_dw_ale(cudaStream_t s, int nNo, int ld, const double* x4, const double* Ag, const double* Yg,
                       const double* Dg, float2* xw, float2* Agw, float2* Ygw, float2* Ymw);
 // Mixed-precision ALE fluid elements of the FSI equation: residual rows in double-word
-// FP32 into dws.R, tangent blocks in FP32 into Val32.
+// FP32 into dws.R, tangent blocks in FP32 into Val32 (none when Val32 is null).
 void launch_fluid_ale_mixed(cudaStream_t s, const FluidConsts& c, int e0, int ne, const int* ien, const uint8_t* boff,
                             const int* elem_id, const double* x4, int ld, const double* Ag, const double* Yg,
                             const double* Dg, const int* rowPtr, float* Val32, int* errflag, const DwState& dws);

@@ -852,8 +852,9 @@ void launch_fluid_ale_mixed(cudaStream_t s, const FluidConsts& c, int e0, int ne
   const int grid = (ne + 127) / 128;
   fluid_res_dw_kernel<true><<<(ne + RDW_BLOCK - 1) / RDW_BLOCK, RDW_BLOCK, 0, s>>>(c, e0, ne, ien, elem_id, nullptr,
                                                                                   errflag, dws);
-  fluid_p1_kernel<float, float, false, true, true><<<grid, 128, 0, s>>>(
-      c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, nullptr, rowPtr, nullptr, Val32, errflag, ld, Dg);
+  if (Val32)
+    fluid_p1_kernel<float, float, false, true, true><<<grid, 128, 0, s>>>(
+        c, e0, ne, ien, boff, elem_id, x4, Ag, Yg, nullptr, rowPtr, nullptr, Val32, errflag, ld, Dg);
 }
 
 void launch_neu_backflow(cudaStream_t s, const FluidConsts& c, double h, int e0, int ne,

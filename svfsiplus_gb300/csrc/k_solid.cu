@@ -134,9 +134,9 @@ __global__ void __launch_bounds__(128) struct_p1_kernel(SolidConsts c, int e0, i
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) S[i][j] = J2d * g1 * (i == j ? 1.0 : 0.0) - r1 * Ci[i][j];
   const int vi[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
-  double Dm[6][6];
+  double Dm[6][6];  // the tangent's material part (not needed for the residual rows alone)
   const double c1 = 2.0 * (r1 - p * J), c2 = pl * J - 2.0 * r1 / 3.0;
-  for (int a = 0; a < 6; a++)
+  for (int a = 0; a < 6 && Val; a++)
     for (int b = 0; b < 6; b++) {
       const int i = vi[a][0], j = vi[a][1], k = vi[b][0], l = vi[b][1];
       Dm[a][b] = (-2.0 / 3.0) * (Ci[i][j] * S[k][l] + S[i][j] * Ci[k][l]) +
@@ -176,6 +176,7 @@ __global__ void __launch_bounds__(128) struct_p1_kernel(SolidConsts c, int e0, i
     double* Ra = R + (long)DOF * nd[a];
     for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
   }
+  if (!Val) return;  // residual rows only
   // tangent: w * sum_g [ amd N_a N_b delta_ij + afu (Nx_a S Nx_b delta_ij + Bm_a^T Dm Bm_b) ]
   double Bm[4][6][3];
   for (int a = 0; a < 4; a++)

@@ -256,3 +256,36 @@ def test_gpu_fsi_steps_mixed_multilevel_mesh_equation(golden, mode):
         print("step", step, "mesh Krylov its", mesh_its, {k: f"{v:.2e}" for k, v in errs.items()})
         assert max(errs.values()) <= 1e-6, errs
     s.ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fsi_kept_tangent_reaches_the_same_solution(golden):
+    """svgpu_fsi_opts.reuse_tangent = 1 (the FSI equation's tangent of a step's first
+    iteration kept for the later ones, residual rows reassembled every iteration) changes
+    the path of the Newton iteration, not its fixed point: with both equations driven to
+    picc's 1e-10 (at most 12 iterations each), 3 steps of the mixed multilevel path with
+    and without the kept tangent agree within 1e-8 per field."""
+    from svfsiplus_gb300 import api
+    g = golden("fsi_run_small")
+    ps = _run_params(g)
+    m = named_pipe("fsi_small")
+    p = api.fsi_props(ps["rho_f"], ps["mu"], ps["backflow_beta"], ps["rho_s"], ps["E"], ps["nu"], ps["dt"],
+                      ps["rho_inf"], ps["mesh_E"], ps["mesh_nu"], ps["mesh_rho"])
+    out = {}
+    for reuse in (0, 1):
+        s = api.PipeFsiSolver(m, p, newton=(1, 12, 1e-10), mesh_newton=(1, 12, 1e-10),
+                              gmres=(1e-4, 1e-17, 100, 50), precision=api.SVGPU_MIXED,
+                              mesh_gmres=(1e-6, 1e-17, 100, 50))
+        s.opts.reuse_tangent = reuse
+        s.ctx.set_solver_mode(2)
+        its = []
+        for step in (1, 2, 3):
+            st = s.step(ps["u_mean"], ps["u_amp"], ps["u_freq"])
+            assert all(d["suc"] == 1 for _, d in st)
+            its.append(sum(1 for q, _ in st if q == 0))
+        out[reuse] = (s.Yn.copy(), s.Dn.copy(), its)
+        s.ctx.close()
+    (Y0, D0, i0), (Y1, D1, i1) = out[0], out[1]
+    errs = {"velocity and pressure": rel(Y1[:, :4], Y0[:, :4]), "displacements": rel(D1[:, :7], D0[:, :7])}
+    print("FSI Newton iterations per step, reassembled / kept:", i0, i1, {k: f"{v:.2e}" for k, v in errs.items()})
+    assert max(errs.values()) <= 1e-8, errs
