@@ -501,13 +501,29 @@ __global__ void diag_w32_kernel(int nNo, const int* __restrict__ diagPtr, const 
   W[t] = w;
 }
 
+// Val_k <- diag(W_row) Val_k diag(W_col) for the FP32 tangent, one thread per block:
+// the two 4-entry slices of W rounded to FP32 once, then 32 FP32 multiplies (the FP32
+// result of the FP64 product would differ by at most a few ulp; FP64 arithmetic on the
+// 1/64-rate FP64 pipe made this kernel 2.4 ms per tangent at 8M tets)
 __global__ void scale_val32_kernel(long nnz, const int* __restrict__ blkRow, const int* __restrict__ colPtr,
                                    const double* __restrict__ W, float* __restrict__ Val) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nnz * 16) return;
-  const long k = t >> 4;
-  const int r = (int)((t >> 2) & 3), c = (int)(t & 3);
-  Val[t] = (float)(((double)Val[t] * W[4L * blkRow[k] + r]) * W[4L * colPtr[k] + c]);
+  const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  const double2* wr = reinterpret_cast<const double2*>(W + 4L * blkRow[k]);
+  const double2* wc = reinterpret_cast<const double2*>(W + 4L * colPtr[k]);
+  const double2 r01 = wr[0], r23 = wr[1], c01 = wc[0], c23 = wc[1];
+  const float r[4] = {(float)r01.x, (float)r01.y, (float)r23.x, (float)r23.y};
+  const float4 c = make_float4((float)c01.x, (float)c01.y, (float)c23.x, (float)c23.y);
+  float4* v = reinterpret_cast<float4*>(Val + 16 * k);
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    float4 b = v[q];
+    b.x = b.x * r[q] * c.x;
+    b.y = b.y * r[q] * c.y;
+    b.z = b.z * r[q] * c.z;
+    b.w = b.w * r[q] * c.w;
+    v[q] = b;
+  }
 }
 
 // y = K x, FP32 matrix and vectors, FP32 accumulation; 4 lanes per block row, each
@@ -626,15 +642,17 @@ __global__ void __launch_bounds__(256) multidot32_kernel(long n, int m, const fl
   }
 }
 
-// Partial <V_j, w>, j < m <= MDW_MAXM, over FP32 vectors read as float4.  Each CTA
-// owns one contiguous range of the vectors (equal shares), walked in tiles of
-// MDW_T x 256 float4: the tile of w stays in registers (MDW_T float4 per thread) while
-// one pass over the m basis vectors streams their tiles with MDW_U x MDW_T loads in
-// flight per thread.  Per vector and tile a warp sums its 32 x MDW_T x 4 products in
-// FP32 (a shuffle tree) and adds the sum in FP64 to its own shared-memory accumulator;
-// the CTA's warps are summed in FP64 at the end, in a fixed order (deterministic).
-// w is read once per launch instead of once per group of vectors.
-constexpr int MDW_T = 4, MDW_U = 4, MDW_MAXM = 256;
+// Partial <V_j, w>, j < m <= MDW_MAXM, over FP32 vectors read as float4.  The vectors
+// are cut into tiles of MDW_T x 256 float4, dealt to the CTAs in turn (CTA b takes
+// tiles b, b + gridDim.x, ...), so that at any moment the CTAs read one compact window
+// of every vector; per tile the tile of w stays in registers (MDW_T float4 per thread)
+// while one pass over the m basis vectors streams their tiles with MDW_U x MDW_T loads
+// in flight per thread.  With 4 CTAs per SM an 8M-tet pipe's vectors give each CTA
+// 2.9 tiles of 3 x 256 float4.  Per vector and tile a warp sums its 32 x MDW_T x 4
+// products in FP32 (a shuffle tree) and adds the sum in FP64 to its own shared-memory
+// accumulator; the CTA's warps are summed in FP64 at the end, in a fixed order
+// (deterministic).  w is read once per launch instead of once per group of vectors.
+constexpr int MDW_T = 3, MDW_U = 4, MDW_MAXM = 256;
 
 __global__ void __launch_bounds__(256) multidot32w_kernel(long n4, int m, const float4* __restrict__ V, long ldv4,
                                                           const float4* __restrict__ w, double* __restrict__ partial,
@@ -644,17 +662,14 @@ __global__ void __launch_bounds__(256) multidot32w_kernel(long n4, int m, const 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = lane; j < m; j += 32) red[warp][j] = 0.0;
   __syncwarp();
-  const long share = (n4 + gridDim.x - 1) / gridDim.x;
-  const long beg = (long)blockIdx.x * share;
-  const long end = beg + share < n4 ? beg + share : n4;
   constexpr long tile = (long)MDW_T * 256;
-  for (long base = beg; base < end; base += tile) {
+  for (long base = (long)blockIdx.x * tile; base < n4; base += (long)gridDim.x * tile) {
     float4 wr[MDW_T];
     bool in[MDW_T];
 #pragma unroll
     for (int t = 0; t < MDW_T; t++) {
       const long k = base + (long)t * 256 + threadIdx.x;
-      in[t] = k < end;
+      in[t] = k < n4;
       wr[t] = in[t] ? w[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     for (int j0 = 0; j0 < m; j0 += MDW_U) {
@@ -803,7 +818,7 @@ void launch_diag_w32(cudaStream_t s, int nNo, const int* diagPtr, const float* V
 }
 
 void launch_scale_val32(cudaStream_t s, long nnz, const int* blkRow, const int* colPtr, const double* W, float* Val) {
-  scale_val32_kernel<<<(unsigned)((nnz * 16 + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, W, Val);
+  scale_val32_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, blkRow, colPtr, W, Val);
 }
 
 void launch_spmv4_f32(cudaStream_t s, int nNo, const int* rowPtr, const int* colPtr, const float* Val,
