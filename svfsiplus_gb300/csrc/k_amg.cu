@@ -182,8 +182,10 @@ __global__ void ap_values_kernel(int nb, const int* __restrict__ sumPtr, const i
 // Coarse correction and post-smoothing of the finest level in one pass:
 //   r' = r - (A P) xc            (from_zero: r' = b - (A P) xc)
 //   x <- x + P xc + omega D^-1 r'  (from_zero: x <- P xc + omega D^-1 r')
-// The product with the FP16 A P runs with 4 lanes per block row taking whole blocks
-// (bsr4_row; a row of A P has about 4 blocks), after which lane q holds r'_q; the 4
+// The product with the FP16 A P runs with 4 lanes per block row taking whole blocks,
+// one at a time (bsr4_row with U = 1: a row of A P has about 4 blocks, and the smaller
+// register count lets more warps hide the dependent index loads: 72 against 87 us at
+// 8M tets with two in flight), after which lane q holds r'_q; the 4
 // lanes of a row exchange their r' by shuffles and lane q applies row q of the node's
 // 4x4 inverse.  r' itself is not stored: nothing after the post-smoothing reads it.
 __global__ void __launch_bounds__(256) correct_smooth_kernel(int n, const int* __restrict__ apRow,
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(256) correct_smooth_kernel(int n, const int* _
     d = *reinterpret_cast<const float4*>(dinv + 16 * row + 4 * q);
     pc = xc[4L * agg[row] + q];
   }
-  const float rq = rin - bsr4_row<BSR4_U_F16>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
+  const float rq = rin - bsr4_row<1>(live, row, q, apRow, apCol, Bsr4F16{apVal}, xc);
   const int base = (int)(threadIdx.x & 31) & ~3;
   const float r0 = __shfl_sync(0xffffffffu, rq, base);
   const float r1 = __shfl_sync(0xffffffffu, rq, base + 1);
