@@ -355,7 +355,8 @@ long long svgpu_learned_rejects(const svgpu_ctx* ctx);
  * 7 right preconditioner (network, or the V-cycle's finest level), 8 operator product,
  * 9 Gram-Schmidt and Givens, 10 the V-cycle's coarse levels, 11 its two finest-level
  * products, 12 its finest-level restriction and prolongation (7 then keeps the
- * finest-level smoothing).  n: entries of ms / intervals (13); intervals may be NULL. */
+ * finest-level smoothing); 13 the mesh equation's assembly and solve in
+ * svgpu_fsi_step.  n: entries of ms / intervals (14); intervals may be NULL. */
 int svgpu_phase_timing(svgpu_ctx* ctx, int on);
 int svgpu_phase_times(svgpu_ctx* ctx, double* ms, long long* intervals, int n);
 

@@ -364,7 +364,8 @@ class Context:
         return int(lib().svgpu_learned_rejects(self._h))
 
     PHASES = ("assembly", "precond", "amg_setup", "learned_guess", "restart", "cycles", "other",
-              "cycle_precond", "cycle_spmv", "cycle_ortho", "cycle_coarse", "vcycle_spmv", "vcycle_transfer")
+              "cycle_precond", "cycle_spmv", "cycle_ortho", "cycle_coarse", "vcycle_spmv", "vcycle_transfer",
+              "mesh_equation")
 
     def phase_timing(self, on=True):
         self._check(lib().svgpu_phase_timing(self._h, int(bool(on))), "phase_timing")

@@ -240,7 +240,7 @@ extern "C" int svgpu_fsi_step(svgpu_ctx* ctx, const svgpu_fsi_props* props, cons
     ctx->launches++;
     svgpu_ls_stats st;
     std::memset(&st, 0, sizeof(st));
-    phase_mark(ctx, PH_ASSEMBLY);
+    phase_mark(ctx, cEq == 0 ? PH_ASSEMBLY : PH_MESH);
     if (cEq == 0) {
       // ls_alloc zeroes R and Val (ls.cpp:51-61); construct_fsi + the outlet's Neumann term
       SVGPU_CUDA(ctx, cudaMemsetAsync(ctx->R.p, 0, 4L * nNo * sizeof(double), ctx->stream));

@@ -191,7 +191,8 @@ enum Phase {
   PH_CYC_COARSE = 10,  // coarse levels of the V-cycle and the coarsest solve
   PH_VC_SPMV = 11,     // the V-cycle's two finest-level products (FP16 matrix)
   PH_VC_TRANSFER = 12, // the V-cycle's finest-level restriction and prolongation
-  PH_COUNT = 13
+  PH_MESH = 13,        // svgpu_fsi_step: the mesh equation's assembly and solve
+  PH_COUNT = 14
 };
 
 struct PhaseTimer {

@@ -151,7 +151,6 @@ __global__ void prolong_kernel(int n, const int* __restrict__ agg, const float* 
   x[t] += xc[4L * agg[i] + (t & 3)];
 }
 
-// y = A x, or with b given y = b - A x (the residual fused into the product)
 // y = A x or r = b - A x on the coarse levels (FP32 blocks), 4 lanes per block row
 // taking whole blocks (bsr4_row)
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict__ rowPtr,
