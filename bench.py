@@ -1109,7 +1109,11 @@ def run_long(args):
     """Several solver paths over many steps from rest, each with the headline's warm-up
     (and, for the learned path, its online training): per-path mean s per step
     (CUDA-synchronised host clock around every step), Krylov iterations per step, the
-    first Newton solve's iterations and its initial-guess residual."""
+    first Newton solve's iterations and its initial-guess residual.  With --long-error
+    the FP64 solution of the same steps (fp64_solution's settings: FP64 residual and
+    tangent, Newton to 1e-10) runs in lockstep from the same start, and every step's
+    per-field relative L2 difference is reported (computed on the device; the FP64
+    solver's time is not in mean_s)."""
     import torch
     from svfsiplus_gb300 import api
     from svfsiplus_gb300.mesh import named_pipe
@@ -1120,15 +1124,31 @@ def run_long(args):
     for path in args.paths.split(","):
         s, mode = make_solver(api, mesh, rowPtr, colPtr, path, 0)
         api.lib().svgpu_set_stream(s.ctx._h, api.C.c_void_p(stream.cuda_stream))
-        step, _ = device_stepper(api, s)
+        step, state = device_stepper(api, s)
+        ref = ref_state = ref_step = None
+        if args.long_error:
+            ref, _ = make_solver(api, mesh, rowPtr, colPtr, "multilevel", 0, newton_tol=1e-10, newton_max=14,
+                                 lin_rel_tol=1e-4, precision=api.SVGPU_FP64)
+            api.lib().svgpu_set_stream(ref.ctx._h, api.C.c_void_p(stream.cuda_stream))
+            ref_step, ref_state = device_stepper(api, ref)
+        ev, ep = [], []
+
+        def compare():
+            if ref_step is None:
+                return
+            ref_step()
+            a, b = state["Yo"], ref_state["Yo"]
+            ev.append(float(torch.linalg.norm(a[:, :3] - b[:, :3]) / torch.linalg.norm(b[:, :3])))
+            ep.append(float(torch.linalg.norm(a[:, 3] - b[:, 3]) / torch.linalg.norm(b[:, 3])))
         for k in range(args.warmup):
             step()
+            compare()
             if mode in (3, 4):
                 train_online(api, s)
         if mode in (3, 4):
             s.ctx.gnn_collect(False)
             s.ctx.set_solver_mode(mode)
-        its, k0, x0, secs = [], [], [], []
+        its, k0, x0, secs, newton = [], [], [], [], []
         for _ in range(args.long):
             torch.cuda.synchronize()
             t = time.perf_counter()
@@ -1136,14 +1156,24 @@ def run_long(args):
             torch.cuda.synchronize()
             secs.append(time.perf_counter() - t)
             its.append(sum(r["itr"] for r in q))
+            newton.append(len(q))
             k0.append(q[0]["itr"])
             x0.append(round(q[0]["x0_rel"], 3))
-        print(json.dumps({"workload": args.workload, "path": path, "solver_mode": mode, "steps": args.long,
-                          "warmup": args.warmup, "mean_s": float(np.mean(secs)), "krylov_its_total": int(sum(its)),
-                          "krylov_its": its, "first_solve_its": k0, "first_solve_x0_rel": x0,
-                          "guesses_tried_rejected_with_network": s.ctx.guess_stats if mode in (4, 5) else None,
-                          "s": [round(v, 3) for v in secs]}), flush=True)
+            compare()
+        rec = {"workload": args.workload, "path": path, "solver_mode": mode, "steps": args.long,
+               "warmup": args.warmup, "mean_s": float(np.mean(secs)), "krylov_its_total": int(sum(its)),
+               "krylov_its": its, "newton_iters": newton, "first_solve_its": k0, "first_solve_x0_rel": x0,
+               "guesses_tried_rejected_with_network": s.ctx.guess_stats if mode in (4, 5) else None,
+               "s": [round(v, 3) for v in secs]}
+        if ev:
+            rec["error_vs_fp64"] = {"velocity_rel_l2": [float("%.3g" % v) for v in ev],
+                                    "pressure_rel_l2": [float("%.3g" % v) for v in ep],
+                                    "max_velocity": max(ev), "max_pressure": max(ep),
+                                    "steps_compared": "all warm-up and timed steps, from rest"}
+        print(json.dumps(rec), flush=True)
         s.ctx.close()
+        if ref is not None:
+            ref.ctx.close()
         torch.cuda.empty_cache()
 
 
@@ -1257,6 +1287,8 @@ def main():
     ap.add_argument("--reuse-tangent", type=int, default=None,
                     help="1: mixed paths keep the tangent of a step's first Newton iteration (modified Newton)")
     ap.add_argument("--long", type=int, default=0, help="steps per path of a long run of --paths")
+    ap.add_argument("--long-error", action="store_true",
+                    help="--long: also run the FP64 solution in lockstep and report every step's error")
     ap.add_argument("--paths", default="multilevel,history,learned", help="--long: comma-separated paths")
     ap.add_argument("--increments", type=int, default=0,
                     help="steps from rest: compare the Newton increments of consecutive steps")
