@@ -918,6 +918,73 @@ def run_config1(args):
     print(json.dumps({"config1": {"gpu": config1_gpu(api), "cpu": config1_cpu()}}), flush=True)
 
 
+def fsi_solver(api, mesh, rowPtr, colPtr, path, args):
+    """The FSI pipe's solver for one path of run_fsi: fp64 (the FP64 solution: FP64
+    assembly, both Newton loops to 1e-10), learned / history / multilevel (mixed
+    precision, the headline's tolerances, both tangents kept within a step) or plain
+    (the reference's method); returns the solver and its first solver mode."""
+    tight = path == "fp64"
+    mixed = path in ("learned", "history", "multilevel")
+    newton = (1, 14, 1e-10) if tight else (1, NEWTON_MAX, NEWTON_TOL)
+    gm = (1e-4 if tight else LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM)
+    mesh_tol = 1e-6 if tight else args.mesh_cg_tol
+    s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=newton, mesh_newton=newton, gmres=gm,
+                          cg=(mesh_tol, 1e-17, 5000), rowPtr=rowPtr, colPtr=colPtr,
+                          precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
+                          mesh_gmres=(mesh_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM) if path != "plain" else None)
+    # the mixed paths keep the FSI equation's tangent within a step, as the fluid path
+    # keeps its own (svgpu_fsi_opts.reuse_tangent; --reuse-tangent 0 turns it off)
+    s.opts.reuse_tangent = int(mixed and REUSE_TANGENT)
+    mode = {"fp64": 2, "learned": 5, "history": 5, "multilevel": 2, "plain": 0}[path]
+    if path == "learned":
+        s.ctx.gnn_create(api.pipe_node_features(mesh), 1)
+        s.ctx.gnn_collect(2)
+    s.ctx.set_solver_mode(mode)
+    return s, mode
+
+
+def run_fsi_long(args):
+    """The learned FSI path over many steps (--fsi-long N after --warmup training steps)
+    with the FP64 solution of the same steps in lockstep from the same start: per step
+    the device time, the FSI Krylov iterations and the per-field relative L2 difference
+    (fluid velocity, pressure, solid and mesh displacement)."""
+    from svfsiplus_gb300 import api
+    from svfsiplus_gb300.mesh import named_pipe
+    name = args.workload if args.workload != WORKLOAD else "fsi5m"
+    mesh = named_pipe(name)
+    rowPtr, colPtr = api.csr_pattern(mesh.nNo, mesh.ien)
+    solid = np.zeros(mesh.nNo, bool)
+    solid[mesh.ien[mesh.eid == 2].ravel()] = True
+    s, _ = fsi_solver(api, mesh, rowPtr, colPtr, "learned", args)
+    ref, _ = fsi_solver(api, mesh, rowPtr, colPtr, "fp64", args)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+    err = {"velocity": [], "pressure": [], "solid_displacement": [], "mesh_displacement": []}
+    dev, its = [], []
+    for k in range(args.warmup + args.fsi_long):
+        if k == args.warmup:
+            s.ctx.gnn_collect(False)
+            s.ctx.set_solver_mode(4)
+        st = s.step(15.0, 5.0, 1.0)
+        if k >= args.warmup:
+            dev.append(s.ctx.step_device_ms() / 1e3)
+            its.append(sum(d["itr"] for q, d in st if q == 0))
+        elif s.ctx.gnn_pair_count() > 0:
+            s.ctx.gnn_train(TRAIN_ITERS, TRAIN_LR)
+        ref.step(15.0, 5.0, 1.0)
+        err["velocity"].append(rel(s.Yn[~solid, :3], ref.Yn[~solid, :3]))
+        err["pressure"].append(rel(s.Yn[:, 3], ref.Yn[:, 3]))
+        err["solid_displacement"].append(rel(s.Dn[solid, :3], ref.Dn[solid, :3]))
+        err["mesh_displacement"].append(rel(s.Dn[:, 4:7], ref.Dn[:, 4:7]))
+    print(json.dumps({"workload": name, "path": "learned", "warmup": args.warmup, "steps": args.fsi_long,
+                      "s_per_step": float(np.mean(dev)), "fsi_krylov_its": its,
+                      "guesses_tried_rejected_with_network": s.ctx.guess_stats,
+                      "error_vs_fp64": {k: {"max": max(v), "last": v[-1], "every_10": v[::10]}
+                                        for k, v in err.items()},
+                      "within_1e-6": bool(max(max(v) for v in err.values()) <= 1e-6)}), flush=True)
+    s.ctx.close()
+    ref.ctx.close()
+
+
 def run_fsi(args):
     """The coupled ALE FSI pipe (lumen + 1 mm neo-Hookean wall, linear-elastic mesh
     motion, pulsatile inflow 15 + 5 sin(2 pi t) cm/s), every path from rest over the same
@@ -951,23 +1018,7 @@ def run_fsi(args):
     paths = ["fp64", "learned", "history", "multilevel"] + (["plain"] if args.fsi_plain else [])
     fields = {}
     for path in paths:
-        tight = path == "fp64"
-        mixed = path in ("learned", "history", "multilevel")
-        newton = (1, 14, 1e-10) if tight else (1, NEWTON_MAX, NEWTON_TOL)
-        gm = (1e-4 if tight else LIN_REL_TOL, 1e-17, MAX_RESTARTS, KRYLOV_DIM)
-        mesh_tol = 1e-6 if tight else args.mesh_cg_tol
-        s = api.PipeFsiSolver(mesh, api.fsi_props(), newton=newton, mesh_newton=newton, gmres=gm,
-                              cg=(mesh_tol, 1e-17, 5000), rowPtr=rowPtr, colPtr=colPtr,
-                              precision=api.SVGPU_MIXED if mixed else api.SVGPU_FP64,
-                              mesh_gmres=(mesh_tol, 1e-17, MAX_RESTARTS, KRYLOV_DIM) if path != "plain" else None)
-        # the mixed paths keep the FSI equation's tangent within a step, as the fluid
-        # path keeps its own (svgpu_fsi_opts.reuse_tangent; --reuse-tangent 0 turns it off)
-        s.opts.reuse_tangent = int(mixed and REUSE_TANGENT)
-        mode = {"fp64": 2, "learned": 5, "history": 5, "multilevel": 2, "plain": 0}[path]
-        if path == "learned":
-            s.ctx.gnn_create(api.pipe_node_features(mesh), 1)
-            s.ctx.gnn_collect(2)
-        s.ctx.set_solver_mode(mode)
+        s, mode = fsi_solver(api, mesh, rowPtr, colPtr, path, args)
         steps, Ys, Ds = [], [], []
         for k in range(nsteps):
             if path == "learned" and k == args.warmup:
@@ -1276,6 +1327,9 @@ def main():
                     help="only the 50k-tet pipe at the reference's settings, 10 steps, GPU and CPU")
     ap.add_argument("--mesh-cg-tol", type=float, default=1e-3,
                     help="--fsi: relative tolerance of the mesh equation's solves")
+    ap.add_argument("--fsi-long", type=int, default=0,
+                    help="--fsi: the learned path over this many steps after --warmup training steps, "
+                         "the FP64 solution in lockstep")
     ap.add_argument("--fsi-plain", action="store_true",
                     help="--fsi: also the reference's method (FP64 GMRES + diagonal; about 12 s per step on fsi5m)")
     ap.add_argument("--tol-study", default=None,
@@ -1307,6 +1361,8 @@ def main():
         run_assembly_only(args)
     elif args.study:
         run_study(args)
+    elif args.fsi and args.fsi_long:
+        run_fsi_long(args)
     elif args.fsi:
         run_fsi(args)
     elif args.config1_only:
