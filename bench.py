@@ -275,8 +275,9 @@ def spmv_roofline(ctx, colPtr, nNo, mode, stream, reps=20):
     achieved = bytes_ / (ms * 1e-3) / 1e9
     # DRAM bytes per launch of this kernel on the 8M-tet pipe from one ncu capture of the
     # unchanged kernel (dram__bytes_read.sum + dram__bytes_write.sum, mean of six
-    # launches; the command is in profiles/spmv4_f32_pipe8m_traffic.md): ncu cannot run
-    # inside this timed program, so the capture is a separate run of the same kernel
+    # launches of `--study history --workload pipe8m --steps 1` with SVGPU_GRAPHS=0):
+    # ncu cannot run inside this timed program, so the capture is a separate run of the
+    # same kernel
     traffic = TRAFFIC_SPMV4_F32_PIPE8M if (mode >= 0 and colPtr.size == BLOCKS_PIPE8M) else None
     return {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
