@@ -1,7 +1,8 @@
 """The reference-side GPU back-end (svfsiplus_gb300/integration/GpuLinearAlgebra.{h,cpp},
 the LinearAlgebra subclass a reference build selects for this library): compiled
-against the reference's own headers (LinearAlgebra.h:40-63, FsilsLinearAlgebra's includes) and linked with the
-reference's objects and libsvgpu.so by oracle/build_ref.sh.  Runs where the reference
+against the reference's own headers (LinearAlgebra.h:40-63, FsilsLinearAlgebra's
+includes) and linked with the reference's objects and libsvgpu.so by
+oracle/build_ref.sh.  Runs where the reference
 tree exists (skipped elsewhere); the linked executable is run without arguments, which
 reports the link and touches no GPU."""
 import os
