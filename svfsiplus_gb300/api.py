@@ -652,8 +652,11 @@ class PipeFluidSolver:
         dirY, dirA = inflow(self.dir_prof, self.time, u_mean, u_amp, freq)
         stats = self.ctx.fluid_step(self.props, self.opts, dirY, dirA, self.Ao, self.Yo, self.Do,
                                     self.An, self.Yn, self.Dn, self.norms)
-        self.Ao[:] = self.An
-        self.Yo[:] = self.Yn
+        # the new state is the next step's old state: Ao/Yo become the same page-locked
+        # arrays as An/Yn instead of copies of them (fluid_step reads every input before
+        # it writes an output, so in and out may be one array)
+        self.Ao = self.An
+        self.Yo = self.Yn
         return stats
 
 
@@ -758,7 +761,8 @@ class PipeFsiSolver:
         zm = np.zeros((self.dirM.size, 3))
         stats = self.ctx.fsi_step(self.props, self.opts, (self.dirF, dY, dA), (self.dirM, zm, zm), self.Ao, self.Yo,
                                   self.Do, self.An, self.Yn, self.Dn, self.iNorm, self.pNorm)
-        self.Ao[:] = self.An
-        self.Yo[:] = self.Yn
-        self.Do[:] = self.Dn
+        # the new state becomes the old one by reference (see PipeFluidSolver.step)
+        self.Ao = self.An
+        self.Yo = self.Yn
+        self.Do = self.Dn
         return stats
