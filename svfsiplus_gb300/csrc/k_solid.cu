@@ -262,19 +262,15 @@ __global__ void __launch_bounds__(128) mesh_p1_kernel(MeshConsts c, int e0, int 
                        mu * ed[3], mu * ed[4], mu * ed[5]};
   double Nq[4][4];
   quad_N(Nq);
-  double lR[4][3], MN[4][4];
-  for (int a = 0; a < 4; a++) {
+  double lR[4][3];
+  for (int a = 0; a < 4; a++)
     for (int i = 0; i < 3; i++) lR[a][i] = 0.0;
-    for (int b = 0; b < 4; b++) MN[a][b] = 0.0;
-  }
   for (int g = 0; g < 4; g++) {
     double ud[3] = {0, 0, 0};
     for (int a = 0; a < 4; a++)
       for (int i = 0; i < 3; i++) ud[i] += Nq[g][a] * al[a][i];
-    for (int a = 0; a < 4; a++) {
+    for (int a = 0; a < 4; a++)
       for (int i = 0; i < 3; i++) lR[a][i] += w * c.rho * Nq[g][a] * ud[i];
-      for (int b = 0; b < 4; b++) MN[a][b] += Nq[g][a] * Nq[g][b];
-    }
   }
   for (int a = 0; a < 4; a++) {
     lR[a][0] += 4.0 * w * (Nx[0][a] * S[0] + Nx[1][a] * S[3] + Nx[2][a] * S[5]);
@@ -284,6 +280,13 @@ __global__ void __launch_bounds__(128) mesh_p1_kernel(MeshConsts c, int e0, int 
     for (int i = 0; i < 3; i++) Ra[i] += lR[a][i];
   }
   if (!Val) return;  // residual rows only
+  double MN[4][4];  // sum_g N_a N_b, for the tangent's mass part
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++) {
+      double m = 0.0;
+      for (int g = 0; g < 4; g++) m += Nq[g][a] * Nq[g][b];
+      MN[a][b] = m;
+    }
   for (int a = 0; a < 4; a++) {
     const int rowbase = rowPtr[nd[a]];
     for (int b = 0; b < 4; b++) {
