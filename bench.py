@@ -549,6 +549,19 @@ def headline_config(name, mesh, nNo, nblocks, world):
             "l2": "inputs larger than L2 (Val is 1.3-2.6 GB)", "parallelism": "replicas" if world > 1 else "1 GPU"}
 
 
+def max_over_ranks(v, device=None):
+    """The largest of every rank's v (the slowest replica's time, `bench.py --gpus N`
+    under torchrun); v itself without an initialised process group of more than one
+    rank.  device: where the reduction's tensor lives ("cuda" for NCCL, None for gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(v)
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args):
     import torch
     from svfsiplus_gb300 import api
@@ -583,11 +596,9 @@ def run_ours(args):
         rec = timed_steps(s, args.steps, keep_fields=args.error)
     launches = s.ctx.kernel_launches - launches0
     summ = step_summary(rec)
-    dev_s = summ["s_per_step"]
-    if world > 1:
-        t = torch.tensor([dev_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
+    # replicas: the slowest rank's times are the job's
+    dev_s = max_over_ranks(summ["s_per_step"], "cuda")
+    summ["e2e_s_per_step"] = max_over_ranks(summ["e2e_s_per_step"], "cuda")
     guesses = tuple(a - b for a, b in zip(s.ctx.guess_stats, guesses0))
     h2d = 3 * nNo * 4 * 8 + 2 * s.dir_nodes.size * 3 * 8
     d2h = 3 * nNo * 4 * 8
